@@ -1,0 +1,101 @@
+"""ctypes binding of the C ABI in include/hyperdeal_gb300.h.
+
+The shared library is built in-tree (hyperdeal_gb300/build.py).  There is no
+fallback: if the library cannot be loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+MAX_DIM = 6
+HD_OK, HD_ERR_INVALID, HD_ERR_UNSUPPORTED, HD_ERR_CUDA, HD_ERR_ALLOC, HD_ERR_DEVICE = range(6)
+HD_F64, HD_F32 = 0, 1
+HD_BC_HOMOGENEOUS, HD_BC_FUNCTION = 0, 1
+
+#: every symbol the C header declares
+EXPORTED_SYMBOLS = (
+    "hd_last_error", "hd_version", "hd_adv_create", "hd_adv_destroy", "hd_adv_n_dofs", "hd_adv_apply",
+    "hd_adv_critical_time_step", "hd_interpolate", "hd_norm_and_error", "hd_lsrk_create", "hd_lsrk_destroy",
+    "hd_lsrk_n_stages", "hd_lsrk_step", "hd_lsrk_step_unfused", "hd_lsrk_stage_update", "hd_lsrk_coefficients",
+)
+
+
+class HdError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("hyperdeal_gb300 error %d: %s" % (code, msg))
+        self.code = code
+
+
+class hd_function(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("amp", ctypes.c_double),
+                ("omega", ctypes.c_double * MAX_DIM), ("speed", ctypes.c_double * MAX_DIM),
+                ("phase", ctypes.c_double * MAX_DIM), ("cosine", ctypes.c_int * MAX_DIM)]
+
+
+class hd_adv_desc(ctypes.Structure):
+    _fields_ = [("dim_x", ctypes.c_int), ("dim_v", ctypes.c_int), ("degree", ctypes.c_int),
+                ("n_points", ctypes.c_int), ("dtype", ctypes.c_int),
+                ("cells_x", ctypes.c_int * 3), ("cells_v", ctypes.c_int * 3),
+                ("lo_x", ctypes.c_double * 3), ("hi_x", ctypes.c_double * 3),
+                ("lo_v", ctypes.c_double * 3), ("hi_v", ctypes.c_double * 3),
+                ("periodic_x", ctypes.c_int), ("periodic_v", ctypes.c_int),
+                ("velocity", ctypes.c_double * MAX_DIM), ("skew", ctypes.c_double),
+                ("bc_kind", ctypes.c_int), ("bc", hd_function)]
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load the CUDA library (building it first when it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB_PATH
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise HdError(HD_ERR_UNSUPPORTED, "CUDA library %s is not built" % path)
+        _build.build()
+    L = ctypes.CDLL(path)
+    vp = ctypes.c_void_p
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.hd_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.hd_version.restype = ctypes.c_char_p
+    L.hd_adv_create.argtypes = [ctypes.POINTER(hd_adv_desc), ctypes.POINTER(vp)]
+    L.hd_adv_destroy.argtypes = [vp]
+    L.hd_adv_n_dofs.argtypes = [vp]
+    L.hd_adv_n_dofs.restype = ctypes.c_longlong
+    L.hd_adv_apply.argtypes = [vp, vp, vp, ctypes.c_double, vp]
+    L.hd_adv_critical_time_step.argtypes = [vp]
+    L.hd_adv_critical_time_step.restype = ctypes.c_double
+    L.hd_interpolate.argtypes = [vp, ctypes.POINTER(hd_function), ctypes.c_double, vp, vp]
+    L.hd_norm_and_error.argtypes = [vp, ctypes.POINTER(hd_function), ctypes.c_double, vp, dp, vp]
+    L.hd_lsrk_create.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
+    L.hd_lsrk_destroy.argtypes = [vp]
+    L.hd_lsrk_n_stages.argtypes = [vp]
+    L.hd_lsrk_step.argtypes = [vp, vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
+                               ctypes.c_double, ctypes.c_double, vp]
+    L.hd_lsrk_step_unfused.argtypes = [vp, vp, vp, vp, vp, ctypes.c_double, ctypes.c_double, vp]
+    L.hd_lsrk_stage_update.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_double, ctypes.c_double,
+                                       vp, vp, vp, vp]
+    L.hd_lsrk_coefficients.argtypes = [vp, dp, dp, dp]
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    buf = ctypes.create_string_buffer(1024)
+    load().hd_last_error(buf, 1024)
+    return buf.value.decode()
+
+
+def check(rc: int) -> None:
+    if rc != HD_OK:
+        raise HdError(rc, last_error())

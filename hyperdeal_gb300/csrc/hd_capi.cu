@@ -1,0 +1,546 @@
+// hd_capi.cu -- C ABI of the GB300 advection path (include/hyperdeal_gb300.h).
+//
+// Host side: validates the descriptor, builds the 1D tables (Gauss-Lobatto
+// nodes/weights and the collocation derivative matrix), derives the
+// per-direction line operators from the reference's operator formulas, picks
+// the (D, k, dtype) kernel and runs the LSRK stage sequence.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/hyperdeal_gb300.h"
+#include "hd_ecl.cuh"
+#include "hd_vector.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(HD_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// Legendre P_n and P_n' (three-term recurrence)
+void legendre(int n, double x, double* p, double* dp) {
+  double p0 = 1.0, p1 = x;
+  if (n == 0) { *p = 1.0; *dp = 0.0; return; }
+  for (int k = 2; k <= n; ++k) {
+    const double pk = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+    p0 = p1;
+    p1 = pk;
+  }
+  *p = p1;
+  *dp = n * (p0 - x * p1) / (1.0 - x * x);
+}
+
+// Gauss-Lobatto rule with n points on [0,1]: end points plus the roots of
+// P_{n-1}' (Newton from Chebyshev-Gauss-Lobatto guesses); w = 2/(n(n-1)P^2)/2
+void gauss_lobatto(int n, double* x, double* w) {
+  const int m = n - 1;
+  x[0] = 0.0;
+  x[n - 1] = 1.0;
+  for (int i = 1; i < m; ++i) {
+    double z = -std::cos(M_PI * i / m);
+    for (int it = 0; it < 100; ++it) {
+      double p, dp;
+      legendre(m, z, &p, &dp);
+      const double ddp = (2.0 * z * dp - m * (m + 1.0) * p) / (1.0 - z * z);
+      const double dz = dp / ddp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-17) break;
+    }
+    x[i] = 0.5 * (1.0 + z);
+  }
+  for (int i = 0; i < n; ++i) {
+    double p, dp;
+    const double z = 2.0 * x[i] - 1.0;
+    if (i == 0 || i == n - 1) {
+      p = (i == 0 && (m % 2)) ? -1.0 : 1.0;  // P_m(+-1) = (+-1)^m
+    } else {
+      legendre(m, z, &p, &dp);
+    }
+    w[i] = 1.0 / (m * (m + 1.0) * p * p);
+  }
+  for (int i = 0; i < n / 2; ++i) {  // exact symmetry
+    const double xs = 0.5 * (x[i] + (1.0 - x[n - 1 - i]));
+    const double ws = 0.5 * (w[i] + w[n - 1 - i]);
+    x[i] = xs;
+    x[n - 1 - i] = 1.0 - xs;
+    w[i] = ws;
+    w[n - 1 - i] = ws;
+  }
+  if (n % 2) x[n / 2] = 0.5;
+}
+
+// D[q][j] = l_j'(x_q) for the Lagrange basis on the nodes x
+void lagrange_derivative_matrix(int n, const double* x, double* D) {
+  for (int q = 0; q < n; ++q)
+    for (int j = 0; j < n; ++j) {
+      double s = 0.0;
+      for (int l = 0; l < n; ++l) {
+        if (l == j) continue;
+        double t = 1.0 / (x[j] - x[l]);
+        for (int m = 0; m < n; ++m)
+          if (m != j && m != l) t *= (x[q] - x[m]) / (x[j] - x[m]);
+        s += t;
+      }
+      D[q * n + j] = s;
+    }
+}
+
+// The reference's operator restricted to one line of n nodes along direction d
+// of a Cartesian cell (constant velocity a, width h, skew factor s), with the
+// exterior values uL / uR of the left / right faces; the JxW factors of the
+// other directions cancel between integration and inverse mass:
+//   volume  (1-s) (a/h) (1/w_i) sum_q D[q][i] w_q u_q  -  s (a/h) sum_j D[i][j] u_j
+//           (advection_operation.h:325-404, fe_evaluation_cell.h:278-348)
+//   faces   -(flux - s u- a.n) / (h w_i) at i = 0 (n = -e_d) and i = n-1 (n = +e_d),
+//           flux = 0.5 ((u- + u+) a.n + |a.n| (u- - u+))  (alpha = 1)
+//           (advection_operation.h:459-482, fe_evaluation_face.h:381-399)
+//   inverse mass: division by JxW_i (fe_evaluation_cell_inverse.h:131-133)
+void line_operator(int n, const double* w, const double* D, double a, double h, double s, const double* u,
+                   double uL, double uR, double* out) {
+  for (int i = 0; i < n; ++i) {
+    double vol = 0.0, skw = 0.0;
+    for (int q = 0; q < n; ++q) vol += D[q * n + i] * w[q] * u[q];
+    for (int j = 0; j < n; ++j) skw += D[i * n + j] * u[j];
+    out[i] = (1.0 - s) * (a / h) * vol / w[i] - s * (a / h) * skw;
+  }
+  {
+    const double an = -a, um = u[0];
+    const double flux = 0.5 * ((um + uL) * an + std::fabs(an) * (um - uL));
+    out[0] += -(flux - s * um * an) / (h * w[0]);
+  }
+  {
+    const double an = a, um = u[n - 1];
+    const double flux = 0.5 * ((um + uR) * an + std::fabs(an) * (um - uR));
+    out[n - 1] += -(flux - s * um * an) / (h * w[n - 1]);
+  }
+}
+
+struct LineOpD {
+  double M[hd::kMaxN * hd::kMaxN];
+  double cin;
+  int in_node, nb_node, step, active;
+};
+
+// linear operator coefficients by probing line_operator with unit inputs
+bool derive_line_op(int n, const double* w, const double* D, double a, double h, double s, LineOpD* op) {
+  double u[hd::kMaxN], out[hd::kMaxN];
+  bool any = false;
+  for (int q = 0; q < n; ++q) {
+    for (int j = 0; j < n; ++j) u[j] = (j == q);
+    line_operator(n, w, D, a, h, s, u, 0.0, 0.0, out);
+    for (int i = 0; i < n; ++i) {
+      op->M[i * n + q] = out[i];
+      any = any || out[i] != 0.0;
+    }
+  }
+  for (int j = 0; j < n; ++j) u[j] = 0.0;
+  double cL[hd::kMaxN], cR[hd::kMaxN];
+  line_operator(n, w, D, a, h, s, u, 1.0, 0.0, cL);
+  line_operator(n, w, D, a, h, s, u, 0.0, 1.0, cR);
+  for (int i = 1; i < n; ++i)
+    if (cL[i] != 0.0) return false;
+  for (int i = 0; i < n - 1; ++i)
+    if (cR[i] != 0.0) return false;
+  if (cL[0] != 0.0 && cR[n - 1] != 0.0) return false;  // not a one-sided upwind flux
+  if (cR[n - 1] != 0.0) {
+    op->step = +1; op->in_node = n - 1; op->nb_node = 0; op->cin = cR[n - 1];
+  } else {
+    op->step = -1; op->in_node = 0; op->nb_node = n - 1; op->cin = cL[0];
+  }
+  op->active = any || op->cin != 0.0;
+  return true;
+}
+
+hd::DevFunction to_dev(const hd_function& f) {
+  hd::DevFunction d;
+  std::memset(&d, 0, sizeof(d));
+  d.kind = f.kind;
+  d.amp = f.amp;
+  for (int i = 0; i < HD_MAX_DIM; ++i) {
+    d.omega[i] = f.omega[i];
+    d.speed[i] = f.speed[i];
+    d.phase[i] = f.phase[i];
+    d.cosine[i] = f.cosine[i];
+  }
+  return d;
+}
+
+}  // namespace
+
+struct hd_adv {
+  hd_adv_desc desc;
+  int D, N, NC, dtype;
+  long long n_cells, n_dofs, ncx;
+  double lo[HD_MAX_DIM], hi[HD_MAX_DIM], h[HD_MAX_DIM];
+  int cells[HD_MAX_DIM], periodic[HD_MAX_DIM];
+  double gl[hd::kMaxN], glw[hd::kMaxN], Dm[hd::kMaxN * hd::kMaxN];
+  LineOpD ops[HD_MAX_DIM];
+  hd::EclLaunchers launchers;
+  hd::EclParams<double> p64;
+  hd::EclParams<float> p32;
+  hd::VecGeom geom;
+  double* d_partials;  // norm reduction scratch (2*kNormBlocks + 2 doubles)
+  int device;
+};
+
+struct hd_lsrk {
+  char type[8];
+  int ns;
+  double ai[16], bi[16], ci[16];
+};
+
+namespace {
+
+template <typename T>
+void fill_params(const hd_adv* op, hd::EclParams<T>* P) {
+  std::memset(P, 0, sizeof(*P));
+  P->n_cells = op->n_cells;
+  P->D = op->D;
+  P->dim_x = op->desc.dim_x;
+  long long st = 1;
+  for (int d = 0; d < op->D; ++d) {
+    P->cells[d] = op->cells[d];
+    P->cstride[d] = st;
+    st *= op->cells[d];
+    P->periodic[d] = op->periodic[d];
+    P->lo[d] = op->lo[d];
+    P->h[d] = op->h[d];
+    const LineOpD& L = op->ops[d];
+    for (int i = 0; i < op->N * op->N; ++i) P->op[d].M[i] = T(L.M[i]);
+    P->op[d].cin = T(L.cin);
+    P->op[d].in_node = L.in_node;
+    P->op[d].nb_node = L.nb_node;
+    P->op[d].step = L.step;
+    P->op[d].active = L.active;
+  }
+  if (op->D < hd::kMaxDim) P->cstride[op->D] = st;
+  for (int i = 0; i < op->N; ++i) P->gl[i] = op->gl[i];
+  P->bc_inhom = op->desc.bc_kind == HD_BC_FUNCTION;
+  P->bc = to_dev(op->desc.bc);
+}
+
+hd::EclLaunchers get_launchers(int D, int N) {
+  switch (D) {
+    case 2: return hd::ecl_launchers_d2(N);
+    case 3: return hd::ecl_launchers_d3(N);
+    case 4: return hd::ecl_launchers_d4(N);
+    case 5: return hd::ecl_launchers_d5(N);
+    case 6: return hd::ecl_launchers_d6(N);
+    default: return hd::EclLaunchers{nullptr, nullptr, 0, 0, 0, 0, 0, 0, false, false};
+  }
+}
+
+int launch(hd_adv* op, int mode, const void* tin, const void* uin, void* uout, void* tout, double fb,
+           double fa, double time, cudaStream_t s) {
+  cudaError_t e;
+  if (op->dtype == HD_F64) {
+    hd::EclParams<double> P = op->p64;
+    P.tin = (const double*)tin; P.uin = (const double*)uin; P.uout = (double*)uout; P.tout = (double*)tout;
+    P.fb = fb; P.fa = fa; P.time = time;
+    e = op->launchers.f64(P, mode, s);
+  } else {
+    hd::EclParams<float> P = op->p32;
+    P.tin = (const float*)tin; P.uin = (const float*)uin; P.uout = (float*)uout; P.tout = (float*)tout;
+    P.fb = float(fb); P.fa = float(fa); P.time = time;
+    e = op->launchers.f32(P, mode, s);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "ECL kernel launch");
+  return HD_OK;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+}  // namespace
+
+extern "C" {
+
+int hd_last_error(char* buf, size_t len) {
+  const int n = int(g_last_error.size());
+  if (buf && len) {
+    std::strncpy(buf, g_last_error.c_str(), len - 1);
+    buf[len - 1] = 0;
+  }
+  return n;
+}
+
+const char* hd_version(void) { return "hyperdeal_gb300 0.1 (sm_103a)"; }
+
+int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
+  try {
+    if (!desc || !out) return fail(HD_ERR_INVALID, "hd_adv_create: null argument");
+    *out = nullptr;
+    const hd_adv_desc& d = *desc;
+    if (d.dim_x < 1 || d.dim_x > 3 || d.dim_v < 1 || d.dim_v > 3)
+      return fail(HD_ERR_INVALID, "dim_x and dim_v must be in 1..3 (got %d, %d)", d.dim_x, d.dim_v);
+    if (d.degree < 1 || d.degree + 1 > hd::kMaxN)
+      return fail(HD_ERR_UNSUPPORTED, "degree %d not built (1..%d)", d.degree, hd::kMaxN - 1);
+    if (d.n_points != d.degree + 1)
+      return fail(HD_ERR_UNSUPPORTED, "n_points must equal degree+1 (Gauss-Lobatto collocation), got %d",
+                  d.n_points);
+    if (d.dtype != HD_F64 && d.dtype != HD_F32) return fail(HD_ERR_INVALID, "unknown dtype %d", d.dtype);
+    if (d.bc_kind != HD_BC_HOMOGENEOUS && d.bc_kind != HD_BC_FUNCTION)
+      return fail(HD_ERR_INVALID, "unknown bc_kind %d", d.bc_kind);
+    if (!std::isfinite(d.skew)) return fail(HD_ERR_INVALID, "skew factor is not finite");
+    hd_adv* op = new (std::nothrow) hd_adv;
+    if (!op) return fail(HD_ERR_ALLOC, "out of host memory");
+    std::memset(op, 0, sizeof(*op));
+    op->desc = d;
+    op->D = d.dim_x + d.dim_v;
+    op->N = d.degree + 1;
+    op->dtype = d.dtype;
+    op->NC = hd::ipow(op->N, op->D);
+    op->n_cells = 1;
+    op->ncx = 1;
+    for (int i = 0; i < op->D; ++i) {
+      const bool isx = i < d.dim_x;
+      const int c = isx ? d.cells_x[i] : d.cells_v[i - d.dim_x];
+      const double lo = isx ? d.lo_x[i] : d.lo_v[i - d.dim_x];
+      const double hi = isx ? d.hi_x[i] : d.hi_v[i - d.dim_x];
+      if (c < 1) { delete op; return fail(HD_ERR_INVALID, "cells in direction %d must be >= 1", i); }
+      if (!(hi > lo) || !std::isfinite(lo) || !std::isfinite(hi)) {
+        delete op;
+        return fail(HD_ERR_INVALID, "box in direction %d must have hi > lo", i);
+      }
+      if (!std::isfinite(d.velocity[i])) { delete op; return fail(HD_ERR_INVALID, "velocity %d not finite", i); }
+      op->cells[i] = c;
+      op->lo[i] = lo;
+      op->hi[i] = hi;
+      op->h[i] = (hi - lo) / c;
+      op->periodic[i] = isx ? (d.periodic_x != 0) : (d.periodic_v != 0);
+      if (op->n_cells > (1LL << 40) / c) { delete op; return fail(HD_ERR_INVALID, "mesh too large"); }
+      op->n_cells *= c;
+      if (isx) op->ncx *= c;
+    }
+    op->n_dofs = op->n_cells * op->NC;
+    gauss_lobatto(op->N, op->gl, op->glw);
+    lagrange_derivative_matrix(op->N, op->gl, op->Dm);
+    for (int i = 0; i < op->D; ++i)
+      if (!derive_line_op(op->N, op->glw, op->Dm, d.velocity[i], op->h[i], d.skew, &op->ops[i])) {
+        delete op;
+        return fail(HD_ERR_UNSUPPORTED, "direction %d: flux is not one-sided upwind", i);
+      }
+    op->launchers = get_launchers(op->D, op->N);
+    const bool ok = d.dtype == HD_F64 ? op->launchers.ok_f64 : op->launchers.ok_f32;
+    if (!op->launchers.f64 || !ok) {
+      delete op;
+      return fail(HD_ERR_UNSUPPORTED, "no kernel for D=%d, degree=%d, dtype=%s (cell does not fit in shared memory)",
+                  d.dim_x + d.dim_v, d.degree, d.dtype == HD_F64 ? "f64" : "f32");
+    }
+    fill_params(op, &op->p64);
+    fill_params(op, &op->p32);
+    hd::VecGeom& g = op->geom;
+    std::memset(&g, 0, sizeof(g));
+    g.D = op->D; g.dim_x = d.dim_x; g.N = op->N; g.NC = op->NC; g.ncx = op->ncx; g.n_dofs = op->n_dofs;
+    for (int i = 0; i < op->D; ++i) { g.cells[i] = op->cells[i]; g.lo[i] = op->lo[i]; g.h[i] = op->h[i]; }
+    for (int i = 0; i < op->N; ++i) { g.gl[i] = op->gl[i]; g.glw[i] = op->glw[i]; }
+    cudaError_t e = cudaGetDevice(&op->device);
+    if (e != cudaSuccess) { delete op; return cuda_fail(e, "cudaGetDevice"); }
+    e = cudaMalloc(&op->d_partials, sizeof(double) * (2 * hd::kNormBlocks + 2));
+    if (e != cudaSuccess) { delete op; return cuda_fail(e, "cudaMalloc (norm scratch)"); }
+    *out = op;
+    return HD_OK;
+  } catch (...) {
+    return fail(HD_ERR_INVALID, "hd_adv_create: unexpected exception");
+  }
+}
+
+int hd_adv_destroy(hd_adv* op) {
+  if (!op) return HD_OK;
+  if (op->d_partials) cudaFree(op->d_partials);
+  delete op;
+  return HD_OK;
+}
+
+long long hd_adv_n_dofs(const hd_adv* op) { return op ? op->n_dofs : -1; }
+
+double hd_adv_critical_time_step(const hd_adv* op) {
+  if (!op) return -1.0;
+  double vx = 0.0, vv = 0.0;
+  for (int d = 0; d < op->D; ++d) {
+    const double v = std::fabs(op->desc.velocity[d] / op->h[d]);
+    if (d < op->desc.dim_x) vx = std::fmax(vx, v);
+    else vv = std::fmax(vv, v);
+  }
+  return std::fmin(1.0 / vx, 1.0 / vv);
+}
+
+int hd_adv_apply(hd_adv* op, void* dst, const void* src, double time, void* stream) {
+  if (!op || !dst || !src) return fail(HD_ERR_INVALID, "hd_adv_apply: null argument");
+  if (!aligned16(dst) || !aligned16(src)) return fail(HD_ERR_INVALID, "hd_adv_apply: vectors must be 16-byte aligned");
+  const size_t bytes = size_t(op->n_dofs) * (op->dtype == HD_F64 ? 8 : 4);
+  const char* a = (const char*)src;
+  const char* b = (const char*)dst;
+  if (a < b + bytes && b < a + bytes) return fail(HD_ERR_INVALID, "hd_adv_apply: dst and src overlap");
+  return launch(op, hd::kApply, src, src, dst, nullptr, 0.0, 0.0, time, (cudaStream_t)stream);
+}
+
+int hd_interpolate(hd_adv* op, const hd_function* f, double time, void* dst, void* stream) {
+  if (!op || !f || !dst) return fail(HD_ERR_INVALID, "hd_interpolate: null argument");
+  cudaError_t e = hd::launch_interpolate(op->geom, to_dev(*f), time, dst, op->dtype == HD_F32, (cudaStream_t)stream);
+  return e == cudaSuccess ? HD_OK : cuda_fail(e, "interpolate kernel");
+}
+
+int hd_norm_and_error(hd_adv* op, const hd_function* f, double time, const void* src, double* result,
+                      void* stream) {
+  if (!op || !f || !src || !result) return fail(HD_ERR_INVALID, "hd_norm_and_error: null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = hd::launch_norm_error(op->geom, to_dev(*f), time, src, op->dtype == HD_F32, op->d_partials,
+                                        op->d_partials + 2 * hd::kNormBlocks, s);
+  if (e != cudaSuccess) return cuda_fail(e, "norm kernel");
+  e = cudaMemcpyAsync(result, op->d_partials + 2 * hd::kNormBlocks, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_fail(e, "norm copy");
+  e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? HD_OK : cuda_fail(e, "norm synchronize");
+}
+
+int hd_lsrk_create(const char* type, hd_lsrk** out) {
+  if (!type || !out) return fail(HD_ERR_INVALID, "hd_lsrk_create: null argument");
+  hd_lsrk rk;
+  std::memset(&rk, 0, sizeof(rk));
+  // Kennedy, Carpenter, Lewis (2000) coefficients, tabulated as in
+  // base/time_integrators.templates.h:33-89
+  if (!std::strcmp(type, "rk33")) {
+    const double b[] = {0.245170287303492, 0.184896052186740, 0.569933660509768};
+    const double a[] = {0.755726351946097, 0.386954477304099};
+    rk.ns = 3; std::memcpy(rk.bi, b, sizeof(b)); std::memcpy(rk.ai, a, sizeof(a));
+  } else if (!std::strcmp(type, "rk45")) {
+    const double b[] = {1153189308089. / 22510343858157., 1772645290293. / 4653164025191.,
+                        -1672844663538. / 4480602732383., 2114624349019. / 3568978502595.,
+                        5198255086312. / 14908931495163.};
+    const double a[] = {970286171893. / 4311952581923., 6584761158862. / 12103376702013.,
+                        2251764453980. / 15575788980749., 26877169314380. / 34165994151039.};
+    rk.ns = 5; std::memcpy(rk.bi, b, sizeof(b)); std::memcpy(rk.ai, a, sizeof(a));
+  } else if (!std::strcmp(type, "rk47")) {
+    const double b[] = {0.0941840925477795334, 0.149683694803496998, 0.285204742060440058,
+                        -0.122201846148053668, 0.0605151571191401122, 0.345986987898399296,
+                        0.186627171718797670};
+    const double a0[] = {0.241566650129646868, 0.0423866513027719953, 0.215602732678803776,
+                         0.232328007537583987, 0.256223412574146438, 0.0978694102142697230};
+    rk.ns = 7; std::memcpy(rk.bi, b, sizeof(b));
+    for (int i = 0; i < 6; ++i) rk.ai[i] = a0[i] + b[i];
+  } else if (!std::strcmp(type, "rk59")) {
+    const double b[] = {2274579626619. / 23610510767302., 693987741272. / 12394497460941.,
+                        -347131529483. / 15096185902911., 1144057200723. / 32081666971178.,
+                        1562491064753. / 11797114684756., 13113619727965. / 44346030145118.,
+                        393957816125. / 7825732611452., 720647959663. / 6565743875477.,
+                        3559252274877. / 14424734981077.};
+    const double a[] = {1107026461565. / 5417078080134., 38141181049399. / 41724347789894.,
+                        493273079041. / 11940823631197., 1851571280403. / 6147804934346.,
+                        11782306865191. / 62590030070788., 9452544825720. / 13648368537481.,
+                        4435885630781. / 26285702406235., 2357909744247. / 11371140753790.};
+    rk.ns = 9; std::memcpy(rk.bi, b, sizeof(b)); std::memcpy(rk.ai, a, sizeof(a));
+  } else {
+    return fail(HD_ERR_UNSUPPORTED, "unknown LSRK type '%s' (rk33, rk45, rk47, rk59)", type);
+  }
+  std::strncpy(rk.type, type, sizeof(rk.type) - 1);
+  // stage times c_s = sum_{j < s-1} b_j + a_{s-1} (time_integrators.templates.h:172-183)
+  double sum_b = 0.0;
+  rk.ci[0] = 0.0;
+  for (int s = 1; s < rk.ns; ++s) {
+    rk.ci[s] = sum_b + rk.ai[s - 1];
+    sum_b += rk.bi[s - 1];
+  }
+  hd_lsrk* p = new (std::nothrow) hd_lsrk(rk);
+  if (!p) return fail(HD_ERR_ALLOC, "out of host memory");
+  *out = p;
+  return HD_OK;
+}
+
+int hd_lsrk_destroy(hd_lsrk* rk) {
+  delete rk;
+  return HD_OK;
+}
+
+int hd_lsrk_n_stages(const hd_lsrk* rk) { return rk ? rk->ns : 0; }
+
+int hd_lsrk_coefficients(const hd_lsrk* rk, double* ai, double* bi, double* ci) {
+  if (!rk) return fail(HD_ERR_INVALID, "hd_lsrk_coefficients: null handle");
+  if (ai) std::memcpy(ai, rk->ai, sizeof(double) * (rk->ns - 1));
+  if (bi) std::memcpy(bi, rk->bi, sizeof(double) * rk->ns);
+  if (ci) std::memcpy(ci, rk->ci, sizeof(double) * rk->ns);
+  return HD_OK;
+}
+
+int hd_lsrk_step(hd_adv* op, const hd_lsrk* rk, void** sol, void** Ki, void** Ti, double time, double dt,
+                 void* stream) {
+  if (!op || !rk || !sol || !Ki || !Ti || !*sol || !*Ki || !*Ti)
+    return fail(HD_ERR_INVALID, "hd_lsrk_step: null argument");
+  if (*sol == *Ki || *sol == *Ti || *Ki == *Ti) return fail(HD_ERR_INVALID, "hd_lsrk_step: vectors must differ");
+  if (!aligned16(*sol) || !aligned16(*Ki) || !aligned16(*Ti))
+    return fail(HD_ERR_INVALID, "hd_lsrk_step: vectors must be 16-byte aligned");
+  cudaStream_t s = (cudaStream_t)stream;
+  // buffer rotation: X0 holds U and T_1; the new solution accumulates in X1;
+  // the stage inputs alternate between X2 and X0
+  void* X0 = *sol;
+  void* X1 = *Ki;
+  void* X2 = *Ti;
+  void* t_in = X0;
+  void* t_free = X2;
+  for (int st = 0; st < rk->ns; ++st) {
+    const double fb = rk->bi[st] * dt;
+    const bool last = st == rk->ns - 1;
+    const double fa = last ? 0.0 : rk->ai[st] * dt;
+    const double t_s = time + rk->ci[st] * dt;
+    int mode = st == 0 ? hd::kStageFirst : (last ? hd::kStageLast : hd::kStageMid);
+    if (st == 0 && last) mode = hd::kStageFirst;  // single-stage schemes are not built
+    const int rc = launch(op, mode, t_in, st == 0 ? t_in : X1, X1, last ? nullptr : t_free, fb, fa, t_s, s);
+    if (rc) return rc;
+    if (!last) {
+      void* next = t_free;
+      t_free = (st == 0) ? X0 : t_in;
+      t_in = next;
+    }
+  }
+  *sol = X1;
+  *Ki = X0;
+  *Ti = X2;
+  return HD_OK;
+}
+
+int hd_lsrk_stage_update(int dtype, long long n, double factor_bi, double factor_ai, const void* K, void* sol,
+                         void* next_T, void* stream) {
+  if (!K || !sol || n < 0) return fail(HD_ERR_INVALID, "hd_lsrk_stage_update: bad argument");
+  if (dtype != HD_F64 && dtype != HD_F32) return fail(HD_ERR_INVALID, "unknown dtype %d", dtype);
+  cudaError_t e = hd::launch_lsrk_update(dtype == HD_F32, n, factor_bi, factor_ai, K, sol,
+                                         factor_ai == 0.0 ? nullptr : next_T, (cudaStream_t)stream);
+  return e == cudaSuccess ? HD_OK : cuda_fail(e, "lsrk update kernel");
+}
+
+int hd_lsrk_step_unfused(hd_adv* op, const hd_lsrk* rk, void* sol, void* Ki, void* Ti, double time, double dt,
+                         void* stream) {
+  if (!op || !rk || !sol || !Ki || !Ti) return fail(HD_ERR_INVALID, "hd_lsrk_step_unfused: null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t bytes = size_t(op->n_dofs) * (op->dtype == HD_F64 ? 8 : 4);
+  // first stage with only_Ti_is_ghosted = true: Ti = sol (time_integrators.templates.h:142-148)
+  cudaError_t e = cudaMemcpyAsync(Ti, sol, bytes, cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "copy sol -> Ti");
+  for (int st = 0; st < rk->ns; ++st) {
+    const bool last = st == rk->ns - 1;
+    int rc = hd_adv_apply(op, Ki, Ti, time + rk->ci[st] * dt, stream);
+    if (rc) return rc;
+    rc = hd_lsrk_stage_update(op->dtype, op->n_dofs, rk->bi[st] * dt, last ? 0.0 : rk->ai[st] * dt, Ki, sol, Ti,
+                              stream);
+    if (rc) return rc;
+  }
+  return HD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,28 @@
+// hd_vector.cuh -- declarations of the vector kernels (hd_vector.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "hd_ecl.cuh"
+
+namespace hd {
+
+constexpr int kNormBlocks = 152 * 4;  // fixed grid -> deterministic reduction order
+
+// geometry of a nodal DG vector on the Cartesian phase-space mesh
+struct VecGeom {
+  int D, dim_x, N, NC;
+  long long ncx, n_dofs;
+  int cells[kMaxDim];
+  double lo[kMaxDim], h[kMaxDim];
+  double gl[kMaxN], glw[kMaxN];
+};
+
+cudaError_t launch_interpolate(const VecGeom& g, const DevFunction& f, double t, void* dst, int is_f32,
+                               cudaStream_t s);
+cudaError_t launch_norm_error(const VecGeom& g, const DevFunction& f, double t, const void* src, int is_f32,
+                              double* partials, double* out, cudaStream_t s);
+cudaError_t launch_lsrk_update(int is_f32, long long n, double bi, double ai, const void* K, void* sol,
+                               void* next_T, cudaStream_t s);
+
+}  // namespace hd

@@ -1,0 +1,172 @@
+/*
+ * hyperdeal_gb300.h -- C ABI of the GB300 (sm_103a) phase-space advection
+ * path: a drop-in for hyper.deal's element-centric (ECL) upwind-DG advection
+ * operator at Gauss-Lobatto collocation and its low-storage Runge-Kutta
+ * driver.
+ *
+ * Conventions
+ *   - Every entry point returns an int status (HD_OK = 0).  No C++ exception
+ *     crosses this boundary; hd_last_error() returns the message of the last
+ *     failure on the calling thread.
+ *   - Vectors are caller-owned DEVICE pointers holding n_dofs values of the
+ *     handle's dtype (double for HD_F64, float for HD_F32), 16-byte aligned.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *     stream).  All work of one call is enqueued on that stream; calls return
+ *     without synchronising unless documented otherwise.
+ *   - A handle is not thread-safe (as the reference operator, whose
+ *     evaluators are members, is not re-entrant).
+ *
+ * DoF numbering (identical to the reference's, 1 rank, NRefinements = 0):
+ *   cell gid = gid_x + n_cells_x * gid_v, gid_x / gid_v lexicographic over
+ *   the x- / v-cells (first direction fastest); each cell owns (k+1)^D
+ *   contiguous values; inside a cell the node index is i_x + (k+1)^dim_x*i_v
+ *   with lexicographic node order (first direction fastest).
+ *   Reference: include/hyper.deal/matrix_free/matrix_free.templates.h:535-563
+ *   (GlobaleCellIDTranslator::translate), :925-932 (sorted local cells),
+ *   include/hyper.deal/matrix_free/vector_partitioner.h:723-724 (n^D values per
+ *   cell), include/hyper.deal/matrix_free/shape_info.h:141-160 (x nodes
+ *   fastest).
+ */
+#ifndef HYPERDEAL_GB300_H
+#define HYPERDEAL_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HD_MAX_DIM 6
+
+enum hd_status {
+  HD_OK = 0,
+  HD_ERR_INVALID = 1,     /* bad argument or descriptor                     */
+  HD_ERR_UNSUPPORTED = 2, /* valid in the reference, not built here         */
+  HD_ERR_CUDA = 3,        /* a CUDA runtime call failed                     */
+  HD_ERR_ALLOC = 4,       /* host or device allocation failed               */
+  HD_ERR_DEVICE = 5       /* a kernel reported an error through its flag    */
+};
+
+enum hd_dtype { HD_F64 = 0, HD_F32 = 1 };
+
+enum hd_bc_kind {
+  HD_BC_HOMOGENEOUS = 0, /* u+ = -u- on non-periodic faces                  */
+  HD_BC_FUNCTION = 1     /* u+ = -u- + 2 g(x, t), g an hd_function          */
+};
+
+/* Analytic function family used for initial data, exact solutions and
+ * Dirichlet data (the reference passes dealii::Function objects):
+ *   kind 0: 0;  kind 1: amp;
+ *   kind 2: amp * prod_d trig_d(omega_d * (x_d - speed_d * t) + phase_d),
+ *           trig_d = cos if cosine[d] else sin.                            */
+typedef struct hd_function {
+  int kind;
+  double amp;
+  double omega[HD_MAX_DIM];
+  double speed[HD_MAX_DIM];
+  double phase[HD_MAX_DIM];
+  int cosine[HD_MAX_DIM];
+} hd_function;
+
+/* Problem descriptor: what the reference sets up through MatrixFree::reinit,
+ * AdvectionOperation::reinit, BoundaryDescriptor and ConstantVelocityFieldView
+ * (include/hyper.deal/operators/advection/advection_operation.h:97-129,
+ *  boundary_descriptor.h:77-104, velocity_field_view.h:64-166).           */
+typedef struct hd_adv_desc {
+  int dim_x, dim_v;     /* 1..3 each                                       */
+  int degree;           /* k; n_points must be k+1 (collocation)           */
+  int n_points;
+  int dtype;            /* HD_F64 or HD_F32 (storage and arithmetic)       */
+  int cells_x[3], cells_v[3];
+  double lo_x[3], hi_x[3], lo_v[3], hi_v[3];
+  int periodic_x, periodic_v;
+  double velocity[HD_MAX_DIM]; /* constant a = (a_x, a_v)                  */
+  double skew;          /* AdvectionOperationParamters::factor_skew        */
+  int bc_kind;          /* enum hd_bc_kind, used on non-periodic faces     */
+  hd_function bc;       /* g for HD_BC_FUNCTION                            */
+} hd_adv_desc;
+
+typedef struct hd_adv hd_adv;
+typedef struct hd_lsrk hd_lsrk;
+
+/* Message of the last failure on this thread (empty if none); returns the
+ * message length. */
+int hd_last_error(char *buf, size_t len);
+
+/* Library version string. */
+const char *hd_version(void);
+
+/* ---- operator ---------------------------------------------------------- */
+
+/* Replaces AdvectionOperation(MatrixFree, table) + reinit(bc, velocity, param)
+ * (advection_operation.h:85-129).  Selects the (dim, degree, dtype) kernel and
+ * derives the per-direction line operators.  Uses the current CUDA device. */
+int hd_adv_create(const hd_adv_desc *desc, hd_adv **out);
+int hd_adv_destroy(hd_adv *op);
+
+/* Number of DoFs = prod(cells) * (k+1)^(dim_x+dim_v). */
+long long hd_adv_n_dofs(const hd_adv *op);
+
+/* dst = M^{-1} A(src) at `time` (boundary data time), i.e.
+ * AdvectionOperation::apply<all>(dst, src, time) in its ECL branch
+ * (advection_operation.h:134-209, :218-566).  dst is overwritten; dst and src
+ * must not overlap. */
+int hd_adv_apply(hd_adv *op, void *dst, const void *src, double time, void *stream);
+
+/* dt_crit = min(1/max_x |a_d/h_d|, 1/max_v |a_d/h_d|)
+ * (operators/advection/cfl.h:56-124, Cartesian mesh). */
+double hd_adv_critical_time_step(const hd_adv *op);
+
+/* ---- vector tools --------------------------------------------------------- */
+
+/* dst = f(x_i, time) at the Gauss-Lobatto support points
+ * (numerics/vector_tools.h:81-135, interpolate with quad_no = 2). */
+int hd_interpolate(hd_adv *op, const hd_function *f, double time, void *dst, void *stream);
+
+/* result[0] = ||src||_L2, result[1] = ||src - f(., time)||_L2 with the
+ * operator's quadrature (Gauss-Lobatto under collocation)
+ * (numerics/vector_tools.h:144-223).  Synchronises `stream`. */
+int hd_norm_and_error(hd_adv *op, const hd_function *f, double time, const void *src,
+                      double *result, void *stream);
+
+/* ---- low-storage Runge-Kutta ------------------------------------------------ */
+
+/* LowStorageRungeKuttaIntegrator(Ki, Ti, type, only_Ti_is_ghosted=true)
+ * (base/time_integrators.h:57-77, time_integrators.templates.h:22-89);
+ * type = "rk33", "rk45", "rk47" or "rk59". */
+int hd_lsrk_create(const char *type, hd_lsrk **out);
+int hd_lsrk_destroy(hd_lsrk *rk);
+int hd_lsrk_n_stages(const hd_lsrk *rk);
+
+/* One time step of perform_time_step(sol, t, dt, op) with op = the advection
+ * operator (time_integrators.templates.h:91-184), fused: every stage is one
+ * kernel that applies the operator and the stage update
+ *   sol <- sol + b_s dt K,  T <- sol_old + a_s dt K
+ * in a single pass.  Neighbours read the stage input while it is being
+ * updated, so the three vectors rotate roles; on return the three pointers
+ * are permuted so that *sol holds the new solution (the others are scratch).
+ * The reference's own Ki/Ti vectors are scratch in the same way.  The values
+ * equal the unfused step within round-off. */
+int hd_lsrk_step(hd_adv *op, const hd_lsrk *rk, void **sol, void **Ki, void **Ti,
+                 double time, double dt, void *stream);
+
+/* The unfused reference form of the same step: op(Ti, Ki, t_s) followed by
+ * the vector update, exactly in the reference's order
+ * (time_integrators.templates.h:103-183).  sol, Ki, Ti keep their roles. */
+int hd_lsrk_step_unfused(hd_adv *op, const hd_lsrk *rk, void *sol, void *Ki, void *Ti,
+                         double time, double dt, void *stream);
+
+/* The LSRK vector update of one stage for any operator (the loop of
+ * time_integrators.templates.h:111-135): with factor_ai == 0 only
+ * sol += factor_bi * K, else also next_T = sol_old + factor_ai * K. */
+int hd_lsrk_stage_update(int dtype, long long n, double factor_bi, double factor_ai,
+                         const void *K, void *sol, void *next_T, void *stream);
+
+/* Stage count, coefficients (ai: n_stages-1 values, bi: n_stages) and the
+ * stage times c_s (n_stages values, c_0 = 0). */
+int hd_lsrk_coefficients(const hd_lsrk *rk, double *ai, double *bi, double *ci);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HYPERDEAL_GB300_H */

@@ -1,0 +1,90 @@
+"""Extracts the reference's golden outputs for the advection path into
+``reference_goldens.json`` (run once in a checkout that has the reference tree).
+
+Usage:  python tests/golden/make_goldens.py /path/to/hyperdeal
+
+Sources (paths relative to the reference root):
+  examples/advection/tests/*.configuration, *.json, *.out
+      -- application time series "Time, norm, error" (compared by numdiff
+         -a 1e-5 -r 1e-8, cmake/macros/macro_hyper_deal_pickup_tests.cmake:57)
+  tests/time_discretization/time_integrators_01.output  -- stage counts
+  tests/time_discretization/time_integrators_02.mpirun=1.output -- rk45 KAT
+  tests/vector_tools/vector_tools_01.mpirun=1.output   -- interpolate + L2
+The fixture holds numbers and run parameters only.
+"""
+import glob
+import json
+import os
+import re
+import sys
+
+NUM = r"[-+]?\d+\.?\d*(?:e[-+]?\d+)?"
+
+
+def parse_configuration(path):
+    out = {}
+    for tok in open(path).read().split():
+        k, v = tok.split("=")
+        out[k] = int(v)
+    return out
+
+
+def main(root):
+    here = os.path.dirname(os.path.abspath(__file__))
+    adv_dir = os.path.join(root, "examples", "advection", "tests")
+    advection = []
+    for jpath in sorted(glob.glob(os.path.join(adv_dir, "*.json"))):
+        name = os.path.basename(jpath)[:-5]
+        prefix = name.split(".")[0]
+        conf = parse_configuration(os.path.join(adv_dir, prefix + ".configuration"))
+        prm = json.load(open(jpath))
+        rows = []
+        for line in open(os.path.join(adv_dir, name + ".out")):
+            vals = re.findall(r"[-+]?\d\.\d+e[-+]\d+", line)
+            if vals:
+                rows.append([float(v) for v in vals])
+        case = prm["Case"]
+        sub_x = [int(v) for v in case["NSubdivisionsX"].values()]
+        sub_v = [int(v) for v in case["NSubdivisionsV"].values()]
+        td = prm["TemporalDiscretization"]
+        advection.append({
+            "name": name,
+            "dim_x": conf["DIM_X"], "dim_v": conf["DIM_V"],
+            "degree": conf["DEGREE"], "n_points": conf["N_POINTS"],
+            "subdivisions": sub_x[:conf["DIM_X"]] + sub_v[:conf["DIM_V"]],
+            "periodic_x": case["PeriodicX"] == "true",
+            "periodic_v": case["PeriodicV"] == "true",
+            "collocation": prm["SpatialDiscretization"]["DoCollocation"] == "true",
+            "use_ecl": prm["Matrixfree"]["UseECL"] == "true",
+            "skew": float(prm["AdvectionOperation"]["SkewFactor"]),
+            "rk": td["RKType"],
+            "time_step": float(td["TimeStep"]),
+            "start_time": float(td["StartTime"]),
+            "final_time": float(td["FinalTime"]),
+            "cfl": float(td["CFLNumber"]),
+            "tick": float(td["DiagnosticsTick"]),
+            "rows": rows,
+        })
+    ti01 = [int(v) for v in re.findall(r"DEAL::(\d+)", open(
+        os.path.join(root, "tests", "time_discretization", "time_integrators_01.output")).read())]
+    ti02 = [float(v) for v in re.findall(r"= (" + NUM + ")", open(
+        os.path.join(root, "tests", "time_discretization", "time_integrators_02.mpirun=1.output")).read())]
+    vt01 = []
+    for line in open(os.path.join(root, "tests", "vector_tools", "vector_tools_01.mpirun=1.output")):
+        vals = re.findall(NUM, line.split("::", 1)[1]) if "::" in line else []
+        if len(vals) == 2:
+            vt01.append([float(v) for v in vals])
+    out = {
+        "numdiff": {"abs": 1e-5, "rel": 1e-8},
+        "advection": advection,
+        "time_integrators_01_stages": ti01,
+        "time_integrators_02_rk45_values": ti02,
+        "vector_tools_01_rows": vt01,
+    }
+    with open(os.path.join(here, "reference_goldens.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", len(advection), "advection cases")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
