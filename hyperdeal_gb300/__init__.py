@@ -6,7 +6,7 @@ the C ABI in ``include/hyperdeal_gb300.h``; this package is its Python host
 side (used by the tests and the benchmark).
 """
 from ._lib import HdError, load as load_library, lib_path  # noqa: F401
-from .build import build  # noqa: F401
+from .build import build as build_library  # noqa: F401
 
 __version__ = "0.1.0"
 
@@ -16,6 +16,7 @@ def __getattr__(name):
     # symbol checks do not need torch
     if name in ("AdvectionOperation", "AdvectionParameters", "Function", "LowStorageRungeKuttaIntegrator",
                 "TimeLoop", "VectorTools", "compute_critical_time_step", "time_step_rule", "advection"):
-        from . import advection
-        return advection if name == "advection" else getattr(advection, name)
+        import importlib
+        mod = importlib.import_module(__name__ + ".advection")
+        return mod if name == "advection" else getattr(mod, name)
     raise AttributeError(name)
