@@ -1,0 +1,352 @@
+"""Benchmark: fused LSRK(5,4) advection step, 6D (3x+3v) k=3, 8^3 x 8^3 cells, FP32 storage.
+
+One step = one rk45 time step of the phase-space upwind-DG advection operator
+(ECL, Gauss-Lobatto collocation) fused with the stage update: 5 kernel launches
+over 1,073,741,824 DoFs.  Metric: GDoF/s in the reference's time-stepping
+definition, DoFs * stages * steps / time
+(examples/advection/include/application.h:540-543).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+The FP64 form of the same step is timed after the FP32 form (fewer steps) and
+the relative L2 difference of the two solutions after the timed steps is
+reported.  ``--impl reference`` times the CPU restatement of the reference
+operator (the oracle) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "advection GDoF/s (6D k=3) FP32 vs FP64 form at stated L2 err; % HBM roofline"
+UNIT = "GDoF/s"
+DIM_X = DIM_V = 3
+DEGREE = 3
+CELLS = 8
+VELOCITY = [1.0, 0.8, 0.6, 0.4, 0.3, 0.2]
+CFL = 0.2
+N_STAGES = 5
+# algorithmic passes over the vector per rk45 step of the fused path:
+# stage 1 reads U, writes U' and T (3); stages 2-4 read T, U and write U, T' (4 each);
+# stage 5 reads T, U and writes U (3)
+PASSES_PER_STEP = 18
+
+
+def workload_config(extra=None):
+    cfg = {
+        "workload": "6D (3x+3v) upwind DG advection, k=3 Gauss-Lobatto collocation, 8^3 x 8^3 cells "
+                    "(262,144 cells, 1,073,741,824 DoFs), periodic unit box, velocity "
+                    "(1.0, 0.8, 0.6, 0.4, 0.3, 0.2), fused rk45 LSRK step, FP32 storage",
+        "dims": "3x+3v", "degree": DEGREE, "cells": "8^3 x 8^3", "n_dofs": 1073741824, "rk": "rk45",
+        "stages": N_STAGES, "initial": "prod_d sin(2 pi x_d + phi_d), phi = default_rng(0).uniform(0, 2 pi, 6)",
+        "l2_flush": "inputs larger than L2 (4.3 GB per FP32 vector vs 129 MB L2)",
+    }
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed region runs."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        if d.get("hbm_gbs"):
+            return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per stage launch from the committed ncu summary of the stage kernel (or None)."""
+    p = os.path.join(ROOT, "profiles", "ecl_stage_6d_k3_f32.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("dram_bytes_per_launch")
+    return None
+
+
+def cpu_sample(threads: int | None = None):
+    """Oracle rk45 step on a 4^3 x 4^3 mesh of the same 6D k=3 problem (16.8M DoFs), all host threads."""
+    import numpy as np
+
+    from oracle import oracle as O
+    O.build()
+    n = os.cpu_count() if threads is None else threads
+    cells = 4
+    prob = O.Problem(DIM_X, DIM_V, DEGREE, [cells] * 6, [0.0] * 6, [1.0] * 6, VELOCITY, n_threads=n)
+    rng = np.random.default_rng(0)
+    phi = rng.uniform(0, 2 * math.pi, 6)
+    f = O.make_func(2, 1.0, omega=[2 * math.pi] * 6, speed=[0.0] * 6, phase=list(phi))
+    u = O.interpolate(prob, f)
+    Ki = np.zeros_like(u)
+    Ti = np.zeros_like(u)
+    dt = 1e-3
+    t0 = time.perf_counter()
+    O.lsrk_step(prob, "rk45", u, 0.0, dt, Ki, Ti)
+    el = time.perf_counter() - t0
+    return {"value": prob.n_dofs * N_STAGES / el / 1e9, "unit": UNIT, "cores": n, "kind": "port",
+            "sample": "one rk45 step of the oracle (CPU restatement, FP64) on the same 6D k=3 problem with "
+                      "4^3 x 4^3 cells (16,777,216 DoFs), %.2f s" % el}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    vals = []
+    for _ in range(max(1, args.warmup_cpu)):
+        cpu_sample()
+    info = None
+    for _ in range(args.steps_cpu):
+        info = cpu_sample()
+        vals.append(info["value"])
+    v = sorted(vals)[len(vals) // 2]
+    info["value"] = v
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps_cpu,
+           "warmup": args.warmup_cpu, "higher_is_better": True, "impl": "reference", "dtype": "f64",
+           "data": "synthetic", "config": workload_config({"cpu_sample_mesh": "4^3 x 4^3 cells"}),
+           "cpu_baseline": info, "vs_baseline": None,
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--steps-f64", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cells-x", type=int, default=CELLS,
+                    help="x-cells per direction (8 = the benchmark workload; smaller only for profiling)")
+    args = ap.parse_args()
+    args.steps_cpu = 3
+    args.warmup_cpu = 1
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    from hyperdeal_gb300 import advection as A
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def make_op(dtype):
+        p = A.AdvectionParameters(DIM_X, DIM_V, DEGREE, [args.cells_x] * 3, [CELLS] * 3, [0.0] * 3, [1.0] * 3,
+                                  [0.0] * 3, [1.0] * 3, VELOCITY, dtype=dtype)
+        return A.AdvectionOperation(p)
+
+    rng = np.random.default_rng(0)
+    phi = list(rng.uniform(0, 2 * math.pi, 6))
+    f0 = A.Function(2, 1.0, omega=[2 * math.pi] * 6, speed=[0.0] * 6, phase=phi)
+
+    op = make_op("f32")
+    n = op.n_dofs
+    dt = CFL * op.critical_time_step() / DEGREE ** 1.5
+    sol = op.initialize_dof_vector()
+    A.VectorTools.interpolate(op, f0, sol, 0.0)
+    Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
+    integ = A.LowStorageRungeKuttaIntegrator(Ki, Ti, "rk45")
+    stream = torch.cuda.current_stream()
+    t = 0.0
+    for _ in range(args.warmup):
+        integ.perform_time_step(sol, t, dt, op)
+        t += dt
+    torch.cuda.synchronize()
+    barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        integ.perform_time_step(sol, t, dt, op)
+        t += dt
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    if dist is not None:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    ms_step = ms / args.steps
+    value = world * n * N_STAGES * args.steps / (ms / 1e3) / 1e9
+
+    # roofline of the dominant kernel (the fused stage kernel, 5 launches per step)
+    peak, peak_kind = measured_peak_hbm()
+    bytes_per_launch = PASSES_PER_STEP / N_STAGES * 4 * n
+    achieved = bytes_per_launch / (ms_step / N_STAGES / 1e3) / 1e9
+    traffic = profiled_traffic()
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+                "bytes_per_launch": bytes_per_launch, "kernel": "hd::ecl_kernel<6,4,float,stage>"}
+
+    # FP64 form of the same steps, and the L2 difference of the two solutions
+    f64 = {}
+    l2 = None
+    if args.steps_f64 > 0:
+        op64 = make_op("f64")
+        s64 = op64.initialize_dof_vector()
+        A.VectorTools.interpolate(op64, f0, s64, 0.0)
+        K64, T64 = op64.initialize_dof_vector(), op64.initialize_dof_vector()
+        i64 = A.LowStorageRungeKuttaIntegrator(K64, T64, "rk45")
+        t64 = 0.0
+        for _ in range(args.warmup):
+            i64.perform_time_step(s64, t64, dt, op64)
+            t64 += dt
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps_f64):
+            i64.perform_time_step(s64, t64, dt, op64)
+            t64 += dt
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1) / args.steps_f64
+        v64 = n * N_STAGES / (ms64 / 1e3) / 1e9
+        f64 = {"value": round(v64, 3), "ms_per_step": round(ms64, 3), "steps": args.steps_f64}
+        # same number of steps from the same initial data in both forms
+        s32 = op.initialize_dof_vector()
+        A.VectorTools.interpolate(op, f0, s32, 0.0)
+        s64b = op64.initialize_dof_vector()
+        A.VectorTools.interpolate(op64, f0, s64b, 0.0)
+        nsteps = args.warmup + args.steps_f64
+        tt = 0.0
+        for _ in range(nsteps):
+            integ.perform_time_step(s32, tt, dt, op)
+            i64.perform_time_step(s64b, tt, dt, op64)
+            tt += dt
+        d = (s32.double() - s64b)
+        l2 = float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(s64b))
+        f64["l2_compared_after_steps"] = nsteps
+        del op64, s64, K64, T64, i64, s64b, d, s32
+        torch.cuda.empty_cache()
+
+    # end to end through the public API with host buffers: H2D of the state, one fused step, D2H
+    e2e = None
+    if not args.no_e2e:
+        host_in = torch.empty(n, dtype=torch.float32, pin_memory=True)
+        host_in.copy_(sol)
+        host_out = torch.empty(n, dtype=torch.float32, pin_memory=True)
+        k_e2e = max(3, min(args.steps, 5))
+        for _ in range(2):
+            sol.copy_(host_in, non_blocking=True)
+            integ.perform_time_step(sol, t, dt, op)
+            host_out.copy_(sol, non_blocking=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(k_e2e):
+            sol.copy_(host_in, non_blocking=True)
+            integ.perform_time_step(sol, t, dt, op)
+            host_out.copy_(sol, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_e2e = e0.elapsed_time(e1) / k_e2e
+        e2e = {"value": round(world * n * N_STAGES / (ms_e2e / 1e3) / 1e9, 3), "unit": UNIT,
+               "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": 4 * n, "ms_per_step": round(ms_e2e, 3),
+               "steps": k_e2e, "path": "hd_lsrk_step (C ABI) with pinned host state copied in and out every step"}
+        del host_in, host_out
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_sample()
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": workload_config({"parallelism": "replicas" if world > 1 else "single GPU",
+                                          **({} if args.cells_x == CELLS else
+                                             {"profiling_case_cells": "%d^3 x 8^3" % args.cells_x,
+                                              "n_dofs": n})}),
+               "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+               "gpu_launches": N_STAGES * args.steps,
+               "f64_form": f64, "f32_over_f64": round(value / f64["value"], 3) if f64 else None,
+               "l2_rel_err_f32_vs_f64": l2}
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

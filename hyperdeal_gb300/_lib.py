@@ -20,7 +20,9 @@ EXPORTED_SYMBOLS = (
     "hd_last_error", "hd_version", "hd_adv_create", "hd_adv_destroy", "hd_adv_n_dofs", "hd_adv_apply",
     "hd_adv_critical_time_step", "hd_interpolate", "hd_norm_and_error", "hd_lsrk_create", "hd_lsrk_destroy",
     "hd_lsrk_n_stages", "hd_lsrk_step", "hd_lsrk_step_unfused", "hd_lsrk_stage_update", "hd_lsrk_coefficients",
+    "hd_adv_set_kernel", "hd_adv_kernel", "hd_adv_device_status",
 )
+HD_KERNEL_AUTO, HD_KERNEL_GENERIC, HD_KERNEL_PIPELINED = 0, 1, 2
 
 
 class HdError(RuntimeError):
@@ -73,6 +75,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.hd_adv_n_dofs.argtypes = [vp]
     L.hd_adv_n_dofs.restype = ctypes.c_longlong
     L.hd_adv_apply.argtypes = [vp, vp, vp, ctypes.c_double, vp]
+    L.hd_adv_set_kernel.argtypes = [vp, ctypes.c_int]
+    L.hd_adv_kernel.argtypes = [vp]
+    L.hd_adv_device_status.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     L.hd_adv_critical_time_step.argtypes = [vp]
     L.hd_adv_critical_time_step.restype = ctypes.c_double
     L.hd_interpolate.argtypes = [vp, ctypes.POINTER(hd_function), ctypes.c_double, vp, vp]

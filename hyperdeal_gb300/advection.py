@@ -158,6 +158,23 @@ class AdvectionOperation:
     def critical_time_step(self) -> float:
         return float(self._L.hd_adv_critical_time_step(self._h))
 
+    def set_kernel(self, variant: str) -> None:
+        """'auto', 'generic' or 'pipelined' (see hd_adv_set_kernel)."""
+        v = {"auto": _lib.HD_KERNEL_AUTO, "generic": _lib.HD_KERNEL_GENERIC,
+             "pipelined": _lib.HD_KERNEL_PIPELINED}[variant]
+        check(self._L.hd_adv_set_kernel(self._h, v))
+
+    @property
+    def kernel(self) -> str:
+        return {_lib.HD_KERNEL_GENERIC: "generic", _lib.HD_KERNEL_PIPELINED: "pipelined"}[
+            int(self._L.hd_adv_kernel(self._h))]
+
+    def device_status(self) -> int:
+        """Error code recorded by the device since the last call (0 = none); synchronises."""
+        st = ctypes.c_int(0)
+        check(self._L.hd_adv_device_status(self._h, ctypes.byref(st)))
+        return int(st.value)
+
 
 def compute_critical_time_step(op: AdvectionOperation) -> float:
     return op.critical_time_step()

@@ -197,8 +197,10 @@ struct hd_adv {
   hd::EclParams<double> p64;
   hd::EclParams<float> p32;
   hd::VecGeom geom;
-  double* d_partials;  // norm reduction scratch (2*kNormBlocks + 2 doubles)
+  double* d_partials;  // norm reduction scratch (2*kNormBlocks + 2 doubles) + error flag
+  int* d_err;          // device error flag of the pipelined kernel (inside d_partials)
   int device;
+  int variant;         // HD_KERNEL_AUTO / _GENERIC / _PIPELINED
 };
 
 struct hd_lsrk {
@@ -226,6 +228,8 @@ void fill_params(const hd_adv* op, hd::EclParams<T>* P) {
     const LineOpD& L = op->ops[d];
     for (int i = 0; i < op->N * op->N; ++i) P->op[d].M[i] = T(L.M[i]);
     P->op[d].cin = T(L.cin);
+    P->op[d].c0 = L.in_node == 0 ? T(L.cin) : T(0);
+    P->op[d].cl = L.in_node == op->N - 1 ? T(L.cin) : T(0);
     P->op[d].in_node = L.in_node;
     P->op[d].nb_node = L.nb_node;
     P->op[d].step = L.step;
@@ -248,10 +252,22 @@ hd::EclLaunchers get_launchers(int D, int N) {
   }
 }
 
+// kernel that runs for this operator (HD_KERNEL_GENERIC or HD_KERNEL_PIPELINED)
+int selected_kernel(const hd_adv* op) {
+  const bool pipelined_ok = op->dtype == HD_F32 && op->N == 4 && hd::ecl6_eligible(op->p32);
+  if (op->variant == HD_KERNEL_GENERIC) return HD_KERNEL_GENERIC;
+  return pipelined_ok ? HD_KERNEL_PIPELINED : HD_KERNEL_GENERIC;
+}
+
 int launch(hd_adv* op, int mode, const void* tin, const void* uin, void* uout, void* tout, double fb,
            double fa, double time, cudaStream_t s) {
   cudaError_t e;
-  if (op->dtype == HD_F64) {
+  if (selected_kernel(op) == HD_KERNEL_PIPELINED) {
+    hd::EclParams<float> P = op->p32;
+    P.tin = (const float*)tin; P.uin = (const float*)uin; P.uout = (float*)uout; P.tout = (float*)tout;
+    P.fb = float(fb); P.fa = float(fa); P.time = time;
+    e = hd::launch_ecl6(P, op->d_err, mode, s);
+  } else if (op->dtype == HD_F64) {
     hd::EclParams<double> P = op->p64;
     P.tin = (const double*)tin; P.uin = (const double*)uin; P.uout = (double*)uout; P.tout = (double*)tout;
     P.fb = fb; P.fa = fa; P.time = time;
@@ -353,8 +369,12 @@ int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
     for (int i = 0; i < op->N; ++i) { g.gl[i] = op->gl[i]; g.glw[i] = op->glw[i]; }
     cudaError_t e = cudaGetDevice(&op->device);
     if (e != cudaSuccess) { delete op; return cuda_fail(e, "cudaGetDevice"); }
-    e = cudaMalloc(&op->d_partials, sizeof(double) * (2 * hd::kNormBlocks + 2));
+    e = cudaMalloc(&op->d_partials, sizeof(double) * (2 * hd::kNormBlocks + 3));
     if (e != cudaSuccess) { delete op; return cuda_fail(e, "cudaMalloc (norm scratch)"); }
+    op->d_err = reinterpret_cast<int*>(op->d_partials + 2 * hd::kNormBlocks + 2);
+    e = cudaMemset(op->d_err, 0, sizeof(int));
+    if (e != cudaSuccess) { cudaFree(op->d_partials); delete op; return cuda_fail(e, "cudaMemset (error flag)"); }
+    op->variant = HD_KERNEL_AUTO;
     *out = op;
     return HD_OK;
   } catch (...) {
@@ -370,6 +390,31 @@ int hd_adv_destroy(hd_adv* op) {
 }
 
 long long hd_adv_n_dofs(const hd_adv* op) { return op ? op->n_dofs : -1; }
+
+int hd_adv_set_kernel(hd_adv* op, int variant) {
+  if (!op) return fail(HD_ERR_INVALID, "hd_adv_set_kernel: null handle");
+  if (variant != HD_KERNEL_AUTO && variant != HD_KERNEL_GENERIC && variant != HD_KERNEL_PIPELINED)
+    return fail(HD_ERR_INVALID, "unknown kernel variant %d", variant);
+  if (variant == HD_KERNEL_PIPELINED && !(op->dtype == HD_F32 && op->N == 4 && hd::ecl6_eligible(op->p32)))
+    return fail(HD_ERR_UNSUPPORTED, "the pipelined kernel needs a fully periodic 3x+3v mesh, degree 3, FP32");
+  op->variant = variant;
+  return HD_OK;
+}
+
+int hd_adv_kernel(const hd_adv* op) { return op ? selected_kernel(op) : -1; }
+
+int hd_adv_device_status(hd_adv* op, int* status) {
+  if (!op || !status) return fail(HD_ERR_INVALID, "hd_adv_device_status: null argument");
+  int v = 0;
+  cudaError_t e = cudaMemcpy(&v, op->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "read device error flag");
+  *status = v;
+  if (v) {
+    e = cudaMemset(op->d_err, 0, sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(e, "clear device error flag");
+  }
+  return HD_OK;
+}
 
 double hd_adv_critical_time_step(const hd_adv* op) {
   if (!op) return -1.0;

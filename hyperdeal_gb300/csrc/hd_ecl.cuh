@@ -41,6 +41,7 @@ template <typename T>
 struct LineOp {
   T M[kMaxN * kMaxN];  // out_i += M[i*N + q] * u_q
   T cin;               // out_{in_node} += cin * u+
+  T c0, cl;            // the same coefficient split by target: node 0 / node N-1 (the other is 0)
   int in_node;         // node of the line that receives the inflow term
   int nb_node;         // node of the upwind neighbour's line giving u+
   int step;            // -1: upwind neighbour on the left, +1: on the right
@@ -229,15 +230,12 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
               for (int q = 0; q < N; ++q) s = fma(L.M[i * N + q], uu[q][b], s);
               acc[i][b] = s;
             }
-            T up;
-            const int in = L.in_node;
-            T um = T(0);
-#pragma unroll
-            for (int q = 0; q < N; ++q) if (q == in) um = uu[q][b];
-            if (nbA >= 0) up = __ldg(P.tin + nbA * NC + base + L.nb_node * strideA + b * strideB);
-            else up = boundary_value<D, N, T>(P, cc, dA, base + in * strideA + b * strideB, um);
-#pragma unroll
-            for (int q = 0; q < N; ++q) if (q == in) acc[q][b] = fma(L.cin, up, acc[q][b]);
+            const bool first = L.in_node == 0;
+            const T um = first ? uu[0][b] : uu[N - 1][b];
+            const T up = nbA >= 0 ? __ldg(P.tin + nbA * NC + base + L.nb_node * strideA + b * strideB)
+                                  : boundary_value<D, N, T>(P, cc, dA, base + L.in_node * strideA + b * strideB, um);
+            acc[0][b] = fma(L.c0, up, acc[0][b]);
+            acc[N - 1][b] = fma(L.cl, up, acc[N - 1][b]);
           }
         }
         if (valid && P.op[dB].active) {
@@ -251,15 +249,12 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
               for (int q = 0; q < N; ++q) s = fma(L.M[i * N + q], uu[a][q], s);
               acc[a][i] = s;
             }
-            T up;
-            const int in = L.in_node;
-            T um = T(0);
-#pragma unroll
-            for (int q = 0; q < N; ++q) if (q == in) um = uu[a][q];
-            if (nbB >= 0) up = __ldg(P.tin + nbB * NC + base + a * strideA + L.nb_node * strideB);
-            else up = boundary_value<D, N, T>(P, cc, dB, base + a * strideA + in * strideB, um);
-#pragma unroll
-            for (int q = 0; q < N; ++q) if (q == in) acc[a][q] = fma(L.cin, up, acc[a][q]);
+            const bool first = L.in_node == 0;
+            const T um = first ? uu[a][0] : uu[a][N - 1];
+            const T up = nbB >= 0 ? __ldg(P.tin + nbB * NC + base + a * strideA + L.nb_node * strideB)
+                                  : boundary_value<D, N, T>(P, cc, dB, base + a * strideA + L.in_node * strideB, um);
+            acc[a][0] = fma(L.c0, up, acc[a][0]);
+            acc[a][N - 1] = fma(L.cl, up, acc[a][N - 1]);
           }
         }
         if (!last) {
@@ -302,15 +297,11 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
             for (int q = 0; q < N; ++q) s = fma(L.M[i * N + q], uu[q], s);
             acc[i] = s;
           }
-          const int in = L.in_node;
-          T um = T(0);
-#pragma unroll
-          for (int q = 0; q < N; ++q) if (q == in) um = uu[q];
-          T up;
-          if (nbA >= 0) up = __ldg(P.tin + nbA * NC + base + L.nb_node * strideA);
-          else up = boundary_value<D, N, T>(P, cc, dA, base + in * strideA, um);
-#pragma unroll
-          for (int q = 0; q < N; ++q) if (q == in) acc[q] = fma(L.cin, up, acc[q]);
+          const T um = L.in_node == 0 ? uu[0] : uu[N - 1];
+          const T up = nbA >= 0 ? __ldg(P.tin + nbA * NC + base + L.nb_node * strideA)
+                                : boundary_value<D, N, T>(P, cc, dA, base + L.in_node * strideA, um);
+          acc[0] = fma(L.c0, up, acc[0]);
+          acc[N - 1] = fma(L.cl, up, acc[N - 1]);
         }
         if (!last) {
 #pragma unroll
@@ -380,6 +371,11 @@ EclLaunchers make_launchers() {
   return EclLaunchers{&launch_ecl<D, N, double>, &launch_ecl<D, N, float>, S64::SMEM, S32::SMEM,
                       S64::THREADS, S32::THREADS, S64::CPB, S32::CPB, S64::SUPPORTED, S32::SUPPORTED};
 }
+
+// pipelined 6D degree-3 FP32 kernel (hd_ecl6.cu): eligible for fully periodic
+// 3x+3v meshes; err receives a device error code on a bounded-wait time-out
+bool ecl6_eligible(const EclParams<float>& P);
+cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int mode, cudaStream_t stream);
 
 // defined in hd_ecl_d{2..6}.cu
 EclLaunchers ecl_launchers_d2(int N);

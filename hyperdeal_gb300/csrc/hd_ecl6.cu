@@ -1,0 +1,110 @@
+// hd_ecl6.cu -- host side of the pipelined 6D degree-3 FP32 kernel:
+// tensor-map encoding (through the driver entry point, no -lcuda) and launch.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <mutex>
+
+#include "hd_ecl6.cuh"
+
+namespace hd {
+
+namespace {
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// rank-3 view [outer][4][inner] of the vector with a box of one face (index 1 fixed)
+bool encode_trace(EncodeTiledFn enc, CUtensorMap* m, const float* base, long long n, cuuint64_t inner,
+                  cuuint32_t box_outer) {
+  cuuint64_t dims[3] = {inner, 4, cuuint64_t(n) / (inner * 4)};
+  cuuint64_t strides[2] = {inner * 4, inner * 16};
+  cuuint32_t box[3] = {cuuint32_t(inner), 1, box_outer};
+  cuuint32_t es[3] = {1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+cudaError_t encode_ecl6_maps(const float* base, long long n, Ecl6Maps* m) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return cudaErrorNotSupported;
+  std::memset(m, 0, sizeof(*m));
+  {
+    cuuint64_t dims[2] = {32, cuuint64_t(n) / 32};
+    cuuint64_t strides[1] = {128};
+    cuuint32_t box[2] = {32, 128};
+    cuuint32_t es[2] = {1, 1};
+    if (enc(&m->tcell, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+  }
+  // faces of x1 (inner 4), x2 (16), v0 (64), v1 (256); one cell = 1024 / inner outer rows
+  const cuuint64_t inner[4] = {4, 16, 64, 256};
+  for (int d = 0; d < 4; ++d)
+    if (!encode_trace(enc, &m->tr[d], base, n, inner[d], cuuint32_t(1024 / inner[d])))
+      return cudaErrorInvalidValue;
+  return cudaSuccess;
+}
+
+bool ecl6_eligible(const EclParams<float>& P) {
+  if (P.D != 6 || P.dim_x != 3) return false;
+  for (int d = 0; d < 6; ++d)
+    if (!P.periodic[d]) return false;
+  if (P.n_cells * 4096LL > (1LL << 36)) return false;  // TMA row coordinate range
+  return true;
+}
+
+cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int mode, cudaStream_t stream) {
+  Ecl6Params E;
+  E.p = P;
+  E.row_len = P.cells[0];
+  E.n_rows = int(P.n_cells / P.cells[0]);
+  E.err = err;
+  Ecl6Maps maps;
+  cudaError_t e = encode_ecl6_maps(P.tin, P.n_cells * 4096LL, &maps);
+  if (e != cudaSuccess) return e;
+  static bool attr_done[4] = {false, false, false, false};
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int grid = 2 * sms;
+  if (grid > E.n_rows) grid = E.n_rows;
+  auto go = [&](auto kern) -> cudaError_t {
+    if (!attr_done[mode]) {
+      cudaError_t ee = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, E6_SMEM);
+      if (ee != cudaSuccess) return ee;
+      attr_done[mode] = true;
+    }
+    kern<<<grid, E6_THREADS, E6_SMEM, stream>>>(E, maps);
+    return cudaGetLastError();
+  };
+  switch (mode) {
+    case kApply: return go(ecl6_kernel<kApply>);
+    case kStageFirst: return go(ecl6_kernel<kStageFirst>);
+    case kStageMid: return go(ecl6_kernel<kStageMid>);
+    case kStageLast: return go(ecl6_kernel<kStageLast>);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace hd

@@ -107,6 +107,19 @@ int hd_adv_destroy(hd_adv *op);
 /* Number of DoFs = prod(cells) * (k+1)^(dim_x+dim_v). */
 long long hd_adv_n_dofs(const hd_adv *op);
 
+/* Kernel selection: AUTO picks the persistent TMA-pipelined kernel where it
+ * applies (FP32, degree 3, fully periodic 3x+3v mesh) and the generic
+ * shared-memory kernel otherwise; GENERIC forces the latter.  Both compute
+ * the same operator.  hd_adv_kernel() returns the kernel that will run. */
+enum hd_kernel { HD_KERNEL_AUTO = 0, HD_KERNEL_GENERIC = 1, HD_KERNEL_PIPELINED = 2 };
+int hd_adv_set_kernel(hd_adv *op, int variant);
+int hd_adv_kernel(const hd_adv *op);
+
+/* Device-side error code of the pipelined kernel since the last call (0 = none;
+ * 1/2 = a bounded wait on a copy / buffer slot timed out and the kernel
+ * returned early).  Synchronises the device; clears the flag. */
+int hd_adv_device_status(hd_adv *op, int *status);
+
 /* dst = M^{-1} A(src) at `time` (boundary data time), i.e.
  * AdvectionOperation::apply<all>(dst, src, time) in its ECL branch
  * (advection_operation.h:134-209, :218-566).  dst is overwritten; dst and src

@@ -234,3 +234,58 @@ def test_full_size_6d_f32_properties():
     mass = (K.double() @ w6).sum().item()
     scale = (K.double().abs() @ w6).sum().item()
     assert abs(mass) <= 1e-6 * scale
+
+
+PIPE_CASES = [
+    ([2, 3, 2, 2, 2, 3], [1.0, 0.8, 0.6, 0.4, 0.3, 0.2]),
+    ([3, 2, 2, 3, 2, 2], [-1.0, 0.8, -0.6, 0.4, -0.3, 0.2]),
+    ([1, 2, 2, 2, 2, 1], [0.5, -0.7, 0.0, 1.2, -0.3, 0.9]),
+    ([5, 1, 2, 3, 1, 2], [-0.2, 0.0, 0.6, -0.4, 0.3, -0.25]),
+    ([4, 4, 4, 4, 4, 4], [1.0, 0.8, 0.6, 0.4, 0.3, 0.2]),
+]
+
+
+@pytest.mark.parametrize("cells,vel", PIPE_CASES, ids=["c%d" % i for i in range(len(PIPE_CASES))])
+def test_pipelined_kernel_matches_oracle_and_generic(cells, vel):
+    rng = np.random.default_rng(11)
+    lo = list(rng.uniform(-1, 0, 6))
+    hi = [l + rng.uniform(0.5, 2.0) for l in lo]
+    op, prob = make(3, 3, 3, cells, vel, lo, hi, dtype="f32")
+    assert op.kernel == "pipelined"
+    u = rng.standard_normal(prob.n_dofs).astype(np.float32)
+    src = torch.tensor(u, device="cuda")
+    d_pipe = op.initialize_dof_vector()
+    op.apply(d_pipe, src, 0.0)
+    assert op.device_status() == 0
+    op.set_kernel("generic")
+    assert op.kernel == "generic"
+    d_gen = op.initialize_dof_vector()
+    op.apply(d_gen, src, 0.0)
+    ref = O.apply(prob, u.astype(np.float64))
+    assert rel_err(d_pipe.double().cpu().numpy(), ref) <= F32_TOL
+    assert rel_err(d_pipe.double().cpu().numpy(), d_gen.double().cpu().numpy()) <= 1e-6
+    # fused LSRK steps through both kernels
+    sols = []
+    for kern in ("pipelined", "generic"):
+        op.set_kernel(kern)
+        sol = src.clone()
+        Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
+        integ = A.LowStorageRungeKuttaIntegrator(Ki, Ti, "rk45")
+        for s in range(3):
+            integ.perform_time_step(sol, s * 1e-3, 1e-3, op)
+        sols.append(sol.double().cpu().numpy())
+    assert op.device_status() == 0
+    assert rel_err(sols[0], sols[1]) <= 1e-6
+    uo = u.astype(np.float64)
+    for s in range(3):
+        O.lsrk_step(prob, "rk45", uo, s * 1e-3, 1e-3)
+    assert rel_err(sols[0], uo) <= 2e-5
+
+
+def test_pipelined_kernel_selection_rules():
+    op, _ = make(3, 3, 3, [2] * 6, [1.0] * 6, dtype="f32", periodic=(True, False))
+    assert op.kernel == "generic"
+    with pytest.raises(A.HdError):
+        op.set_kernel("pipelined")
+    op64, _ = make(3, 3, 3, [2] * 6, [1.0] * 6, dtype="f64")
+    assert op64.kernel == "generic"
