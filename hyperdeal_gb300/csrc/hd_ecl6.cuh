@@ -40,7 +40,7 @@ constexpr int E6_CTHREADS = 256;  // compute threads
 constexpr int E6_THREADS = 288;   // + one producer warp
 constexpr int E6_STAGES = 2;
 constexpr int E6_STAGE_BYTES = 16384 + 5 * 4096;  // cell tile + 5 traces
-constexpr int E6_OUT_BYTES = 16384;
+constexpr int E6_OUT_BYTES = 2 * 16384;  // double-buffered accumulator tile
 constexpr int E6_SMEM = 1024 /*alignment slack*/ + E6_STAGES * E6_STAGE_BYTES + E6_OUT_BYTES + 64;
 constexpr unsigned E6_WAIT_LIMIT = 1u << 22;  // try_wait rounds before giving up (~seconds)
 
@@ -148,17 +148,17 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   float* s_stage = reinterpret_cast<float*>(base);
-  float* s_out = reinterpret_cast<float*>(base + E6_STAGES * E6_STAGE_BYTES);
+  float* s_out = reinterpret_cast<float*>(base + E6_STAGES * E6_STAGE_BYTES);  // 2 accumulator tiles
   uint64_t* bars = reinterpret_cast<uint64_t*>(base + E6_STAGES * E6_STAGE_BYTES + E6_OUT_BYTES);
-  uint64_t* full = bars;               // [E6_STAGES]
-  uint64_t* empty = bars + E6_STAGES;  // [E6_STAGES]
+  uint64_t* full = bars;               // [E6_STAGES]: TMA bytes landed
+  uint64_t* empty = bars + E6_STAGES;  // [E6_STAGES]: all 8 compute warps done with the slot
   volatile int* s_abort = reinterpret_cast<volatile int*>(bars + 2 * E6_STAGES);
 
   const int tid = threadIdx.x;
   if (tid == 0) {
     for (int s = 0; s < E6_STAGES; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+      mbar_init(&empty[s], E6_CTHREADS / 32);
     }
     *s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -173,10 +173,14 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
     if (tid == E6_CTHREADS) {
       int issued = 0;
       bool ok = true;
+      uint32_t bytes = 16384;
+#pragma unroll
+      for (int d = 1; d < 6; ++d) bytes += P.p.op[d].active ? 4096u : 0u;
       for (int it = 0; it < n_cells_cta; ++it) {
         const int s = it % E6_STAGES;
         if (it >= E6_STAGES && !mbar_wait(&empty[s], ((it / E6_STAGES) - 1) & 1)) {
           atomicExch(P.err, E6_ERR_TIMEOUT_EMPTY);
+          *s_abort = 1;
           ok = false;
           break;
         }
@@ -184,9 +188,6 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
         const int r = (int)blockIdx.x + (it / P.row_len) * (int)gridDim.x;
         const long long gid = e6_cell(P, r, it % P.row_len);
         float* st = s_stage + s * (E6_STAGE_BYTES / 4);
-        uint32_t bytes = 16384;
-#pragma unroll
-        for (int d = 1; d < 6; ++d) bytes += P.p.op[d].active ? 4096u : 0u;
         mbar_arrive_expect_tx(&full[s], bytes);
         tma_load_2d(st, &maps.tcell, 0, int(gid * 128), &full[s]);
         // upwind traces (face node nb_node of the upwind neighbour)
@@ -200,10 +201,8 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
                     &full[s]);
         ++issued;
       }
-      (void)ok;
-      // drain: wait (bounded) for every issued load the consumers did not consume
-      // (on the normal path the consumers waited for all of them already)
-      if (!ok || *s_abort) {
+      // on an abort, wait (bounded) for the copies still in flight before leaving
+      if (!ok) {
         for (int it = issued - E6_STAGES < 0 ? 0 : issued - E6_STAGES; it < issued; ++it)
           mbar_wait(&full[it % E6_STAGES], (it / E6_STAGES) & 1);
       }
@@ -214,7 +213,26 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
   // -------------------------------------------------------------------- consumers
   const LineOp<float>* L = P.p.op;
   float carry[4] = {0.f, 0.f, 0.f, 0.f};
-  const long long NC = 4096;
+  constexpr long long NC = 4096;
+  const int lane = tid & 31, warp = tid >> 5;
+
+  // per-thread shared-memory offsets (floats); the compile-time parts are added per access
+  // phase 0: plane 16*tid + a + 4b, rows tid>>1 of the swizzled tiles
+  const int row0 = tid >> 1;
+  const int t0_chunk = (4 * (tid & 1)) ^ (row0 & 7);
+  const int o0_chunk = (4 * (tid & 1)) ^ (row0 & 7) ^ (((row0 >> 3) & 1) << 2);
+  // phase 1: nodes (lo + 256 hi) + 16a + 64b; R = (a>>1) + 2b picks the row, a&1 the chunk bit 2
+  const int lo = tid & 15, hi = tid >> 4;
+  int tb1[4], ob1[4][2];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    tb1[r] = 256 * hi + (lo & 3) + 4 * ((lo >> 2) ^ r);
+    ob1[r][0] = tb1[r] + 16 * (hi & 1);
+    ob1[r][1] = tb1[r] + 16 - 16 * (hi & 1);
+  }
+  // phase 2: nodes tid + 256a + 1024b; row & 7 = warp
+  const int tb2 = (tid & ~28) | ((((tid >> 2) & 7) ^ warp) << 2);
+  const int ob2[2] = {tb2, (tid & ~28) | ((((tid >> 2) & 7) ^ warp ^ 4) << 2)};
 
   for (int it = 0; it < n_cells_cta; ++it) {
     const int s = it % E6_STAGES;
@@ -222,11 +240,11 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
     const int r = (int)blockIdx.x + (it / P.row_len) * (int)gridDim.x;
     const long long gid = e6_cell(P, r, k);
     const float* st = s_stage + s * (E6_STAGE_BYTES / 4);
+    float* so = s_out + (it & 1) * 4096;
 
     // row start: x0 face of the upwind neighbour of the row's first cell
     if (k == 0 && L[0].active) {
-      const long long g0 = e6_nb(P, gid, 0);
-      const float* src = P.p.tin + g0 * NC + 16 * tid + L[0].nb_node;
+      const float* src = P.p.tin + e6_nb(P, gid, 0) * NC + 16 * tid + L[0].nb_node;
 #pragma unroll
       for (int b = 0; b < 4; ++b) carry[b] = __ldg(src + 4 * b);
     }
@@ -240,21 +258,19 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
         for (int a = 0; a < 4; ++a) uU[a + 4 * b] = __ldg(up + 256 * a + 1024 * b);
     }
 
-    if (tid == 0) *s_abort = mbar_wait(&full[s], (it / E6_STAGES) & 1) ? 0 : 1;
-    bar_compute();
-    if (*s_abort) {
-      if (tid == 0) atomicExch(P.err, E6_ERR_TIMEOUT_FULL);
-      return;
+    // every compute thread waits for the slot (bounded); a time-out turns the
+    // rest of the CTA's work into no-ops (no stores) without leaving any barrier
+    if (!*s_abort && !mbar_wait(&full[s], (it / E6_STAGES) & 1)) {
+      *s_abort = 1;
+      atomicExch(P.err, E6_ERR_TIMEOUT_FULL);
     }
 
     // ---------------- phase 0: directions x0 (a) and x1 (b); plane = nodes 16*tid + a + 4b
     {
       float uu[4][4], acc[4][4];
-      const int row = tid >> 1;
 #pragma unroll
       for (int b = 0; b < 4; ++b) {
-        const int ch = (((tid & 1) * 4 + b) ^ (row & 7));
-        const float4 v = *reinterpret_cast<const float4*>(st + row * 32 + ch * 4);
+        const float4 v = *reinterpret_cast<const float4*>(st + row0 * 32 + ((t0_chunk ^ b) << 2));
         uu[0][b] = v.x; uu[1][b] = v.y; uu[2][b] = v.z; uu[3][b] = v.w;
       }
 #pragma unroll
@@ -296,27 +312,26 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
         }
       }
 #pragma unroll
-      for (int b = 0; b < 4; ++b) {
-        const int node = 16 * tid + 4 * b;
-        *reinterpret_cast<float4*>(s_out + swz_o(node)) = make_float4(acc[0][b], acc[1][b], acc[2][b], acc[3][b]);
-      }
+      for (int b = 0; b < 4; ++b)
+        *reinterpret_cast<float4*>(so + row0 * 32 + ((o0_chunk ^ b) << 2)) =
+            make_float4(acc[0][b], acc[1][b], acc[2][b], acc[3][b]);
     }
     bar_compute();
 
     // ---------------- phase 1: directions x2 (a, stride 16) and v0 (b, stride 64)
     {
-      const int lo = tid & 15, hi = tid >> 4;
-      const int pb = lo + 256 * hi;
       float uu[4][4], acc[4][4];
 #pragma unroll
       for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-          const int node = pb + 16 * a + 64 * b;
-          uu[a][b] = st[swz_t(node)];
-          acc[a][b] = s_out[swz_o(node)];
+          const int R = (a >> 1) + 2 * b;
+          const int e = (a & 1) ^ (R >> 2);
+          uu[a][b] = st[tb1[R & 3] + 32 * R + 16 * e];
+          acc[a][b] = so[ob1[R & 3][e] + 32 * R];
         }
       if (L[2].active) {
+        const float* tr = st + 5120 + 64 * hi + lo;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
 #pragma unroll
@@ -326,12 +341,13 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
             for (int q = 0; q < 4; ++q) sacc = fmaf(L[2].M[i * 4 + q], uu[q][b], sacc);
             acc[i][b] = sacc;
           }
-          const float up = st[4096 + 1024 + 16 * b + 64 * hi + lo];
-acc[0][b] = fmaf(L[2].c0, up, acc[0][b]);
+          const float up = tr[16 * b];
+          acc[0][b] = fmaf(L[2].c0, up, acc[0][b]);
           acc[3][b] = fmaf(L[2].cl, up, acc[3][b]);
         }
       }
       if (L[3].active) {
+        const float* tr = st + 6144 + 64 * hi + lo;
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
 #pragma unroll
@@ -341,15 +357,19 @@ acc[0][b] = fmaf(L[2].c0, up, acc[0][b]);
             for (int q = 0; q < 4; ++q) sacc = fmaf(L[3].M[i * 4 + q], uu[a][q], sacc);
             acc[a][i] = sacc;
           }
-          const float up = st[4096 + 2048 + 64 * hi + lo + 16 * a];
-acc[a][0] = fmaf(L[3].c0, up, acc[a][0]);
+          const float up = tr[16 * a];
+          acc[a][0] = fmaf(L[3].c0, up, acc[a][0]);
           acc[a][3] = fmaf(L[3].cl, up, acc[a][3]);
         }
       }
 #pragma unroll
       for (int a = 0; a < 4; ++a)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) s_out[swz_o(pb + 16 * a + 64 * b)] = acc[a][b];
+        for (int b = 0; b < 4; ++b) {
+          const int R = (a >> 1) + 2 * b;
+          const int e = (a & 1) ^ (R >> 2);
+          so[ob1[R & 3][e] + 32 * R] = acc[a][b];
+        }
     }
     bar_compute();
 
@@ -360,11 +380,11 @@ acc[a][0] = fmaf(L[3].c0, up, acc[a][0]);
       for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-          const int node = tid + 256 * a + 1024 * b;
-          uu[a][b] = st[swz_t(node)];
-          acc[a][b] = s_out[swz_o(node)];
+          uu[a][b] = st[tb2 + 256 * a + 1024 * b];
+          acc[a][b] = so[ob2[a & 1] + 256 * a + 1024 * b];
         }
       if (L[4].active) {
+        const float* tr = st + 7168 + tid;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
 #pragma unroll
@@ -374,12 +394,13 @@ acc[a][0] = fmaf(L[3].c0, up, acc[a][0]);
             for (int q = 0; q < 4; ++q) sacc = fmaf(L[4].M[i * 4 + q], uu[q][b], sacc);
             acc[i][b] = sacc;
           }
-          const float up = st[4096 + 3072 + 256 * b + tid];
-acc[0][b] = fmaf(L[4].c0, up, acc[0][b]);
+          const float up = tr[256 * b];
+          acc[0][b] = fmaf(L[4].c0, up, acc[0][b]);
           acc[3][b] = fmaf(L[4].cl, up, acc[3][b]);
         }
       }
       if (L[5].active) {
+        const float* tr = st + 8192 + tid;
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
 #pragma unroll
@@ -389,29 +410,33 @@ acc[0][b] = fmaf(L[4].c0, up, acc[0][b]);
             for (int q = 0; q < 4; ++q) sacc = fmaf(L[5].M[i * 4 + q], uu[a][q], sacc);
             acc[a][i] = sacc;
           }
-          const float up = st[4096 + 4096 + tid + 256 * a];
-acc[a][0] = fmaf(L[5].c0, up, acc[a][0]);
+          const float up = tr[256 * a];
+          acc[a][0] = fmaf(L[5].c0, up, acc[a][0]);
           acc[a][3] = fmaf(L[5].cl, up, acc[a][3]);
         }
       }
-      const long long g0 = gid * NC + tid;
+      // this warp is done with the stage slot
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+      if (!*s_abort) {
+        float* go = P.p.uout + gid * NC + tid;
+        float* gt = P.p.tout + gid * NC + tid;
 #pragma unroll
-      for (int b = 0; b < 4; ++b)
+        for (int b = 0; b < 4; ++b)
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          const long long gi = g0 + 256 * a + 1024 * b;
-          const float kk = acc[a][b];
-          if constexpr (MODE == kApply) {
-            P.p.uout[gi] = kk;
-          } else {
-            const float u = (MODE == kStageFirst) ? uu[a][b] : uU[a + 4 * b];
-            P.p.uout[gi] = fmaf(P.p.fb, kk, u);
-            if constexpr (MODE != kStageLast) P.p.tout[gi] = fmaf(P.p.fa, kk, u);
+          for (int a = 0; a < 4; ++a) {
+            const int off = 256 * a + 1024 * b;
+            const float kk = acc[a][b];
+            if constexpr (MODE == kApply) {
+              go[off] = kk;
+            } else {
+              const float u = (MODE == kStageFirst) ? uu[a][b] : uU[a + 4 * b];
+              go[off] = fmaf(P.p.fb, kk, u);
+              if constexpr (MODE != kStageLast) gt[off] = fmaf(P.p.fa, kk, u);
+            }
           }
-        }
+      }
     }
-    bar_compute();
-    if (tid == 0) mbar_arrive(&empty[s]);
   }
 }
 
