@@ -44,25 +44,28 @@ bool encode_trace(EncodeTiledFn enc, CUtensorMap* m, const float* base, long lon
 
 }  // namespace
 
-cudaError_t encode_ecl6_maps(const float* base, long long n, Ecl6Maps* m) {
+// T (and U) tiles of one cell: [n/32][32] floats, box [128][32], 128-byte swizzle
+static bool encode_tile(EncodeTiledFn enc, CUtensorMap* m, const float* base, long long n) {
+  cuuint64_t dims[2] = {32, cuuint64_t(n) / 32};
+  cuuint64_t strides[1] = {128};
+  cuuint32_t box[2] = {32, 128};
+  cuuint32_t es[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+cudaError_t encode_ecl6_maps(const float* tin, const float* uin, long long n, Ecl6Maps* m) {
   EncodeTiledFn enc = encode_fn();
   if (!enc) return cudaErrorNotSupported;
   std::memset(m, 0, sizeof(*m));
-  {
-    cuuint64_t dims[2] = {32, cuuint64_t(n) / 32};
-    cuuint64_t strides[1] = {128};
-    cuuint32_t box[2] = {32, 128};
-    cuuint32_t es[2] = {1, 1};
-    if (enc(&m->tcell, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-      return cudaErrorInvalidValue;
-  }
-  // faces of x1 (inner 4), x2 (16), v0 (64), v1 (256); one cell = 1024 / inner outer rows
-  const cuuint64_t inner[4] = {4, 16, 64, 256};
-  for (int d = 0; d < 4; ++d)
-    if (!encode_trace(enc, &m->tr[d], base, n, inner[d], cuuint32_t(1024 / inner[d])))
-      return cudaErrorInvalidValue;
+  if (!encode_tile(enc, &m->tcell, tin, n) || !encode_tile(enc, &m->ucell, uin ? uin : tin, n))
+    return cudaErrorInvalidValue;
+  // faces: view [n/(4S)][4][S] with S the node stride of the direction; one face of
+  // one cell is the box [1024/S][1][S]
+  if (!encode_trace(enc, &m->tx2, tin, n, 16, 64) || !encode_trace(enc, &m->tv0, tin, n, 64, 16) ||
+      !encode_trace(enc, &m->tv1, tin, n, 256, 4))
+    return cudaErrorInvalidValue;
   return cudaSuccess;
 }
 
@@ -81,7 +84,7 @@ cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int mode, cudaStrea
   E.n_rows = int(P.n_cells / P.cells[0]);
   E.err = err;
   Ecl6Maps maps;
-  cudaError_t e = encode_ecl6_maps(P.tin, P.n_cells * 4096LL, &maps);
+  cudaError_t e = encode_ecl6_maps(P.tin, P.uin, P.n_cells * 4096LL, &maps);
   if (e != cudaSuccess) return e;
   static bool attr_done[4] = {false, false, false, false};
   int dev = 0, sms = 0;

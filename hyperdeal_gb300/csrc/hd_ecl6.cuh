@@ -7,15 +7,18 @@
 //     needs is the previous cell's face, which the thread owning that plane
 //     still holds in registers ("carry"); only a row's first cell reads it
 //     from global memory.
-//   * The producer warp streams, per cell, through a 2-stage ring guarded by
-//     mbarriers: the cell's 4096 values as one 2D TMA tile with the 128-byte
-//     swizzle (conflict-free plane reads), the upwind face traces of x1, x2,
-//     v0, v1 as one 3D TMA box each, and the v2 trace (contiguous) as one 1D
-//     bulk copy.
+//   * The producer warp streams, per cell, through a 2-slot ring guarded by
+//     mbarriers: the cell's 4096 stage-input values and its 4096 RK-solution
+//     values as two 2D TMA tiles with the 128-byte swizzle (conflict-free
+//     plane reads), and the upwind face traces of x2, v0, v1 (3D TMA boxes)
+//     and v2 (contiguous, 1D bulk copy).  The x1 trace (4 floats at a 64-byte
+//     stride, a poor TMA shape) is loaded one cell ahead by the compute
+//     threads with one 128-bit load each.
 //   * The compute warps apply the line operators two directions per phase
 //     (x0x1, x2v0, v1v2) with an XOR-swizzled accumulator tile in shared
-//     memory; the last phase writes K or the fused LSRK update with coalesced
-//     stores.  U (own nodes) is prefetched into registers at the cell start.
+//     memory; the last phase transposes the result through the warp's own
+//     slice of that tile and writes K or the fused LSRK update with 128-bit
+//     stores.
 //   * Every mbarrier wait is bounded: on time-out the kernel records an
 //     error code, drains its own in-flight copies (bounded) and returns.
 //
@@ -31,20 +34,28 @@
 
 namespace hd {
 
+
 struct Ecl6Maps {
-  CUtensorMap tcell;  // vector as [n/32][32] floats, box [128][32], 128B swizzle
-  CUtensorMap tr[4];  // traces of x1, x2, v0, v1: [n/S][4][S], box [256/S... ][1][S]
+  CUtensorMap tcell;  // stage input T as [n/32][32] floats, box [128][32], 128B swizzle
+  CUtensorMap ucell;  // RK solution U, same shape (stage kernels that read U)
+  CUtensorMap tx2;    // T as [n/64][4][16], box [64][1][16]: one x2 face
+  CUtensorMap tv0;    // T as [n/256][4][64], box [16][1][64]: one v0 face
+  CUtensorMap tv1;    // T as [n/1024][4][256], box [4][1][256]: one v1 face
 };
 
 constexpr int E6_CTHREADS = 256;  // compute threads
 constexpr int E6_THREADS = 288;   // + one producer warp
 constexpr int E6_STAGES = 2;
-constexpr int E6_STAGE_BYTES = 16384 + 5 * 4096;  // cell tile + 5 traces
-constexpr int E6_OUT_BYTES = 2 * 16384;  // double-buffered accumulator tile
-constexpr int E6_SMEM = 1024 /*alignment slack*/ + E6_STAGES * E6_STAGE_BYTES + E6_OUT_BYTES + 64;
+// slot (floats): T tile [0,4096), U tile [4096,8192), faces x2 [8192,9216), v0 [9216,10240),
+// v1 [10240,11264), v2 [11264,12288)
+constexpr int E6_STAGE_FLOATS = 12288;
+constexpr int E6_STAGE_BYTES = 4 * E6_STAGE_FLOATS;
+constexpr int E6_OUT_BYTES = 16384;  // accumulator tile
+constexpr int E6_SMEM = E6_STAGES * E6_STAGE_BYTES + E6_OUT_BYTES + 64;
 constexpr unsigned E6_WAIT_LIMIT = 1u << 22;  // try_wait rounds before giving up (~seconds)
 
-enum : int { E6_ERR_TIMEOUT_FULL = 1, E6_ERR_TIMEOUT_EMPTY = 2 };
+enum : int { E6_ERR_TIMEOUT_FULL = 1, E6_ERR_TIMEOUT_EMPTY = 2, E6_ERR_SMEM_ALIGN = 3 };
+
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -124,32 +135,48 @@ struct Ecl6Params {
   int* err;            // device error flag
 };
 
-// cell id of the k-th cell of row r in the row's upwind traversal order
-__device__ __forceinline__ long long e6_cell(const Ecl6Params& P, int r, int k) {
-  const int c = P.p.op[0].step < 0 ? k : (P.row_len - 1 - k);
-  return (long long)r * P.row_len + c;
+// first cell id of row r and the upwind-neighbour offsets (in cells) of the
+// row's cells in directions 1..5 (inside a row only x0 varies)
+struct E6Row {
+  long long first;
+  int nb[6];
+};
+
+__device__ __forceinline__ E6Row e6_row(const Ecl6Params& P, int r) {
+  E6Row R;
+  R.first = (long long)r * P.row_len;
+  R.nb[0] = 0;
+  int rem = r;
+#pragma unroll
+  for (int d = 1; d < 6; ++d) {
+    const int nc = P.p.cells[d];
+    const int c = rem % nc;
+    rem /= nc;
+    const int step = P.p.op[d].step;
+    const int cs = int(P.p.cstride[d]);
+    const int cn = c + step;
+    R.nb[d] = (cn < 0) ? (nc - 1) * cs : (cn >= nc ? -(nc - 1) * cs : step * cs);
+  }
+  return R;
 }
 
-// upwind neighbour of `gid` in direction d on the fully periodic mesh
-__device__ __forceinline__ long long e6_nb(const Ecl6Params& P, long long gid, int d) {
-  const long long cs = P.p.cstride[d];
-  const int nc = P.p.cells[d];
-  const int c = int((gid / cs) % nc);
-  const int step = P.p.op[d].step;
-  const int cn = c + step;
-  if (cn < 0) return gid + (long long)(nc - 1) * cs;
-  if (cn >= nc) return gid - (long long)(nc - 1) * cs;
-  return gid + step * cs;
+// cell id of the k-th cell of a row in the upwind traversal order of x0
+__device__ __forceinline__ long long e6_cell(const Ecl6Params& P, long long first, int k) {
+  return first + (P.p.op[0].step < 0 ? k : (P.row_len - 1 - k));
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_constant__ Ecl6Params P,
-                                                             const __grid_constant__ Ecl6Maps maps) {
-  extern __shared__ unsigned char smem_raw[];
-  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  float* s_stage = reinterpret_cast<float*>(base);
-  float* s_out = reinterpret_cast<float*>(base + E6_STAGES * E6_STAGE_BYTES);  // 2 accumulator tiles
-  uint64_t* bars = reinterpret_cast<uint64_t*>(base + E6_STAGES * E6_STAGE_BYTES + E6_OUT_BYTES);
+__global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params P,
+                                             const __grid_constant__ Ecl6Maps maps) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  constexpr bool READ_U = (MODE == kStageMid || MODE == kStageLast);
+  if (smem_u32(smem_raw) & 1023u) {  // the swizzled tiles need 1024-byte alignment
+    if (threadIdx.x == 0) atomicExch(P.err, E6_ERR_SMEM_ALIGN);
+    return;
+  }
+  float* s_stage = reinterpret_cast<float*>(smem_raw);
+  float* so = reinterpret_cast<float*>(smem_raw + E6_STAGES * E6_STAGE_BYTES);  // accumulator tile
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + E6_STAGES * E6_STAGE_BYTES + E6_OUT_BYTES);
   uint64_t* full = bars;               // [E6_STAGES]: TMA bytes landed
   uint64_t* empty = bars + E6_STAGES;  // [E6_STAGES]: all 8 compute warps done with the slot
   volatile int* s_abort = reinterpret_cast<volatile int*>(bars + 2 * E6_STAGES);
@@ -173,9 +200,11 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
     if (tid == E6_CTHREADS) {
       int issued = 0;
       bool ok = true;
-      uint32_t bytes = 16384;
+      uint32_t bytes = 16384u + (READ_U ? 16384u : 0u);
 #pragma unroll
-      for (int d = 1; d < 6; ++d) bytes += P.p.op[d].active ? 4096u : 0u;
+      for (int d = 2; d < 6; ++d) bytes += P.p.op[d].active ? 4096u : 0u;
+      int r = (int)blockIdx.x, k = 0;
+      E6Row R = e6_row(P, r < P.n_rows ? r : 0);
       for (int it = 0; it < n_cells_cta; ++it) {
         const int s = it % E6_STAGES;
         if (it >= E6_STAGES && !mbar_wait(&empty[s], ((it / E6_STAGES) - 1) & 1)) {
@@ -185,21 +214,25 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
           break;
         }
         if (*s_abort) { ok = false; break; }
-        const int r = (int)blockIdx.x + (it / P.row_len) * (int)gridDim.x;
-        const long long gid = e6_cell(P, r, it % P.row_len);
-        float* st = s_stage + s * (E6_STAGE_BYTES / 4);
+        const long long gid = e6_cell(P, R.first, k);
+        float* st = s_stage + s * E6_STAGE_FLOATS;
         mbar_arrive_expect_tx(&full[s], bytes);
         tma_load_2d(st, &maps.tcell, 0, int(gid * 128), &full[s]);
-        // upwind traces (face node nb_node of the upwind neighbour)
-#pragma unroll
-        for (int d = 1; d < 5; ++d)
-          if (P.p.op[d].active)
-            tma_load_3d(st + 4096 + (d - 1) * 1024, &maps.tr[d - 1], 0, P.p.op[d].nb_node,
-                        int(e6_nb(P, gid, d) * (256 >> (2 * (d - 1)))), &full[s]);
+        if (READ_U) tma_load_2d(st + 4096, &maps.ucell, 0, int(gid * 128), &full[s]);
+        if (P.p.op[2].active)
+          tma_load_3d(st + 8192, &maps.tx2, 0, P.p.op[2].nb_node, int((gid + R.nb[2]) * 64), &full[s]);
+        if (P.p.op[3].active)
+          tma_load_3d(st + 9216, &maps.tv0, 0, P.p.op[3].nb_node, int((gid + R.nb[3]) * 16), &full[s]);
+        if (P.p.op[4].active)
+          tma_load_3d(st + 10240, &maps.tv1, 0, P.p.op[4].nb_node, int((gid + R.nb[4]) * 4), &full[s]);
         if (P.p.op[5].active)
-          bulk_load(st + 4096 + 4 * 1024, P.p.tin + e6_nb(P, gid, 5) * 4096 + P.p.op[5].nb_node * 1024, 4096u,
-                    &full[s]);
+          bulk_load(st + 11264, P.p.tin + (gid + R.nb[5]) * 4096 + P.p.op[5].nb_node * 1024, 4096u, &full[s]);
         ++issued;
+        if (++k == P.row_len) {
+          k = 0;
+          r += (int)gridDim.x;
+          if (r < P.n_rows) R = e6_row(P, r);
+        }
       }
       // on an abort, wait (bounded) for the copies still in flight before leaving
       if (!ok) {
@@ -212,7 +245,6 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
 
   // -------------------------------------------------------------------- consumers
   const LineOp<float>* L = P.p.op;
-  float carry[4] = {0.f, 0.f, 0.f, 0.f};
   constexpr long long NC = 4096;
   const int lane = tid & 31, warp = tid >> 5;
 
@@ -233,37 +265,44 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
   // phase 2: nodes tid + 256a + 1024b; row & 7 = warp
   const int tb2 = (tid & ~28) | ((((tid >> 2) & 7) ^ warp) << 2);
   const int ob2[2] = {tb2, (tid & ~28) | ((((tid >> 2) & 7) ^ warp ^ 4) << 2)};
+  // epilogue: each lane owns 4 float4 chunks of its warp's 512 phase-2 nodes,
+  // nodes vnode + 1024 j + (0..3) with vnode = 4 (lane & 7) + 32 warp + 256 (lane >> 3)
+  const int vnode = 4 * (lane & 7) + 32 * warp + 256 * (lane >> 3);
+  const int vt = 32 * warp + 256 * (lane >> 3) + (((lane & 7) ^ warp) << 2);  // T / U tiles
+  const int vo = 32 * warp + 256 * (lane >> 3) + (((lane & 7) ^ warp ^ (4 * ((lane >> 3) & 1))) << 2);
 
+  float carry[4] = {0.f, 0.f, 0.f, 0.f};  // x0 face of the previous cell of the row
+  float4 px1 = make_float4(0.f, 0.f, 0.f, 0.f);  // x1 face values of this thread's plane
+  auto fetch_x1 = [&](long long g, int nb1) {
+    if (L[1].active)
+      px1 = __ldg(reinterpret_cast<const float4*>(P.p.tin + (g + nb1) * NC + 16 * tid + 4 * L[1].nb_node));
+  };
+
+  int r = (int)blockIdx.x, k = 0;
+  E6Row R = e6_row(P, r < P.n_rows ? r : 0);
+  if (n_cells_cta > 0) fetch_x1(e6_cell(P, R.first, 0), R.nb[1]);
   for (int it = 0; it < n_cells_cta; ++it) {
     const int s = it % E6_STAGES;
-    const int k = it % P.row_len;
-    const int r = (int)blockIdx.x + (it / P.row_len) * (int)gridDim.x;
-    const long long gid = e6_cell(P, r, k);
-    const float* st = s_stage + s * (E6_STAGE_BYTES / 4);
-    float* so = s_out + (it & 1) * 4096;
+    const long long gid = e6_cell(P, R.first, k);
+    const float* st = s_stage + s * E6_STAGE_FLOATS;
+    const bool has_next = it + 1 < n_cells_cta;
+    const bool new_row = k + 1 == P.row_len;
 
-    // row start: x0 face of the upwind neighbour of the row's first cell
+    // row start: x0 face of the upwind neighbour of the row's first cell (periodic wrap)
     if (k == 0 && L[0].active) {
-      const float* src = P.p.tin + e6_nb(P, gid, 0) * NC + 16 * tid + L[0].nb_node;
+      const long long g0 = R.first + (L[0].step < 0 ? P.row_len - 1 : 0);
+      const float* src = P.p.tin + g0 * NC + 16 * tid + L[0].nb_node;
 #pragma unroll
       for (int b = 0; b < 4; ++b) carry[b] = __ldg(src + 4 * b);
     }
-    // U at this thread's phase-2 nodes
-    float uU[16];
-    if constexpr (MODE == kStageMid || MODE == kStageLast) {
-      const float* up = P.p.uin + gid * NC + tid;
-#pragma unroll
-      for (int b = 0; b < 4; ++b)
-#pragma unroll
-        for (int a = 0; a < 4; ++a) uU[a + 4 * b] = __ldg(up + 256 * a + 1024 * b);
-    }
 
-    // every compute thread waits for the slot (bounded); a time-out turns the
-    // rest of the CTA's work into no-ops (no stores) without leaving any barrier
-    if (!*s_abort && !mbar_wait(&full[s], (it / E6_STAGES) & 1)) {
+    // one lane per warp waits for the slot (bounded); a time-out turns the rest
+    // of the CTA's work into no-ops (no stores) without leaving any barrier
+    if (lane == 0 && !*s_abort && !mbar_wait(&full[s], (it / E6_STAGES) & 1)) {
       *s_abort = 1;
       atomicExch(P.err, E6_ERR_TIMEOUT_FULL);
     }
+    __syncwarp();
 
     // ---------------- phase 0: directions x0 (a) and x1 (b); plane = nodes 16*tid + a + 4b
     {
@@ -296,8 +335,7 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
         for (int b = 0; b < 4; ++b) carry[b] = L[0].nb_node ? uu[3][b] : uu[0][b];
       }
       if (L[1].active) {
-        const float4 t1 = *reinterpret_cast<const float4*>(st + 4096 + 4 * tid);
-        const float upv[4] = {t1.x, t1.y, t1.z, t1.w};
+        const float upv[4] = {px1.x, px1.y, px1.z, px1.w};
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
 #pragma unroll
@@ -316,6 +354,15 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
         *reinterpret_cast<float4*>(so + row0 * 32 + ((o0_chunk ^ b) << 2)) =
             make_float4(acc[0][b], acc[1][b], acc[2][b], acc[3][b]);
     }
+    // x1 face of the next cell of this CTA
+    if (has_next) {
+      if (new_row) {
+        const E6Row Rn = e6_row(P, r + (int)gridDim.x);
+        fetch_x1(e6_cell(P, Rn.first, 0), Rn.nb[1]);
+      } else {
+        fetch_x1(e6_cell(P, R.first, k + 1), R.nb[1]);
+      }
+    }
     bar_compute();
 
     // ---------------- phase 1: directions x2 (a, stride 16) and v0 (b, stride 64)
@@ -325,13 +372,13 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
       for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-          const int R = (a >> 1) + 2 * b;
-          const int e = (a & 1) ^ (R >> 2);
-          uu[a][b] = st[tb1[R & 3] + 32 * R + 16 * e];
-          acc[a][b] = so[ob1[R & 3][e] + 32 * R];
+          const int Rr = (a >> 1) + 2 * b;
+          const int e = (a & 1) ^ (Rr >> 2);
+          uu[a][b] = st[tb1[Rr & 3] + 32 * Rr + 16 * e];
+          acc[a][b] = so[ob1[Rr & 3][e] + 32 * Rr];
         }
       if (L[2].active) {
-        const float* tr = st + 5120 + 64 * hi + lo;
+        const float* tr = st + 8192 + 64 * hi + lo;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
 #pragma unroll
@@ -347,7 +394,7 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
         }
       }
       if (L[3].active) {
-        const float* tr = st + 6144 + 64 * hi + lo;
+        const float* tr = st + 9216 + 64 * hi + lo;
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
 #pragma unroll
@@ -366,9 +413,9 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
       for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-          const int R = (a >> 1) + 2 * b;
-          const int e = (a & 1) ^ (R >> 2);
-          so[ob1[R & 3][e] + 32 * R] = acc[a][b];
+          const int Rr = (a >> 1) + 2 * b;
+          const int e = (a & 1) ^ (Rr >> 2);
+          so[ob1[Rr & 3][e] + 32 * Rr] = acc[a][b];
         }
     }
     bar_compute();
@@ -384,7 +431,7 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
           acc[a][b] = so[ob2[a & 1] + 256 * a + 1024 * b];
         }
       if (L[4].active) {
-        const float* tr = st + 7168 + tid;
+        const float* tr = st + 10240 + tid;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
 #pragma unroll
@@ -400,7 +447,7 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
         }
       }
       if (L[5].active) {
-        const float* tr = st + 8192 + tid;
+        const float* tr = st + 11264 + tid;
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
 #pragma unroll
@@ -415,27 +462,49 @@ __global__ void __launch_bounds__(E6_THREADS, 2) ecl6_kernel(const __grid_consta
           acc[a][3] = fmaf(L[5].cl, up, acc[a][3]);
         }
       }
-      // this warp is done with the stage slot
+      // U at the epilogue nodes (the T tile for the first stage), read before the slot is released
+      float4 uv[4];
+      if constexpr (MODE != kApply) {
+        const float* ut = READ_U ? st + 4096 : st;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) uv[j] = *reinterpret_cast<const float4*>(ut + vt + 1024 * j);
+      }
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[s]);
+      // transpose K through this warp's private slice of the accumulator tile
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) so[ob2[a & 1] + 256 * a + 1024 * b] = acc[a][b];
+      __syncwarp();
       if (!*s_abort) {
-        float* go = P.p.uout + gid * NC + tid;
-        float* gt = P.p.tout + gid * NC + tid;
+        float4* go = reinterpret_cast<float4*>(P.p.uout + gid * NC + vnode);
 #pragma unroll
-        for (int b = 0; b < 4; ++b)
-#pragma unroll
-          for (int a = 0; a < 4; ++a) {
-            const int off = 256 * a + 1024 * b;
-            const float kk = acc[a][b];
-            if constexpr (MODE == kApply) {
-              go[off] = kk;
-            } else {
-              const float u = (MODE == kStageFirst) ? uu[a][b] : uU[a + 4 * b];
-              go[off] = fmaf(P.p.fb, kk, u);
-              if constexpr (MODE != kStageLast) gt[off] = fmaf(P.p.fa, kk, u);
+        for (int j = 0; j < 4; ++j) {
+          const float4 kv = *reinterpret_cast<const float4*>(so + vo + 1024 * j);
+          if constexpr (MODE == kApply) {
+            go[256 * j] = kv;
+          } else {
+            const float4 u = uv[j];
+            go[256 * j] = make_float4(fmaf(P.p.fb, kv.x, u.x), fmaf(P.p.fb, kv.y, u.y), fmaf(P.p.fb, kv.z, u.z),
+                                      fmaf(P.p.fb, kv.w, u.w));
+            if constexpr (MODE != kStageLast) {
+              float4* gt = reinterpret_cast<float4*>(P.p.tout + gid * NC + vnode);
+              gt[256 * j] = make_float4(fmaf(P.p.fa, kv.x, u.x), fmaf(P.p.fa, kv.y, u.y), fmaf(P.p.fa, kv.z, u.z),
+                                        fmaf(P.p.fa, kv.w, u.w));
             }
           }
+        }
       }
+    }
+    // the accumulator tile is rewritten by the next cell's phase 0
+    bar_compute();
+    if (new_row) {
+      k = 0;
+      r += (int)gridDim.x;
+      if (r < P.n_rows) R = e6_row(P, r);
+    } else {
+      ++k;
     }
   }
 }
