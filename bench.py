@@ -259,7 +259,9 @@ def main():
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic,
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
-                "bytes_per_launch": bytes_per_launch, "kernel": "hd::ecl_kernel<6,4,float,stage>"}
+                "bytes_per_launch": bytes_per_launch,
+                "kernel": ("hd::ecl6_kernel<stage> (persistent, TMA-pipelined)" if op.kernel == "pipelined"
+                           else "hd::ecl_kernel<6,4,float,stage> (generic)")}
 
     # FP64 form of the same steps, and the L2 difference of the two solutions
     f64 = {}
