@@ -20,7 +20,7 @@ EXPORTED_SYMBOLS = (
     "hd_last_error", "hd_version", "hd_adv_create", "hd_adv_destroy", "hd_adv_n_dofs", "hd_adv_apply",
     "hd_adv_critical_time_step", "hd_interpolate", "hd_norm_and_error", "hd_lsrk_create", "hd_lsrk_destroy",
     "hd_lsrk_n_stages", "hd_lsrk_step", "hd_lsrk_step_unfused", "hd_lsrk_stage_update", "hd_lsrk_coefficients",
-    "hd_adv_set_kernel", "hd_adv_kernel", "hd_adv_device_status",
+    "hd_adv_set_kernel", "hd_adv_kernel", "hd_adv_device_status", "hd_norm_and_error_noalloc",
 )
 HD_KERNEL_AUTO, HD_KERNEL_GENERIC, HD_KERNEL_PIPELINED = 0, 1, 2
 
@@ -82,6 +82,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.hd_adv_critical_time_step.restype = ctypes.c_double
     L.hd_interpolate.argtypes = [vp, ctypes.POINTER(hd_function), ctypes.c_double, vp, vp]
     L.hd_norm_and_error.argtypes = [vp, ctypes.POINTER(hd_function), ctypes.c_double, vp, dp, vp]
+    L.hd_norm_and_error_noalloc.argtypes = [ctypes.POINTER(hd_adv_desc), ctypes.POINTER(hd_function),
+                                            ctypes.c_double, vp, dp, vp]
     L.hd_lsrk_create.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
     L.hd_lsrk_destroy.argtypes = [vp]
     L.hd_lsrk_n_stages.argtypes = [vp]

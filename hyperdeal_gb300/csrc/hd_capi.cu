@@ -185,6 +185,11 @@ hd::DevFunction to_dev(const hd_function& f) {
 
 }  // namespace
 
+namespace hd {
+// lets the other translation units report through hd_last_error()
+void set_last_error(const char* msg) { g_last_error = msg; }
+}  // namespace hd
+
 struct hd_adv {
   hd_adv_desc desc;
   int D, N, NC, dtype;

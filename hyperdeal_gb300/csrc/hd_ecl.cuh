@@ -372,6 +372,9 @@ EclLaunchers make_launchers() {
                       S64::THREADS, S32::THREADS, S64::CPB, S32::CPB, S64::SUPPORTED, S32::SUPPORTED};
 }
 
+// message of the last failure for hd_last_error() (hd_capi.cu)
+void set_last_error(const char* msg);
+
 // pipelined 6D degree-3 FP32 kernel (hd_ecl6.cu): eligible for fully periodic
 // 3x+3v meshes; err receives a device error code on a bounded-wait time-out
 bool ecl6_eligible(const EclParams<float>& P);

@@ -142,6 +142,20 @@ int hd_interpolate(hd_adv *op, const hd_function *f, double time, void *dst, voi
 int hd_norm_and_error(hd_adv *op, const hd_function *f, double time, const void *src,
                       double *result, void *stream);
 
+/* The same result as hd_norm_and_error for callers that must not allocate
+ * device memory (a host application that owns all device memory, a time loop
+ * that forbids allocation after start-up).  No counterpart in the reference:
+ * it takes the descriptor instead of a handle (hd_adv_create allocates) and
+ * calls no cudaMalloc / cudaFree; its scratch is a fixed 256 KiB array in
+ * device global memory inside the library, held by every GPU that loads the
+ * library until exit.  Limit: at most 134,217,728 DoFs (larger meshes get
+ * HD_ERR_INVALID; use hd_norm_and_error).  All calls share the scratch, so
+ * calls whose kernels overlap on the GPU race: serialise them.  The first call
+ * on a device looks up the scratch address for that device (make it before
+ * any stream capture).  Synchronises `stream`; result is host memory. */
+int hd_norm_and_error_noalloc(const hd_adv_desc *desc, const hd_function *f, double time,
+                              const void *src, double *result, void *stream);
+
 /* ---- low-storage Runge-Kutta ------------------------------------------------ */
 
 /* LowStorageRungeKuttaIntegrator(Ki, Ti, type, only_Ti_is_ghosted=true)
