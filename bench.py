@@ -118,11 +118,11 @@ def measured_peak_hbm():
 
 
 def profiled_traffic():
-    """DRAM bytes per stage launch from the committed ncu summary of the stage kernel (or None)."""
+    """DRAM bytes per (average) stage launch from the committed ncu summary of the stage kernel (or None)."""
     p = os.path.join(ROOT, "profiles", "ecl_stage_6d_k3_f32.json")
     if os.path.exists(p):
         d = json.load(open(p))
-        return d.get("dram_bytes_per_launch")
+        return d.get("dram_bytes_per_avg_launch")
     return None
 
 
