@@ -75,6 +75,25 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     return LIB_PATH
 
 
+def build_cpp_app(name: str = "advection_hyperrectangle") -> str:
+    """Compile a C++ host program of cpp/ against include/hyperdeal_gb300.hpp and the library (g++)."""
+    lib = build()
+    src = os.path.join(PKG, "cpp", name + ".cc")
+    exe = os.path.join(OUT_DIR, name)
+    if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(src), os.path.getmtime(lib),
+                                                             os.path.getmtime(os.path.join(ROOT, "include",
+                                                                                           "hyperdeal_gb300.hpp"))):
+        return exe
+    cuda_home = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+    cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(cuda_home, "include"),
+           src, "-o", exe, "-L", OUT_DIR, "-lhyperdeal_gb300", "-Wl,-rpath," + OUT_DIR,
+           "-L", os.path.join(cuda_home, "lib64"), "-lcudart", "-Wl,-rpath," + os.path.join(cuda_home, "lib64")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("g++ failed:\n%s\n%s" % (r.stdout, r.stderr))
+    return exe
+
+
 if __name__ == "__main__":
     import sys
     print(build(force="--force" in sys.argv, verbose=True))

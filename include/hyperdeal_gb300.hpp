@@ -1,0 +1,268 @@
+// hyperdeal_gb300.hpp -- header-only C++ interface over the C ABI with the
+// class names and call signatures of hyper.deal's advection path:
+//
+//   AdvectionOperation::apply(dst, src, time)
+//       include/hyper.deal/operators/advection/advection_operation.h:134-209
+//   LowStorageRungeKuttaIntegrator(vec_Ki, vec_Ti, type, only_Ti_is_ghosted),
+//   perform_time_step(solution, current_time, time_step, op), n_stages()
+//       include/hyper.deal/base/time_integrators.h:47-115
+//   TimeLoop::loop(solution, time_integrator, runnable, diagnostics)
+//       source/base/time_loop.cc:33-67
+//   VectorTools::interpolate / norm_and_error
+//       include/hyper.deal/numerics/vector_tools.h:81-223
+//
+// Vectors are DeviceVector<Number> (device memory, the reference's DoF
+// numbering).  Errors throw std::runtime_error with hd_last_error()'s message,
+// as the reference throws dealii::ExceptionBase from AssertThrow.
+#ifndef HYPERDEAL_GB300_HPP
+#define HYPERDEAL_GB300_HPP
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "hyperdeal_gb300.h"
+
+namespace hyperdeal_gb300 {
+
+inline void check(int rc) {
+  if (rc != HD_OK) {
+    char buf[512];
+    hd_last_error(buf, sizeof(buf));
+    throw std::runtime_error(std::string("hyperdeal_gb300: ") + buf);
+  }
+}
+
+inline void check_cuda(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename Number>
+struct dtype_of;
+template <>
+struct dtype_of<double> {
+  static constexpr int value = HD_F64;
+};
+template <>
+struct dtype_of<float> {
+  static constexpr int value = HD_F32;
+};
+
+// Device-resident DoF vector (owned; move-only; swap exchanges storages).
+template <typename Number>
+class DeviceVector {
+ public:
+  DeviceVector() = default;
+  explicit DeviceVector(long long n) { reinit(n); }
+  ~DeviceVector() { release(); }
+  DeviceVector(const DeviceVector&) = delete;
+  DeviceVector& operator=(const DeviceVector&) = delete;
+  DeviceVector(DeviceVector&& o) noexcept { swap(o); }
+  DeviceVector& operator=(DeviceVector&& o) noexcept {
+    swap(o);
+    return *this;
+  }
+
+  void reinit(long long n) {
+    release();
+    n_ = n;
+    if (n > 0) {
+      check_cuda(cudaMalloc(&data_, sizeof(Number) * size_t(n)), "cudaMalloc");
+      check_cuda(cudaMemset(data_, 0, sizeof(Number) * size_t(n)), "cudaMemset");
+    }
+  }
+  Number* data() { return data_; }
+  const Number* data() const { return data_; }
+  long long size() const { return n_; }
+  void swap(DeviceVector& o) noexcept {
+    std::swap(data_, o.data_);
+    std::swap(n_, o.n_);
+  }
+  void copy_from_host(const Number* h) {
+    check_cuda(cudaMemcpy(data_, h, sizeof(Number) * size_t(n_), cudaMemcpyHostToDevice), "copy to device");
+  }
+  void copy_to_host(Number* h) const {
+    check_cuda(cudaMemcpy(h, data_, sizeof(Number) * size_t(n_), cudaMemcpyDeviceToHost), "copy to host");
+  }
+  std::vector<Number> to_host() const {
+    std::vector<Number> v(size_t(n_));
+    copy_to_host(v.data());
+    return v;
+  }
+
+ private:
+  void release() {
+    if (data_) cudaFree(data_);
+    data_ = nullptr;
+    n_ = 0;
+  }
+  Number* data_ = nullptr;
+  long long n_ = 0;
+};
+
+// Analytic function amp * prod_d trig_d(omega_d (x_d - speed_d t) + phase_d).
+inline hd_function make_function(double amp, const std::vector<double>& omega, const std::vector<double>& speed,
+                                 const std::vector<double>& phase, const std::vector<int>& cosine) {
+  hd_function f{};
+  f.kind = 2;
+  f.amp = amp;
+  for (size_t i = 0; i < omega.size() && i < HD_MAX_DIM; ++i) f.omega[i] = omega[i];
+  for (size_t i = 0; i < speed.size() && i < HD_MAX_DIM; ++i) f.speed[i] = speed[i];
+  for (size_t i = 0; i < phase.size() && i < HD_MAX_DIM; ++i) f.phase[i] = phase[i];
+  for (size_t i = 0; i < cosine.size() && i < HD_MAX_DIM; ++i) f.cosine[i] = cosine[i];
+  return f;
+}
+
+template <typename Number>
+class AdvectionOperation {
+ public:
+  // AdvectionOperation(MatrixFree, table) + reinit(bc, velocity, param): the
+  // descriptor carries mesh, degree, velocity, skew and boundary data.
+  explicit AdvectionOperation(hd_adv_desc desc, cudaStream_t stream = nullptr) : stream_(stream) {
+    desc.dtype = dtype_of<Number>::value;
+    desc.n_points = desc.degree + 1;
+    check(hd_adv_create(&desc, &h_));
+  }
+  ~AdvectionOperation() { hd_adv_destroy(h_); }
+  AdvectionOperation(const AdvectionOperation&) = delete;
+  AdvectionOperation& operator=(const AdvectionOperation&) = delete;
+
+  // dst = M^{-1} A(src) at `time`; dst is overwritten.
+  void apply(DeviceVector<Number>& dst, const DeviceVector<Number>& src, const Number time) const {
+    check(hd_adv_apply(h_, dst.data(), src.data(), double(time), stream_));
+  }
+  // the operator signature of the reference's LSRK lambdas: op(src, dst, time)
+  void operator()(const DeviceVector<Number>& src, DeviceVector<Number>& dst, const Number time) const {
+    apply(dst, src, time);
+  }
+
+  long long n_dofs() const { return hd_adv_n_dofs(h_); }
+  double critical_time_step() const { return hd_adv_critical_time_step(h_); }
+  hd_adv* handle() const { return h_; }
+  cudaStream_t stream() const { return stream_; }
+  DeviceVector<Number> create_vector() const { return DeviceVector<Number>(n_dofs()); }
+
+ private:
+  hd_adv* h_ = nullptr;
+  cudaStream_t stream_;
+};
+
+template <typename Number>
+class LowStorageRungeKuttaIntegrator {
+ public:
+  using Operator = std::function<void(const DeviceVector<Number>&, DeviceVector<Number>&, Number)>;
+
+  LowStorageRungeKuttaIntegrator(DeviceVector<Number>& vec_Ki, DeviceVector<Number>& vec_Ti, const std::string& type,
+                                 const bool only_Ti_is_ghosted = true)
+      : Ki_(vec_Ki), Ti_(vec_Ti), only_Ti_is_ghosted_(only_Ti_is_ghosted) {
+    check(hd_lsrk_create(type.c_str(), &rk_));
+    ns_ = hd_lsrk_n_stages(rk_);
+    ai_.resize(ns_);
+    bi_.resize(ns_);
+    ci_.resize(ns_);
+    check(hd_lsrk_coefficients(rk_, ai_.data(), bi_.data(), ci_.data()));
+  }
+  ~LowStorageRungeKuttaIntegrator() { hd_lsrk_destroy(rk_); }
+  LowStorageRungeKuttaIntegrator(const LowStorageRungeKuttaIntegrator&) = delete;
+  LowStorageRungeKuttaIntegrator& operator=(const LowStorageRungeKuttaIntegrator&) = delete;
+
+  unsigned int n_stages() const { return unsigned(ns_); }
+
+  // Fused: every stage is one kernel (operator + stage update).  The three
+  // vectors rotate roles; storages are swapped back so that `solution` holds
+  // the new state and vec_Ki / vec_Ti are scratch, as in the reference.
+  void perform_time_step(DeviceVector<Number>& solution, const Number current_time, const Number time_step,
+                         const AdvectionOperation<Number>& op) {
+    void* s = solution.data();
+    void* k = Ki_.data();
+    void* t = Ti_.data();
+    void* ki_storage = k;
+    check(hd_lsrk_step(op.handle(), rk_, &s, &k, &t, double(current_time), double(time_step), op.stream()));
+    if (s == ki_storage) solution.swap(Ki_);
+  }
+
+  // Any operator op(src, dst, t): the reference's stage sequence
+  // (time_integrators.templates.h:91-184) with the CUDA vector update.
+  void perform_time_step(DeviceVector<Number>& solution, const Number current_time, const Number time_step,
+                         const Operator& op, cudaStream_t stream = nullptr) {
+    const long long n = solution.size();
+    const DeviceVector<Number>* cur = &solution;
+    if (only_Ti_is_ghosted_) {
+      check_cuda(cudaMemcpyAsync(Ti_.data(), solution.data(), sizeof(Number) * size_t(n), cudaMemcpyDeviceToDevice,
+                                 stream),
+                 "copy solution -> Ti");
+      cur = &Ti_;
+    }
+    for (int s = 0; s < ns_; ++s) {
+      op(*cur, Ki_, Number(current_time + ci_[s] * time_step));
+      const double ai = s == ns_ - 1 ? 0.0 : ai_[s] * time_step;
+      check(hd_lsrk_stage_update(dtype_of<Number>::value, n, bi_[s] * time_step, ai, Ki_.data(), solution.data(),
+                                 Ti_.data(), stream));
+      cur = &Ti_;
+    }
+  }
+
+ private:
+  DeviceVector<Number>& Ki_;
+  DeviceVector<Number>& Ti_;
+  bool only_Ti_is_ghosted_;
+  hd_lsrk* rk_ = nullptr;
+  int ns_ = 0;
+  std::vector<double> ai_, bi_, ci_;
+};
+
+// Fixed-step time loop (source/base/time_loop.cc:33-67): diagnostics at the
+// start time and after every step; final_time * (1 + 1e-13) guards round-off.
+template <typename Number, typename Vector>
+class TimeLoop {
+ public:
+  TimeLoop(Number time_step, Number start_time, Number final_time, unsigned max_steps = 100000000u)
+      : dt_(time_step), t0_(start_time), t1_(final_time), max_steps_(max_steps) {}
+
+  template <typename Integrator, typename Runnable, typename Diagnostics>
+  int loop(Vector& solution, Integrator&& time_integrator, Runnable&& runnable, Diagnostics&& diagnostics) const {
+    unsigned n = 1;
+    diagnostics(t0_);
+    for (Number t = t0_ + dt_; t <= t1_ * Number(1.0000000000001) && n <= max_steps_; t += dt_, ++n) {
+      time_integrator(solution, t - dt_, dt_, runnable);
+      diagnostics(t);
+    }
+    return int(n - 1);
+  }
+
+ private:
+  Number dt_, t0_, t1_;
+  unsigned max_steps_;
+};
+
+struct VectorTools {
+  template <typename Number>
+  static void interpolate(const AdvectionOperation<Number>& op, const hd_function& f, DeviceVector<Number>& dst,
+                          const double time = 0.0) {
+    check(hd_interpolate(op.handle(), &f, time, dst.data(), op.stream()));
+  }
+  // {L2 norm of src, L2 error against f(., time)} at the collocation points
+  template <typename Number>
+  static std::pair<double, double> norm_and_error(const AdvectionOperation<Number>& op, const hd_function& f,
+                                                  const DeviceVector<Number>& src, const double time) {
+    double r[2] = {0.0, 0.0};
+    check(hd_norm_and_error(op.handle(), &f, time, src.data(), r, op.stream()));
+    return {r[0], r[1]};
+  }
+};
+
+// dt = min(TimeStep, CFL * dt_crit / k^1.5), then T / ceil(T / dt)
+// (examples/advection/include/application.h:363-392)
+inline double time_step_rule(double time_step, double cfl, double critical, int degree, double start, double final) {
+  const double dt = std::fmin(time_step, cfl * critical / std::pow(double(degree), 1.5));
+  return (final - start) / std::ceil((final - start) / dt);
+}
+
+}  // namespace hyperdeal_gb300
+
+#endif  // HYPERDEAL_GB300_HPP

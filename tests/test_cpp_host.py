@@ -1,0 +1,46 @@
+"""The C++ host side: include/hyperdeal_gb300.hpp and the advection application
+built on it (hyperdeal_gb300/cpp/advection_hyperrectangle.cc)."""
+import json
+import os
+import re
+import subprocess
+
+import pytest
+
+from hyperdeal_gb300 import build as B
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_goldens.json")))
+
+
+def _rows(text):
+    return [tuple(float(v) for v in re.findall(r"[-+]?\d\.\d+e[-+]\d+", line)) for line in text.splitlines()
+            if "Time:" in line]
+
+
+def test_cpp_application_builds_and_reports_usage():
+    exe = B.build_cpp_app()
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 2 and "usage" in r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,args", [
+    ("adv_2D_2D_k3.hyperrectangle_05", ["2", "2", "3", "4", "0", "1.0", "rk45"]),
+])
+def test_cpp_application_reproduces_reference_golden(name, args):
+    """The reference's golden time series (ECL + Dirichlet + Gauss-Lobatto collocation) from the C++ host."""
+    exe = B.build_cpp_app()
+    r = subprocess.run([exe] + args + ["f64"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    rows = _rows(r.stdout)
+    ref = [c for c in GOLD["advection"] if c["name"] == name][0]["rows"]
+    assert len(rows) == len(ref)
+    for (t, n, e), (rt, rn, re_) in zip(rows, ref):
+        assert abs(t - rt) <= 0.5e-3 * max(abs(rt), 1e-3) + 1e-12
+        assert abs(n - rn) <= max(1e-5, 1e-8 * abs(rn)) and abs(n - rn) / rn < 1e-9
+        assert abs(e - re_) <= max(1e-5, 1e-8 * abs(re_))
+    # the FP32-storage form of the same run stays within 1e-5 of the FP64 norms
+    r32 = subprocess.run([exe] + args + ["f32"], capture_output=True, text=True, timeout=600)
+    assert r32.returncode == 0, r32.stderr
+    for (t, n, e), (t2, n2, e2) in zip(rows, _rows(r32.stdout)):
+        assert abs(n2 - n) / n < 1e-5
