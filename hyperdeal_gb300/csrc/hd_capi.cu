@@ -204,6 +204,7 @@ struct hd_adv {
   hd::VecGeom geom;
   double* d_partials;  // norm reduction scratch (2*kNormBlocks + 2 doubles) + error flag
   int* d_err;          // device error flag of the pipelined kernel (inside d_partials)
+  double* d_table;     // factor table of product functions (sum_d cells_d * (k+1) doubles)
   int device;
   int variant;         // HD_KERNEL_AUTO / _GENERIC / _PIPELINED
 };
@@ -380,6 +381,12 @@ int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
     e = cudaMemset(op->d_err, 0, sizeof(int));
     if (e != cudaSuccess) { cudaFree(op->d_partials); delete op; return cuda_fail(e, "cudaMemset (error flag)"); }
     op->variant = HD_KERNEL_AUTO;
+    {
+      size_t tsize = 0;
+      for (int i = 0; i < op->D; ++i) tsize += size_t(op->cells[i]) * op->N;
+      e = cudaMalloc(&op->d_table, sizeof(double) * tsize);
+      if (e != cudaSuccess) { cudaFree(op->d_partials); delete op; return cuda_fail(e, "cudaMalloc (function table)"); }
+    }
     *out = op;
     return HD_OK;
   } catch (...) {
@@ -390,6 +397,7 @@ int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
 int hd_adv_destroy(hd_adv* op) {
   if (!op) return HD_OK;
   if (op->d_partials) cudaFree(op->d_partials);
+  if (op->d_table) cudaFree(op->d_table);
   delete op;
   return HD_OK;
 }
@@ -444,7 +452,9 @@ int hd_adv_apply(hd_adv* op, void* dst, const void* src, double time, void* stre
 
 int hd_interpolate(hd_adv* op, const hd_function* f, double time, void* dst, void* stream) {
   if (!op || !f || !dst) return fail(HD_ERR_INVALID, "hd_interpolate: null argument");
-  cudaError_t e = hd::launch_interpolate(op->geom, to_dev(*f), time, dst, op->dtype == HD_F32, (cudaStream_t)stream);
+  if (f->kind < 0 || f->kind > 2) return fail(HD_ERR_INVALID, "hd_interpolate: unknown function kind %d", f->kind);
+  cudaError_t e = hd::launch_interpolate(op->geom, to_dev(*f), time, dst, op->dtype == HD_F32, op->d_table,
+                                         (cudaStream_t)stream);
   return e == cudaSuccess ? HD_OK : cuda_fail(e, "interpolate kernel");
 }
 
@@ -452,8 +462,9 @@ int hd_norm_and_error(hd_adv* op, const hd_function* f, double time, const void*
                       void* stream) {
   if (!op || !f || !src || !result) return fail(HD_ERR_INVALID, "hd_norm_and_error: null argument");
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = hd::launch_norm_error(op->geom, to_dev(*f), time, src, op->dtype == HD_F32, op->d_partials,
-                                        op->d_partials + 2 * hd::kNormBlocks, s);
+  if (f->kind < 0 || f->kind > 2) return fail(HD_ERR_INVALID, "hd_norm_and_error: unknown function kind %d", f->kind);
+  cudaError_t e = hd::launch_norm_error(op->geom, to_dev(*f), time, src, op->dtype == HD_F32, op->d_table,
+                                        op->d_partials, op->d_partials + 2 * hd::kNormBlocks, s);
   if (e != cudaSuccess) return cuda_fail(e, "norm kernel");
   e = cudaMemcpyAsync(result, op->d_partials + 2 * hd::kNormBlocks, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_fail(e, "norm copy");

@@ -12,47 +12,81 @@
 
 namespace hd {
 
-// geometry of a nodal DG vector (cell gid, node -> coordinates)
-__device__ __forceinline__ void node_coords(const VecGeom& g, long long i, double* x, double* jxw) {
-  const long long gid = i / g.NC;
-  int node = int(i - gid * g.NC);
+// The analytic functions are products of one-dimensional factors, so their
+// values at the nodes are products of table entries: table[off_d + c*N + i]
+// holds factor d at x_d = lo_d + (c + gl_i) h_d (kind 2); the amplitude is
+// applied once per node.  One table kernel per call, then one block per cell.
+__global__ void function_table_kernel(VecGeom g, DevFunction f, double t, double* __restrict__ table, int total) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= total) return;
+  int d = 0, off = 0;
+  while (d < g.D - 1 && e >= off + g.cells[d] * g.N) {
+    off += g.cells[d] * g.N;
+    ++d;
+  }
+  const int c = (e - off) / g.N, i = (e - off) % g.N;
+  const double x = g.lo[d] + (c + g.gl[i]) * g.h[d];
+  const double arg = f.omega[d] * (x - f.speed[d] * t) + f.phase[d];
+  table[e] = f.cosine[d] ? cos(arg) : sin(arg);
+}
+
+// cell coordinates of cell gid and the table offsets of its factors
+__device__ __forceinline__ void cell_offsets(const VecGeom& g, long long gid, int* toff) {
   long long gx = gid % g.ncx, gv = gid / g.ncx;
-  double j = 1.0;
+  int off = 0;
   for (int d = 0; d < g.D; ++d) {
     int c;
     if (d < g.dim_x) { c = int(gx % g.cells[d]); gx /= g.cells[d]; }
     else { c = int(gv % g.cells[d]); gv /= g.cells[d]; }
+    toff[d] = off + c * g.N;
+    off += g.cells[d] * g.N;
+  }
+}
+
+__device__ __forceinline__ double node_value(const VecGeom& g, const DevFunction& f, const double* table,
+                                             const int* toff, int node, double* jxw) {
+  double v = f.kind == 0 ? 0.0 : f.amp, j = 1.0;
+  for (int d = 0; d < g.D; ++d) {
     const int id = node % g.N;
     node /= g.N;
-    x[d] = g.lo[d] + (c + g.gl[id]) * g.h[d];
+    if (f.kind == 2) v *= table[toff[d] + id];
     j *= g.h[d] * g.glw[id];
   }
   *jxw = j;
+  return v;
 }
 
 template <typename T>
-__global__ void interpolate_kernel(VecGeom g, DevFunction f, double t, T* __restrict__ dst, long long n) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    double x[kMaxDim], jxw;
-    node_coords(g, i, x, &jxw);
-    dst[i] = T(eval_function(f, x, g.D, t));
+__global__ void interpolate_kernel(VecGeom g, DevFunction f, const double* __restrict__ table, T* __restrict__ dst,
+                                   long long n_cells) {
+  for (long long gid = blockIdx.x; gid < n_cells; gid += gridDim.x) {
+    int toff[kMaxDim];
+    cell_offsets(g, gid, toff);
+    T* out = dst + gid * g.NC;
+    for (int node = threadIdx.x; node < g.NC; node += blockDim.x) {
+      double jxw;
+      out[node] = T(node_value(g, f, table, toff, node, &jxw));
+    }
   }
 }
 
-// per-block partial sums of (v^2 JxW, (v - f)^2 JxW) in fixed order
+// per-block partial sums of (v^2 JxW, (v - f)^2 JxW); block b handles cells b, b + gridDim, ...
 template <typename T>
-__global__ void norm_error_kernel(VecGeom g, DevFunction f, double t, const T* __restrict__ src, long long n,
-                                  double* __restrict__ partials) {
+__global__ void norm_error_kernel(VecGeom g, DevFunction f, const double* __restrict__ table,
+                                  const T* __restrict__ src, long long n_cells, double* __restrict__ partials) {
   double s0 = 0.0, s1 = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    double x[kMaxDim], jxw;
-    node_coords(g, i, x, &jxw);
-    const double v = double(src[i]);
-    const double e = v - eval_function(f, x, g.D, t);
-    s0 += v * v * jxw;
-    s1 += e * e * jxw;
+  for (long long gid = blockIdx.x; gid < n_cells; gid += gridDim.x) {
+    int toff[kMaxDim];
+    cell_offsets(g, gid, toff);
+    const T* in = src + gid * g.NC;
+    for (int node = threadIdx.x; node < g.NC; node += blockDim.x) {
+      double jxw;
+      const double ex = node_value(g, f, table, toff, node, &jxw);
+      const double v = double(in[node]);
+      const double e = v - ex;
+      s0 += v * v * jxw;
+      s1 += e * e * jxw;
+    }
   }
   __shared__ double r0[32], r1[32];
   for (int o = 16; o > 0; o >>= 1) {
@@ -98,21 +132,42 @@ static unsigned grid_for(long long n, int threads, int max_blocks) {
   return unsigned(b);
 }
 
+static int table_size(const VecGeom& g) {
+  int total = 0;
+  for (int d = 0; d < g.D; ++d) total += g.cells[d] * g.N;
+  return total;
+}
+
+static cudaError_t fill_table(const VecGeom& g, const DevFunction& f, double t, double* table, cudaStream_t s) {
+  if (f.kind != 2) return cudaSuccess;
+  const int total = table_size(g);
+  function_table_kernel<<<(total + 127) / 128, 128, 0, s>>>(g, f, t, table, total);
+  return cudaGetLastError();
+}
+
+static int node_threads(const VecGeom& g) { return g.NC >= 256 ? 256 : ((g.NC + 31) / 32) * 32; }
+
 cudaError_t launch_interpolate(const VecGeom& g, const DevFunction& f, double t, void* dst, int is_f32,
-                               cudaStream_t s) {
-  const long long n = g.n_dofs;
-  const unsigned grid = grid_for(n, 256, 152 * 32);
-  if (is_f32) interpolate_kernel<float><<<grid, 256, 0, s>>>(g, f, t, (float*)dst, n);
-  else interpolate_kernel<double><<<grid, 256, 0, s>>>(g, f, t, (double*)dst, n);
+                               double* table, cudaStream_t s) {
+  cudaError_t e = fill_table(g, f, t, table, s);
+  if (e != cudaSuccess) return e;
+  const long long n_cells = g.n_dofs / g.NC;
+  const unsigned grid = unsigned(n_cells < 152 * 64 ? n_cells : 152 * 64);
+  if (is_f32) interpolate_kernel<float><<<grid, node_threads(g), 0, s>>>(g, f, table, (float*)dst, n_cells);
+  else interpolate_kernel<double><<<grid, node_threads(g), 0, s>>>(g, f, table, (double*)dst, n_cells);
   return cudaGetLastError();
 }
 
 cudaError_t launch_norm_error(const VecGeom& g, const DevFunction& f, double t, const void* src, int is_f32,
-                              double* partials, double* out, cudaStream_t s) {
-  const long long n = g.n_dofs;
+                              double* table, double* partials, double* out, cudaStream_t s) {
+  cudaError_t e = fill_table(g, f, t, table, s);
+  if (e != cudaSuccess) return e;
+  const long long n_cells = g.n_dofs / g.NC;
   const unsigned grid = kNormBlocks;
-  if (is_f32) norm_error_kernel<float><<<grid, 256, 0, s>>>(g, f, t, (const float*)src, n, partials);
-  else norm_error_kernel<double><<<grid, 256, 0, s>>>(g, f, t, (const double*)src, n, partials);
+  if (is_f32)
+    norm_error_kernel<float><<<grid, node_threads(g), 0, s>>>(g, f, table, (const float*)src, n_cells, partials);
+  else
+    norm_error_kernel<double><<<grid, node_threads(g), 0, s>>>(g, f, table, (const double*)src, n_cells, partials);
   reduce_partials_kernel<<<1, 32, 0, s>>>(partials, int(grid), out);
   return cudaGetLastError();
 }

@@ -18,10 +18,11 @@ struct VecGeom {
   double gl[kMaxN], glw[kMaxN];
 };
 
+// `table` holds sum_d cells_d * (k+1) doubles (the factors of a product function)
 cudaError_t launch_interpolate(const VecGeom& g, const DevFunction& f, double t, void* dst, int is_f32,
-                               cudaStream_t s);
+                               double* table, cudaStream_t s);
 cudaError_t launch_norm_error(const VecGeom& g, const DevFunction& f, double t, const void* src, int is_f32,
-                              double* partials, double* out, cudaStream_t s);
+                              double* table, double* partials, double* out, cudaStream_t s);
 cudaError_t launch_lsrk_update(int is_f32, long long n, double bi, double ai, const void* K, void* sol,
                                void* next_T, cudaStream_t s);
 
