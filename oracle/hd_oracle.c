@@ -248,6 +248,17 @@ static void apply_1d(const ctx_t *c, const double *A, int transpose, int d,
 static double func_value(const hdo_func *f, int D, const double *x, double t) {
   if (f->kind == 0) return 0.0;
   if (f->kind == 1) return f->amp;
+  if (f->kind == 3) {
+    /* (1 + amp prod_{cosine[d]==1} cos(omega_d x_d + phase_d)) prod_{cosine[d]==2} exp(-x_d^2/2)/sqrt(2 pi)
+       (examples/vlasov_poisson/cases/hyperrectangle.h:45-58) */
+    double pert = f->amp, r = 1.0;
+    for (int d = 0; d < D; ++d)
+      if (f->cosine[d] == 1) pert *= cos(f->omega[d] * x[d] + f->phase[d]);
+    r += pert;
+    for (int d = 0; d < D; ++d)
+      if (f->cosine[d] == 2) r = r * exp(-0.5 * x[d] * x[d]) / sqrt(2.0 * M_PI);
+    return r;
+  }
   double r = f->amp;
   for (int d = 0; d < D; ++d) {
     double arg = f->omega[d] * (x[d] - f->speed[d] * t) + f->phase[d];
@@ -282,6 +293,29 @@ static void read_cell(src_t src, long long gid, int NC, double *out) {
   }
 }
 
+/* velocity component d at the cell's quadrature point with multi-index
+   (via node strides) q: constant (p->velocity) or the Vlasov-Poisson
+   phase-space field, x-velocity = v-coordinate of the point, v-velocity =
+   efield at the point's x-quadrature index (velocity_field_view.h:103-209 of
+   the reference's vlasov_poisson example).  For face points the digit of
+   the face-normal direction is ignored (the field does not depend on it). */
+static double velocity_at(const hdo_problem *p, const ctx_t *c, const int *cc, int d, int q) {
+  if (!p->efield) return p->velocity[d];
+  const int dx = c->dx, n = c->n;
+  if (d < dx) {
+    const int dv = dx + d; /* the v-direction paired with x-direction d */
+    return p->lo[dv] + (cc[dv] + c->pts[(q / c->nstride[dv]) % n]) * c->h[dv];
+  }
+  long long gx = 0;
+  int qx = 0, sx = 1;
+  for (int e = 0; e < dx; ++e) {
+    gx += cc[e] * c->cstride[e];
+    qx += ((q / c->nstride[e]) % n) * sx;
+    sx *= n;
+  }
+  return p->efield[(gx * sx + qx) * dx + (d - dx)];
+}
+
 /* operator values of cell gid written to out[0 .. NC) */
 static void apply_cell(const hdo_problem *p, const ctx_t *c, src_t src,
                        double *out, double time, long long gid, double *work) {
@@ -304,14 +338,14 @@ static void apply_cell(const hdo_problem *p, const ctx_t *c, src_t src,
   for (int d = 0; d < D; ++d) {
     if (s != 1.0) {
       for (int q = 0; q < NC; ++q)
-        tmp[q] = ((1.0 - s) * v[q] * p->velocity[d]) * (1.0 / c->h[d]) * cell_jxw(c, q);
+        tmp[q] = ((1.0 - s) * v[q] * velocity_at(p, c, cc, d, q)) * (1.0 / c->h[d]) * cell_jxw(c, q);
       apply_1d(c, c->Dq, 1, d, tmp, r, 1);
     }
     if (s != 0.0) {
       /* -s (a . grad u) JxW as a value term (submit_value) */
       apply_1d(c, c->Dq, 0, d, v, tmp2, 0);
       for (int q = 0; q < NC; ++q)
-        r[q] += -s * (tmp2[q] * (1.0 / c->h[d]) * p->velocity[d]) * cell_jxw(c, q);
+        r[q] += -s * (tmp2[q] * (1.0 / c->h[d]) * velocity_at(p, c, cc, d, q)) * cell_jxw(c, q);
     }
   }
 
@@ -385,8 +419,8 @@ static void apply_cell(const hdo_problem *p, const ctx_t *c, src_t src,
         }
       }
     }
-    const double an = p->velocity[d] * (side ? 1.0 : -1.0);
     for (int l = 0; l < NF; ++l) {
+      const double an = velocity_at(p, c, cc, d, fb[l]) * (side ? 1.0 : -1.0);
       double jxw = 1.0;
       for (int e = 0; e < D; ++e)
         if (e != d) jxw *= c->h[e] * c->w[(fb[l] / c->nstride[e]) % n];
@@ -632,12 +666,18 @@ double hdo_critical_time_step(const hdo_problem *p) {
   return fmin(1.0 / vx, 1.0 / vv);
 }
 
-/* v-space integral of f for every x-node (vector_tools.h:230-315 without the
-   MPI reduction); rho is laid out like an x-space DG vector
-   (x-cell gid_x * n^dim_x + i_x).  Collocation only. */
+/* ------------------------------------------------------------------------ */
+/* Vlasov-Poisson pieces (examples/vlasov_poisson/include/application.h:516-602) */
+/* ------------------------------------------------------------------------ */
+
+/* v-space integral of f for every x-DoF: rho[gid_x * n^dim_x + i_x] =
+   sum over v-cells and v-nodes of f * JxW_v with the Gauss-Lobatto support
+   points (quad_no_v = 2) applied to the raw DoF values
+   (numerics/vector_tools.h:230-315; the index i_x + n^dim_v i_v there equals
+   i_x + n^dim_x i_v because dim_x == dim_v). */
 int hdo_velocity_moment(const hdo_problem *p, const double *src, double *rho) {
   ctx_t c;
-  if (make_ctx(p, &c) || !p->collocation) return -1;
+  if (make_ctx(p, &c)) return -1;
   int nx = 1, nv = 1;
   for (int d = 0; d < c.dx; ++d) nx *= c.n;
   for (int d = c.dx; d < c.D; ++d) nv *= c.n;
@@ -652,11 +692,330 @@ int hdo_velocity_moment(const hdo_problem *p, const double *src, double *rho) {
         for (int iv = 0; iv < nv; ++iv) {
           double w = jv;
           int t = iv;
-          for (int d = c.dx; d < c.D; ++d) { w *= c.w[t % c.n]; t /= c.n; }
+          for (int d = c.dx; d < c.D; ++d) { w *= c.glw[t % c.n]; t /= c.n; }
           acc += u[ix + nx * iv] * w;
         }
       }
       rho[gx * nx + ix] = acc;
     }
+  return 0;
+}
+
+/* x-space view of a phase-space context */
+typedef struct {
+  int dx, n, NCx;
+  long long ncx;
+  int nstride[3];
+  long long cstride[3];
+  int cells[3];
+  double h[3];
+  const ctx_t *c;
+  double dval[2][MAXN]; /* psi_j'(0), psi_j'(1) of the point basis */
+} xctx_t;
+
+static void make_xctx(const ctx_t *c, xctx_t *x) {
+  x->dx = c->dx; x->n = c->n; x->c = c;
+  x->NCx = 1;
+  for (int d = 0; d < c->dx; ++d) {
+    x->nstride[d] = x->NCx;
+    x->NCx *= c->n;
+    x->cstride[d] = c->cstride[d];
+    x->cells[d] = c->cells[d];
+    x->h[d] = c->h[d];
+  }
+  x->ncx = c->ncx;
+  lagrange_derivs(c->n, c->pts, 0.0, x->dval[0]);
+  lagrange_derivs(c->n, c->pts, 1.0, x->dval[1]);
+}
+
+/* out (+)= A along x-direction d of an x-space cell tensor */
+static void xapply_1d(const xctx_t *x, const double *A, int transpose, int d, const double *in, double *out,
+                      int add) {
+  const int n = x->n, s = x->nstride[d];
+  for (int base = 0; base < x->NCx; ++base) {
+    if ((base / s) % n != 0) continue;
+    double tout[MAXN];
+    for (int o = 0; o < n; ++o) {
+      double acc = 0.0;
+      for (int i = 0; i < n; ++i) acc += (transpose ? A[i * n + o] : A[o * n + i]) * in[base + i * s];
+      tout[o] = acc;
+    }
+    for (int o = 0; o < n; ++o) out[base + o * s] = add ? out[base + o * s] + tout[o] : tout[o];
+  }
+}
+
+static double xjxw(const xctx_t *x, int q, int skip) {
+  double j = 1.0;
+  for (int d = 0; d < x->dx; ++d)
+    if (d != skip) j *= x->h[d] * x->c->w[(q / x->nstride[d]) % x->n];
+  return j;
+}
+
+/* point values of an x-space DG cell (basis change for Gauss) */
+static void xvalues(const xctx_t *x, const double *u, double *v, double *tmp) {
+  memcpy(v, u, sizeof(double) * x->NCx);
+  for (int d = 0; d < x->dx; ++d) {
+    xapply_1d(x, x->c->S, 0, d, v, tmp, 0);
+    memcpy(v, tmp, sizeof(double) * x->NCx);
+  }
+}
+
+/* point-basis test values -> DoF test values (S^T in every direction) */
+static void xtest(const xctx_t *x, double *r, double *tmp) {
+  for (int d = 0; d < x->dx; ++d) {
+    xapply_1d(x, x->c->S, 1, d, r, tmp, 0);
+    memcpy(r, tmp, sizeof(double) * x->NCx);
+  }
+}
+
+static double vec_mean(const double *v, long long n) {
+  double s = 0.0;
+  for (long long i = 0; i < n; ++i) s += v[i];
+  return s / (double)n;
+}
+
+/* SIPG Laplacian on the periodic x-mesh with the problem's quadrature, src
+   mean removed first (examples/vlasov_poisson/include/poisson.h:100-255):
+   cell  int grad u . grad v;
+   faces int sigma [u][v] - {d_n u}[v] - [u]{d_n v},
+         sigma = (1/h_- + 1/h_+) k (k+1) (the inverse cell extents normal to the face). */
+int hdo_poisson_apply(const hdo_problem *p, const double *src, double *dst) {
+  ctx_t c;
+  if (make_ctx(p, &c)) return -1;
+  xctx_t x;
+  make_xctx(&c, &x);
+  const int NCx = x.NCx, n = x.n;
+  const long long N = x.ncx * NCx;
+  double *u = (double *)malloc(sizeof(double) * N);
+  double *vals = (double *)malloc(sizeof(double) * N);
+  double *rp = (double *)calloc(N, sizeof(double));
+  if (!u || !vals || !rp) { free(u); free(vals); free(rp); return -1; }
+  const double mean = vec_mean(src, N);
+  for (long long i = 0; i < N; ++i) u[i] = src[i] - mean;
+  const int k = p->degree;
+  const double pen = (double)(k > 1 ? k : 1) * (k + 1.0);
+  /* point values of all cells */
+  {
+    double *tmp = (double *)malloc(sizeof(double) * NCx);
+    for (long long g = 0; g < x.ncx; ++g) xvalues(&x, u + g * NCx, vals + g * NCx, tmp);
+    free(tmp);
+  }
+  /* cells */
+  for (long long g = 0; g < x.ncx; ++g) {
+    double grad[MAXN * MAXN * MAXN], t[MAXN * MAXN * MAXN];
+    for (int d = 0; d < x.dx; ++d) {
+      xapply_1d(&x, c.Dq, 0, d, vals + g * NCx, grad, 0);
+      for (int q = 0; q < NCx; ++q) t[q] = grad[q] / x.h[d] * xjxw(&x, q, -1) / x.h[d];
+      xapply_1d(&x, c.Dq, 1, d, t, rp + g * NCx, 1);
+    }
+  }
+  /* faces: the right face of every cell in every direction (periodic pairs) */
+  for (long long g = 0; g < x.ncx; ++g) {
+    int cc[3];
+    long long rem = g;
+    for (int d = 0; d < x.dx; ++d) { cc[d] = (int)(rem % x.cells[d]); rem /= x.cells[d]; }
+    for (int d = 0; d < x.dx; ++d) {
+      const long long gR = cc[d] + 1 < x.cells[d] ? g + x.cstride[d] : g - (long long)(x.cells[d] - 1) * x.cstride[d];
+      const double *vL = vals + g * NCx, *vR = vals + gR * NCx;
+      const int sd = x.nstride[d];
+      const double sigma = (1.0 / x.h[d] + 1.0 / x.h[d]) * pen;
+      for (int b = 0; b < NCx; ++b) {
+        if ((b / sd) % n != 0) continue;
+        double uL = 0.0, uR = 0.0, dL = 0.0, dR = 0.0;
+        for (int j = 0; j < n; ++j) {
+          uL += c.fval[1][j] * vL[b + j * sd];
+          uR += c.fval[0][j] * vR[b + j * sd];
+          dL += x.dval[1][j] * vL[b + j * sd];
+          dR += x.dval[0][j] * vR[b + j * sd];
+        }
+        dL /= x.h[d];
+        dR /= x.h[d];
+        const double jxw = xjxw(&x, b, d);
+        const double jump = uL - uR, avg = 0.5 * (dL + dR);
+        const double vt = (sigma * jump - avg) * jxw, nt = -0.5 * jump * jxw;
+        for (int j = 0; j < n; ++j) {
+          rp[g * NCx + b + j * sd] += c.fval[1][j] * vt + x.dval[1][j] / x.h[d] * nt;
+          rp[gR * NCx + b + j * sd] += -c.fval[0][j] * vt + x.dval[0][j] / x.h[d] * nt;
+        }
+      }
+    }
+  }
+  {
+    double *tmp = (double *)malloc(sizeof(double) * NCx);
+    for (long long g = 0; g < x.ncx; ++g) xtest(&x, rp + g * NCx, tmp);
+    free(tmp);
+  }
+  memcpy(dst, rp, sizeof(double) * N);
+  free(u); free(vals); free(rp);
+  return 0;
+}
+
+/* conjugate gradients on the singular SIPG system (no preconditioner; the
+   converged solution does not depend on it).  phi holds the initial guess
+   and receives the solution; stops at ||r|| <= rel_tol ||r_0||. */
+int hdo_poisson_solve(const hdo_problem *p, const double *rhs, double *phi, double rel_tol, int max_it,
+                      int *iterations) {
+  ctx_t c;
+  if (make_ctx(p, &c)) return -1;
+  long long N = c.ncx;
+  for (int d = 0; d < c.dx; ++d) N *= c.n;
+  double *r = (double *)malloc(sizeof(double) * N), *pp = (double *)malloc(sizeof(double) * N);
+  double *Ap = (double *)malloc(sizeof(double) * N);
+  if (!r || !pp || !Ap) { free(r); free(pp); free(Ap); return -1; }
+  hdo_poisson_apply(p, phi, Ap);
+  double rr = 0.0;
+  for (long long i = 0; i < N; ++i) { r[i] = rhs[i] - Ap[i]; pp[i] = r[i]; rr += r[i] * r[i]; }
+  const double r0 = sqrt(rr);
+  /* a floor at round-off level of the right-hand side keeps a warm start from
+     iterating on noise */
+  double bb = 0.0;
+  for (long long i = 0; i < N; ++i) bb += rhs[i] * rhs[i];
+  const double floor_tol = 1e-14 * sqrt(bb);
+  int it = 0;
+  while (sqrt(rr) > rel_tol * r0 && sqrt(rr) > floor_tol && it < max_it) {
+    hdo_poisson_apply(p, pp, Ap);
+    double pAp = 0.0;
+    for (long long i = 0; i < N; ++i) pAp += pp[i] * Ap[i];
+    if (!(pAp > 0.0)) break;
+    const double alpha = rr / pAp;
+    double rr_new = 0.0;
+    for (long long i = 0; i < N; ++i) {
+      phi[i] += alpha * pp[i];
+      r[i] -= alpha * Ap[i];
+      rr_new += r[i] * r[i];
+    }
+    const double beta = rr_new / rr;
+    for (long long i = 0; i < N; ++i) pp[i] = r[i] + beta * pp[i];
+    rr = rr_new;
+    ++it;
+  }
+  if (iterations) *iterations = it;
+  free(r); free(pp); free(Ap);
+  return 0;
+}
+
+/* right-hand side of the Poisson problem from the charge density:
+   rho~ = rho - mean(rho); rhs_i = -int psi_i rho~; rhs -= mean(rhs)
+   (examples/vlasov_poisson/include/application.h:531-568) */
+int hdo_poisson_rhs(const hdo_problem *p, const double *rho, double *rhs) {
+  ctx_t c;
+  if (make_ctx(p, &c)) return -1;
+  xctx_t x;
+  make_xctx(&c, &x);
+  const long long N = x.ncx * x.NCx;
+  const double mr = vec_mean(rho, N);
+  double *v = (double *)malloc(sizeof(double) * x.NCx), *tmp = (double *)malloc(sizeof(double) * x.NCx);
+  double *u = (double *)malloc(sizeof(double) * x.NCx);
+  for (long long g = 0; g < x.ncx; ++g) {
+    for (int i = 0; i < x.NCx; ++i) u[i] = rho[g * x.NCx + i] - mr;
+    xvalues(&x, u, v, tmp);
+    for (int q = 0; q < x.NCx; ++q) v[q] = -v[q] * xjxw(&x, q, -1);
+    xtest(&x, v, tmp);
+    memcpy(rhs + g * x.NCx, v, sizeof(double) * x.NCx);
+  }
+  const double m2 = vec_mean(rhs, N);
+  for (long long i = 0; i < N; ++i) rhs[i] -= m2;
+  free(v); free(tmp); free(u);
+  return 0;
+}
+
+/* gradient of the potential at the x-quadrature points (the negative electric
+   field, examples/vlasov_poisson/include/derivative_container.h:158-251):
+   E[(gid_x * n^dim_x + q) * dim_x + d] */
+int hdo_vp_field(const hdo_problem *p, const double *phi, double *E) {
+  ctx_t c;
+  if (make_ctx(p, &c)) return -1;
+  xctx_t x;
+  make_xctx(&c, &x);
+  double v[MAXN * MAXN * MAXN], tmp[MAXN * MAXN * MAXN], g[MAXN * MAXN * MAXN];
+  for (long long gx = 0; gx < x.ncx; ++gx) {
+    xvalues(&x, phi + gx * x.NCx, v, tmp);
+    for (int d = 0; d < x.dx; ++d) {
+      xapply_1d(&x, c.Dq, 0, d, v, g, 0);
+      for (int q = 0; q < x.NCx; ++q) E[(gx * x.NCx + q) * x.dx + d] = g[q] / x.h[d];
+    }
+  }
+  return 0;
+}
+
+/* one evaluation of the Vlasov-Poisson right-hand side: rho, Poisson rhs,
+   CG from the previous potential (phi, in/out), field E (out), then the
+   advection operator with the phase-space velocity (v, E) */
+int hdo_vp_operator(const hdo_problem *p, const double *f, double *dst, double time, double *phi, double *E,
+                    double cg_tol, int *iterations) {
+  ctx_t c;
+  if (make_ctx(p, &c)) return -1;
+  long long Nx = c.ncx;
+  for (int d = 0; d < c.dx; ++d) Nx *= c.n;
+  double *rho = (double *)malloc(sizeof(double) * Nx), *rhs = (double *)malloc(sizeof(double) * Nx);
+  if (!rho || !rhs) { free(rho); free(rhs); return -1; }
+  hdo_velocity_moment(p, f, rho);
+  hdo_poisson_rhs(p, rho, rhs);
+  hdo_poisson_solve(p, rhs, phi, cg_tol, 100000, iterations);
+  hdo_vp_field(p, phi, E);
+  hdo_problem q = *p;
+  q.efield = E;
+  const int rc = hdo_apply(&q, f, dst, time);
+  free(rho); free(rhs);
+  return rc;
+}
+
+/* diagnostics (examples/vlasov_poisson/include/diagnostics.h:28-141):
+   out[0..dim_x) = int (d_d phi)^2 per direction; then mass, L2 norm,
+   kinetic energy int |v|^2 f, and momentum int v_d f (dim_v values) */
+int hdo_vp_diagnostics(const hdo_problem *p, const double *f, const double *phi, double *out) {
+  ctx_t c;
+  if (make_ctx(p, &c)) return -1;
+  xctx_t x;
+  make_xctx(&c, &x);
+  const int dx = c.dx, dv = c.dv;
+  for (int i = 0; i < dx + 3 + dv; ++i) out[i] = 0.0;
+  {
+    double v[MAXN * MAXN * MAXN], tmp[MAXN * MAXN * MAXN], g[MAXN * MAXN * MAXN];
+    for (long long gx = 0; gx < x.ncx; ++gx) {
+      xvalues(&x, phi + gx * x.NCx, v, tmp);
+      for (int d = 0; d < dx; ++d) {
+        xapply_1d(&x, c.Dq, 0, d, v, g, 0);
+        for (int q = 0; q < x.NCx; ++q) {
+          const double gd = g[q] / x.h[d];
+          out[d] += gd * gd * xjxw(&x, q, -1);
+        }
+      }
+    }
+  }
+  double mass = 0.0, l2 = 0.0, kin = 0.0, mom[3] = {0.0, 0.0, 0.0};
+#pragma omp parallel reduction(+ : mass, l2, kin)
+  {
+    double *v = (double *)malloc(sizeof(double) * 2 * c.NC), *tmp = v + c.NC;
+    double mloc[3] = {0.0, 0.0, 0.0};
+#pragma omp for schedule(static)
+    for (long long g = 0; g < c.ncells; ++g) {
+      int cc[HDO_MAX_DIM];
+      cell_coords(&c, g, cc);
+      memcpy(v, f + g * c.NC, sizeof(double) * c.NC);
+      if (!p->collocation)
+        for (int d = 0; d < c.D; ++d) { apply_1d(&c, c.S, 0, d, v, tmp, 0); memcpy(v, tmp, sizeof(double) * c.NC); }
+      for (int q = 0; q < c.NC; ++q) {
+        const double jxw = cell_jxw(&c, q);
+        double vv = 0.0, vel[3];
+        for (int d = 0; d < dv; ++d) {
+          const int e = dx + d;
+          vel[d] = p->lo[e] + (cc[e] + c.pts[(q / c.nstride[e]) % c.n]) * c.h[e];
+          vv += vel[d] * vel[d];
+        }
+        mass += v[q] * jxw;
+        l2 += v[q] * v[q] * jxw;
+        kin += vv * v[q] * jxw;
+        for (int d = 0; d < dv; ++d) mloc[d] += vel[d] * v[q] * jxw;
+      }
+    }
+#pragma omp critical
+    for (int d = 0; d < dv; ++d) mom[d] += mloc[d];
+    free(v);
+  }
+  out[dx] = mass;
+  out[dx + 1] = sqrt(l2);
+  out[dx + 2] = kin;
+  for (int d = 0; d < dv; ++d) out[dx + 3 + d] = mom[d];
   return 0;
 }

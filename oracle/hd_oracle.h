@@ -47,7 +47,10 @@ extern "C" {
  *   kind 0: f = 0
  *   kind 1: f = amp
  *   kind 2: f = amp * prod_d trig_d(omega_d * (x_d - speed_d * t) + phase_d)
- *           with trig_d = cos if cosine[d] else sin.                        */
+ *           with trig_d = cos if cosine[d] else sin.
+ *   kind 3: f = (1 + amp * prod_{cosine[d]==1} cos(omega_d x_d + phase_d))
+ *               * prod_{cosine[d]==2} exp(-x_d^2 / 2) / sqrt(2 pi)
+ *           (perturbed Maxwellian of the Vlasov-Poisson cases).           */
 typedef struct hdo_func {
   int kind;
   double amp;
@@ -71,6 +74,12 @@ typedef struct hdo_problem {
   int bc_inhomogeneous; /* non-periodic faces: 0 -> u+ = -u-, 1 -> u+ = -u- + 2 g */
   hdo_func bc_func;     /* g(x, t) for bc_inhomogeneous                  */
   int n_threads;        /* 0: OpenMP default                             */
+  /* Vlasov-Poisson phase-space velocity (dim_x == dim_v): when non-NULL the
+     x-velocity is the point's v-coordinate and the v-velocity is
+     efield[(gid_x * n^dim_x + qx) * dim_x + d] (the gradient of the
+     potential at the x-quadrature points; velocity_field_view.h:103-209 of
+     the vlasov_poisson example); `velocity` is then unused. */
+  const double *efield;
 } hdo_problem;
 
 /* number of DoFs of the problem */
@@ -115,9 +124,25 @@ int hdo_norm_and_error(const hdo_problem *p, const hdo_func *f, double time,
 /* 1 / max_d |a_d / h_d| over x-space, the same over v-space, min of both */
 double hdo_critical_time_step(const hdo_problem *p);
 
-/* velocity-moment of f over v for every x-node (charge density without
- * mean removal): rho[x_dof] = sum over v-cells and v-nodes of f * JxW_v   */
+/* ---- Vlasov-Poisson (dim_x == dim_v, periodic x-mesh) ------------------- */
+
+/* velocity-moment of f over v for every x-DoF (charge density without mean
+ * removal): rho[x_dof] = sum over v-cells and v-nodes of f * JxW_v        */
 int hdo_velocity_moment(const hdo_problem *p, const double *src, double *rho);
+
+/* SIPG Laplacian on the x-mesh (src mean removed first), its right-hand
+ * side from rho, CG (phi: initial guess in, solution out), the potential
+ * gradient at the x-quadrature points, one full Vlasov-Poisson operator
+ * evaluation and the diagnostics (energy per x-direction, mass, L2 norm,
+ * kinetic energy, momentum per v-direction).                             */
+int hdo_poisson_apply(const hdo_problem *p, const double *src, double *dst);
+int hdo_poisson_rhs(const hdo_problem *p, const double *rho, double *rhs);
+int hdo_poisson_solve(const hdo_problem *p, const double *rhs, double *phi, double rel_tol, int max_it,
+                      int *iterations);
+int hdo_vp_field(const hdo_problem *p, const double *phi, double *E);
+int hdo_vp_operator(const hdo_problem *p, const double *f, double *dst, double time, double *phi, double *E,
+                    double cg_tol, int *iterations);
+int hdo_vp_diagnostics(const hdo_problem *p, const double *f, const double *phi, double *out);
 
 #ifdef __cplusplus
 }

@@ -58,7 +58,7 @@ class _Problem(ctypes.Structure):
                 ("hi", ctypes.c_double * MAX_DIM), ("periodic_x", ctypes.c_int),
                 ("periodic_v", ctypes.c_int), ("velocity", ctypes.c_double * MAX_DIM),
                 ("skew", ctypes.c_double), ("bc_inhomogeneous", ctypes.c_int),
-                ("bc_func", Func), ("n_threads", ctypes.c_int)]
+                ("bc_func", Func), ("n_threads", ctypes.c_int), ("efield", ctypes.POINTER(ctypes.c_double))]
 
 
 def make_func(kind: int = 2, amp: float = 1.0, omega: Sequence[float] = (), speed: Sequence[float] = (),
@@ -160,6 +160,13 @@ def lib():
         L.hdo_velocity_moment.argtypes = [P, dp, dp]
         L.hdo_n_dofs.argtypes = [P]
         L.hdo_n_dofs.restype = ctypes.c_longlong
+        L.hdo_poisson_apply.argtypes = [P, dp, dp]
+        L.hdo_poisson_rhs.argtypes = [P, dp, dp]
+        L.hdo_poisson_solve.argtypes = [P, dp, dp, ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+        L.hdo_vp_field.argtypes = [P, dp, dp]
+        L.hdo_vp_operator.argtypes = [P, dp, dp, ctypes.c_double, dp, dp, ctypes.c_double,
+                                      ctypes.POINTER(ctypes.c_int)]
+        L.hdo_vp_diagnostics.argtypes = [P, dp, dp, dp]
         OPF = ctypes.CFUNCTYPE(None, dp, dp, ctypes.c_double, ctypes.c_void_p)
         L.hdo_lsrk_step_op.argtypes = [ctypes.c_longlong, ctypes.c_char_p, dp, dp, dp,
                                        ctypes.c_double, ctypes.c_double, OPF, ctypes.c_void_p]
@@ -346,3 +353,101 @@ def run_hyperrectangle(dim_x: int, dim_v: int, degree: int, subdivisions: Sequen
 
     time_loop(0.0, final_time, dt, step, diag)
     return rows
+
+
+# --------------------------------------------------------------------------
+# Vlasov-Poisson (examples/vlasov_poisson/include/application.h:400-700)
+# --------------------------------------------------------------------------
+
+def x_dofs(p: Problem) -> int:
+    return int(np.prod(p.cells[:p.dim_x])) * (p.degree + 1) ** p.dim_x
+
+
+def poisson_apply(p: Problem, u: np.ndarray) -> np.ndarray:
+    out = np.empty_like(u)
+    cp = p.c()
+    _check(lib().hdo_poisson_apply(ctypes.byref(cp), _ptr(u), _ptr(out)), "poisson_apply")
+    return out
+
+
+def poisson_rhs(p: Problem, rho: np.ndarray) -> np.ndarray:
+    out = np.empty_like(rho)
+    cp = p.c()
+    _check(lib().hdo_poisson_rhs(ctypes.byref(cp), _ptr(rho), _ptr(out)), "poisson_rhs")
+    return out
+
+
+def poisson_solve(p: Problem, rhs: np.ndarray, phi: np.ndarray, rel_tol: float = 1e-12, max_it: int = 100000) -> int:
+    it = ctypes.c_int(0)
+    cp = p.c()
+    _check(lib().hdo_poisson_solve(ctypes.byref(cp), _ptr(rhs), _ptr(phi), rel_tol, max_it, ctypes.byref(it)),
+           "poisson_solve")
+    return it.value
+
+
+def vp_field(p: Problem, phi: np.ndarray) -> np.ndarray:
+    E = np.zeros(x_dofs(p) * p.dim_x)
+    cp = p.c()
+    _check(lib().hdo_vp_field(ctypes.byref(cp), _ptr(phi), _ptr(E)), "vp_field")
+    return E
+
+
+class VPState:
+    """Potential and field carried between operator evaluations (the reference keeps
+    `potential` as the CG initial guess and prints the energy of the last one)."""
+
+    def __init__(self, p: Problem, cg_tol: float = 1e-12):
+        self.p = p
+        self.phi = np.zeros(x_dofs(p))
+        self.E = np.zeros(x_dofs(p) * p.dim_x)
+        self.cg_tol = cg_tol
+        self.iterations = []
+
+    def operator(self, src: np.ndarray, dst: np.ndarray, t: float) -> None:
+        it = ctypes.c_int(0)
+        cp = self.p.c()
+        _check(lib().hdo_vp_operator(ctypes.byref(cp), _ptr(src), _ptr(dst), t, _ptr(self.phi), _ptr(self.E),
+                                     self.cg_tol, ctypes.byref(it)), "vp_operator")
+        self.iterations.append(it.value)
+
+    def diagnostics(self, f: np.ndarray) -> np.ndarray:
+        out = np.zeros(self.p.dim_x + 3 + self.p.dim_v)
+        cp = self.p.c()
+        _check(lib().hdo_vp_diagnostics(ctypes.byref(cp), _ptr(f), _ptr(self.phi), _ptr(out)), "vp_diagnostics")
+        return out
+
+
+def vp_initial_function(dim_x: int, dim_v: int, eps: float = 0.01, k: float = 0.5,
+                        perturbed_dims: Sequence[int] = (0,)) -> Func:
+    """(1 + eps prod_{d in perturbed_dims} cos(k x_d)) prod_v exp(-v^2/2)/sqrt(2 pi)
+    (examples/vlasov_poisson/cases/hyperrectangle.h:45-58 perturbs x_0 only)."""
+    cos_flags = [1 if d in perturbed_dims else 0 for d in range(dim_x)] + [2] * dim_v
+    return make_func(3, eps, omega=[k] * dim_x + [0.0] * dim_v, cosine=cos_flags)
+
+
+def run_vp_hyperrectangle(dim_x: int = 2, dim_v: int = 2, degree: int = 3, cells_x: int = 4, cells_v: int = 4,
+                          collocation: bool = False, final_time: float = 0.5, time_step: float = 0.1,
+                          cfl: float = 0.05, tick: float = 0.1, rk: str = "rk45", cg_tol: float = 1e-12):
+    """The reference's Vlasov-Poisson application on its hyperrectangle case (x in [0, 4 pi]^dim_x,
+    v in [-6, 6]^dim_v, periodic, transport direction (1, .., 6, ..) for the time-step rule);
+    returns the diagnostics rows (time, energy components, mass, l2, kinetic energy, momentum)."""
+    D = dim_x + dim_v
+    p = Problem(dim_x, dim_v, degree, [cells_x] * dim_x + [cells_v] * dim_v, [0.0] * dim_x + [-6.0] * dim_v,
+                [4 * math.pi] * dim_x + [6.0] * dim_v, [1.0] * dim_x + [6.0] * dim_v, collocation=collocation)
+    f0 = vp_initial_function(dim_x, dim_v)
+    sol = interpolate(p, f0, 0.0)
+    dt = time_step_rule(time_step, cfl, critical_time_step(p), degree, 0.0, final_time)
+    st = VPState(p, cg_tol)
+    cp = p.c()
+    st.p = p
+    rows = []
+
+    def step(t, h):
+        lsrk_step_op(rk, sol, t, h, st.operator)
+
+    def diag(t):
+        if tick_due(t, 0.0, dt, tick):
+            rows.append((t,) + tuple(st.diagnostics(sol)))
+
+    time_loop(0.0, final_time, dt, step, diag)
+    return rows, st

@@ -4,6 +4,8 @@
 Usage:  python tests/golden/make_goldens.py /path/to/hyperdeal
 
 Sources (paths relative to the reference root):
+  examples/vlasov_poisson/tests/*.configuration, *.json, *.out
+      -- Vlasov-Poisson diagnostics (field energy, mass, L2, kinetic energy, momentum)
   examples/advection/tests/*.configuration, *.json, *.out
       -- application time series "Time, norm, error" (compared by numdiff
          -a 1e-5 -r 1e-8, cmake/macros/macro_hyper_deal_pickup_tests.cmake:57)
@@ -74,8 +76,29 @@ def main(root):
         vals = re.findall(NUM, line.split("::", 1)[1]) if "::" in line else []
         if len(vals) == 2:
             vt01.append([float(v) for v in vals])
+    vp = []
+    vp_dir = os.path.join(root, "examples", "vlasov_poisson", "tests")
+    for jpath in sorted(glob.glob(os.path.join(vp_dir, "*.json"))):
+        name = os.path.basename(jpath)[:-5]
+        conf = parse_configuration(os.path.join(vp_dir, name.split(".")[0] + ".configuration"))
+        prm = json.load(open(jpath))
+        rows = [[float(v) for v in line.split()] for line in open(os.path.join(vp_dir, name + ".out"))
+                if line.strip() and not line.startswith("#")]
+        td = prm["TemporalDiscretization"]
+        case = prm["Case"]
+        vp.append({
+            "name": name, "dim_x": conf["DIM_X"], "dim_v": conf["DIM_V"], "degree": conf["DEGREE"],
+            "n_points": conf["N_POINTS"],
+            "cells_x": 2 ** int(case["NRefinementsX"]) * int(case["NSubdivisionsX"]["X"]),
+            "cells_v": 2 ** int(case["NRefinementsV"]) * int(case["NSubdivisionsV"]["X"]),
+            "collocation": prm["SpatialDiscretization"]["DoCollocation"] == "true",
+            "final_time": float(td["FinalTime"]), "time_step": float(td["TimeStep"]), "cfl": float(td["CFLNumber"]),
+            "columns": "time, field energy per x-direction, mass, L2 norm, kinetic energy, momentum (3)",
+            "rows": rows,
+        })
     out = {
         "numdiff": {"abs": 1e-5, "rel": 1e-8},
+        "vlasov_poisson": vp,
         "advection": advection,
         "time_integrators_01_stages": ti01,
         "time_integrators_02_rk45_values": ti02,

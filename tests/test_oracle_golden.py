@@ -111,3 +111,39 @@ def test_oracle_collocation_conservation_and_linearity():
     jxw = np.einsum("i,j,k->kji", w * h[0], w * h[1], w * h[2]).ravel()
     mass = (Au.reshape(-1, 64) * jxw).sum()
     assert abs(mass) < 1e-12 * np.abs(Au).max()
+
+
+@pytest.mark.parametrize("case", GOLD["vlasov_poisson"], ids=[c["name"] for c in GOLD["vlasov_poisson"]])
+def test_vlasov_poisson_application_golden(case):
+    """examples/vlasov_poisson/tests/*.out: the oracle's Vlasov-Poisson (moments, SIPG Poisson + CG,
+    field, phase-space advection, rk45) against the reference's diagnostics time series."""
+    rows, st = O.run_vp_hyperrectangle(case["dim_x"], case["dim_v"], case["degree"], case["cells_x"],
+                                       case["cells_v"], collocation=case["collocation"],
+                                       final_time=case["final_time"], time_step=case["time_step"],
+                                       cfl=case["cfl"])
+    ref = case["rows"]
+    assert len(rows) == len(ref)
+    dx = case["dim_x"]
+    for r, g in zip(rows, ref):
+        assert abs(r[0] - g[0]) <= 1e-3
+        got = list(r[1:1 + dx]) + list(r[1 + dx:])
+        exp = g[1:]
+        for a, b in zip(got, exp):
+            assert numdiff_equal(a, b), (r[0], a, b)
+        # mass, L2 norm and kinetic energy far inside the numdiff bound
+        for a, b in zip(got[dx:dx + 3], exp[dx:dx + 3]):
+            assert abs(a - b) <= 1e-12 * abs(b)
+        # field energy: the reference solves Poisson to a 1e-4 relative residual with multigrid
+        if g[1] > 1e-6:
+            assert abs(got[0] - g[1]) <= 1e-7 * g[1]
+
+
+def test_poisson_sipg_operator_properties():
+    """SIPG matrix: symmetric, positive semi-definite, constants in its kernel (periodic mesh)."""
+    p = O.Problem(2, 2, 3, [3, 4, 2, 2], [0, 0, -6, -6], [4 * math.pi, 4 * math.pi, 6, 6], [1.0] * 4)
+    n = O.x_dofs(p)
+    A = np.stack([O.poisson_apply(p, np.eye(n)[i]) for i in range(n)], axis=1)
+    assert np.abs(A - A.T).max() <= 1e-12 * np.abs(A).max()
+    ev = np.linalg.eigvalsh(0.5 * (A + A.T))
+    assert ev.min() > -1e-10 * ev.max()
+    assert np.abs(O.poisson_apply(p, np.ones(n))).max() < 1e-12
