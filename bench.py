@@ -7,6 +7,7 @@ definition, DoFs * stages * steps / time
 (examples/advection/include/application.h:540-543).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  python bench.py --workload vp2x2v   (the Vlasov-Poisson configuration, its own JSON line)
 
 The FP64 form of the same step is timed after the FP32 form (fewer steps) and
 the relative L2 difference of the two solutions after the timed steps is
@@ -172,6 +173,138 @@ def run_reference(args):
     return 0
 
 
+VP_DIM_X = 2
+VP_CELLS_X, VP_CELLS_V = 16, 32
+VP_CFL = 0.05
+
+
+def vp_config(extra=None):
+    cfg = {"workload": "electrostatic Vlasov-Poisson 2x2v, k=3 Gauss-Lobatto collocation, x in [0,4pi]^2 with "
+                       "16^2 cells, v in [-6,6]^2 with 32^2 cells (262,144 cells, 67,108,864 DoFs; 4,096 x-DoFs), "
+                       "periodic, f0 = (1 + 0.01 cos(0.5 x1) cos(0.5 x2)) exp(-|v|^2/2)/(2 pi), rk45, "
+                       "dt = 0.05 dt_crit / k^1.5 with transport velocity (1, 1, 6, 6)",
+           "dims": "2x+2v", "degree": 3, "n_dofs": 67108864, "x_dofs": 4096, "rk": "rk45",
+           "l2_flush": "inputs larger than L2 (537 MB per FP64 vector vs 129 MB L2)"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def run_vp(args):
+    """Vlasov-Poisson step time and CG iterations with the plain (previous-potential), zero and
+    learned initial guesses at a fixed accuracy ||r|| <= tol ||rhs||, and the field energy
+    against the FP64 oracle after a few steps."""
+    import numpy as np
+    import torch
+
+    from hyperdeal_gb300 import vlasov_poisson as V
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    rank = int(os.environ.get("RANK", "0"))
+    two_pi = 4 * math.pi
+    hx, hv = two_pi / VP_CELLS_X, 12.0 / VP_CELLS_V
+    dt = V.time_step_rule(1.0, VP_CFL, min(hx / 1.0, hv / 6.0), DEGREE, 0.0, 1.0)
+    f0 = V.perturbed_maxwellian(VP_DIM_X, eps=0.01, k=0.5, perturbed_dims=(0, 1))
+
+    def make(guess, dtype, tol, rhs_rel):
+        p = V.VlasovPoissonParameters(VP_DIM_X, DEGREE, [VP_CELLS_X] * 2, [VP_CELLS_V] * 2, [0.0] * 2,
+                                      [two_pi] * 2, [-6.0] * 2, [6.0] * 2, dtype=dtype, cg_tol=tol, guess=guess,
+                                      cg_rhs_relative=rhs_rel)
+        return V.VlasovPoissonOperation(p)
+
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    runs = {}
+    clocks = None
+    selected = [r.strip() for r in args.vp_runs.split(",")]
+    for dtype in ("f64", "f32"):
+        for guess in ("previous", "zero", "learned"):
+            if "%s/%s" % (dtype, guess) not in selected:
+                continue
+            op = make(guess, dtype, args.vp_tol, True)
+            sol = op.initialize_dof_vector()
+            op.interpolate(f0, sol)
+            Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
+            integ = V.LowStorageRungeKuttaIntegrator(Ki, Ti, "rk45")
+            t = 0.0
+            for _ in range(args.warmup):
+                op.perform_time_step(integ, sol, t, dt)
+                t += dt
+            torch.cuda.synchronize()
+            st0 = op.cg_stats()
+            sampler = None
+            if dtype == "f64" and guess == "learned":
+                sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+                sampler.start()
+                time.sleep(0.3)
+            w0 = time.perf_counter()
+            e0.record(stream)
+            for _ in range(args.steps):
+                op.perform_time_step(integ, sol, t, dt)
+                t += dt
+            e1.record(stream)
+            torch.cuda.synchronize()
+            wall = (time.perf_counter() - w0) * 1e3 / args.steps
+            if sampler is not None:
+                clocks = sampler.stop()
+            st1 = op.cg_stats()
+            solves = st1["solves"] - st0["solves"]
+            runs["%s/%s" % (dtype, guess)] = {
+                "ms_per_step": round(e0.elapsed_time(e1) / args.steps, 4), "wall_ms_per_step": round(wall, 4),
+                "cg_iterations_per_solve": round((st1["total_iterations"] - st0["total_iterations"]) / solves, 3),
+                "learned_picked": st1["learned_picked"] - st0["learned_picked"], "solves": solves,
+                "field_energy": op.diagnostics(sol)[:VP_DIM_X]}
+            del op, sol, Ki, Ti, integ
+            torch.cuda.empty_cache()
+
+    # field energy after a few steps from f0: GPU (FP64 and FP32 storage, learned guess) vs FP64 oracle
+    energy = {}
+    if args.vp_oracle_steps > 0:
+        from oracle import oracle as O
+        prob = O.Problem(2, 2, DEGREE, [VP_CELLS_X] * 2 + [VP_CELLS_V] * 2, [0.0, 0.0, -6.0, -6.0],
+                         [two_pi, two_pi, 6.0, 6.0], [1.0, 1.0, 6.0, 6.0], collocation=True)
+        fo = O.interpolate(prob, O.vp_initial_function(2, 2, eps=0.01, k=0.5, perturbed_dims=(0, 1)))
+        st = O.VPState(prob, 1e-12)
+        c0 = time.perf_counter()
+        for s in range(args.vp_oracle_steps):
+            O.lsrk_step_op("rk45", fo, s * dt, dt, st.operator)
+        cpu_s = (time.perf_counter() - c0) / args.vp_oracle_steps
+        e_ref = np.array(st.diagnostics(fo)[:VP_DIM_X])
+        for dtype in ("f64", "f32"):
+            op = make("learned", dtype, args.vp_tol, True)
+            sol = op.initialize_dof_vector()
+            op.interpolate(f0, sol)
+            Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
+            integ = V.LowStorageRungeKuttaIntegrator(Ki, Ti, "rk45")
+            for s in range(args.vp_oracle_steps):
+                op.perform_time_step(integ, sol, s * dt, dt)
+            e = np.array(op.diagnostics(sol)[:VP_DIM_X])
+            energy[dtype] = {"field_energy": list(e), "rel_err_vs_oracle": float(np.abs(e - e_ref).max() /
+                                                                                  np.abs(e_ref).max())}
+            del op, sol, Ki, Ti, integ
+            torch.cuda.empty_cache()
+        energy["oracle"] = {"field_energy": list(e_ref), "steps": args.vp_oracle_steps}
+        cpu = {"value": round(cpu_s * 1e3, 1), "unit": "ms/step", "cores": os.cpu_count(), "kind": "port",
+               "sample": "%d rk45 steps of the full workload by the oracle (FP64, OpenMP)" % args.vp_oracle_steps}
+    else:
+        cpu = None
+
+    if rank == 0:
+        main_run = runs.get("f64/learned") or next(iter(runs.values()))
+        plain = runs.get("f64/previous")
+        n = 67108864
+        out = {"metric": "Vlasov-Poisson 2x2v k=3 step time (rk45, FP64 phase space, FP64 CG)", "value":
+               main_run["ms_per_step"], "unit": "ms/step", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+               "ms_per_step": main_run["ms_per_step"], "higher_is_better": False, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+               "config": vp_config({"cg_tolerance": "||r|| <= %g ||rhs||" % args.vp_tol, "dt": dt}),
+               "gdof_per_s": round(n * N_STAGES / (main_run["ms_per_step"] / 1e3) / 1e9, 3),
+               "plain_guess": plain, "runs": runs, "field_energy_vs_oracle": energy, "cpu_baseline": cpu,
+               "clocks": clocks}
+        print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -183,7 +316,18 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cells-x", type=int, default=CELLS,
                     help="x-cells per direction (8 = the benchmark workload; smaller only for profiling)")
+    ap.add_argument("--workload", default="advection6d", choices=["advection6d", "vp2x2v"])
+    ap.add_argument("--vp-tol", type=float, default=1e-10, help="CG: ||r|| <= tol ||rhs|| (vp2x2v)")
+    ap.add_argument("--vp-oracle-steps", type=int, default=2, help="steps compared with the FP64 oracle (vp2x2v)")
+    ap.add_argument("--vp-runs", default="f64/previous,f64/zero,f64/learned,f32/previous,f32/zero,f32/learned",
+                    help="dtype/guess combinations timed (vp2x2v)")
     args = ap.parse_args()
+    if args.workload == "vp2x2v":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the Vlasov-Poisson line is reported by the "
+                              "default arm (oracle host time in field_energy_vs_oracle)"}))
+            return 0
+        return run_vp(args)
     args.steps_cpu = 3
     args.warmup_cpu = 1
     if args.impl == "reference":

@@ -19,4 +19,8 @@ def __getattr__(name):
         import importlib
         mod = importlib.import_module(__name__ + ".advection")
         return mod if name == "advection" else getattr(mod, name)
+    if name in ("VlasovPoissonParameters", "VlasovPoissonOperation", "perturbed_maxwellian", "vlasov_poisson"):
+        import importlib
+        mod = importlib.import_module(__name__ + ".vlasov_poisson")
+        return mod if name == "vlasov_poisson" else getattr(mod, name)
     raise AttributeError(name)

@@ -21,8 +21,12 @@ EXPORTED_SYMBOLS = (
     "hd_adv_critical_time_step", "hd_interpolate", "hd_norm_and_error", "hd_lsrk_create", "hd_lsrk_destroy",
     "hd_lsrk_n_stages", "hd_lsrk_step", "hd_lsrk_step_unfused", "hd_lsrk_stage_update", "hd_lsrk_coefficients",
     "hd_adv_set_kernel", "hd_adv_kernel", "hd_adv_device_status", "hd_norm_and_error_noalloc",
+    "hd_vp_create", "hd_vp_destroy", "hd_vp_n_dofs", "hd_vp_n_dofs_x", "hd_vp_interpolate", "hd_vp_solve_field",
+    "hd_vp_apply", "hd_vp_lsrk_step", "hd_vp_diagnostics", "hd_vp_fields", "hd_vp_cg_stats", "hd_vp_set_guess",
+    "hd_vp_learn_loss_grad",
 )
 HD_KERNEL_AUTO, HD_KERNEL_GENERIC, HD_KERNEL_PIPELINED = 0, 1, 2
+HD_VP_GUESS_ZERO, HD_VP_GUESS_PREVIOUS, HD_VP_GUESS_LEARNED = 0, 1, 2
 
 
 class HdError(RuntimeError):
@@ -46,6 +50,15 @@ class hd_adv_desc(ctypes.Structure):
                 ("periodic_x", ctypes.c_int), ("periodic_v", ctypes.c_int),
                 ("velocity", ctypes.c_double * MAX_DIM), ("skew", ctypes.c_double),
                 ("bc_kind", ctypes.c_int), ("bc", hd_function)]
+
+
+class hd_vp_desc(ctypes.Structure):
+    _fields_ = [("dim_x", ctypes.c_int), ("dim_v", ctypes.c_int), ("degree", ctypes.c_int), ("dtype", ctypes.c_int),
+                ("cells_x", ctypes.c_int * 3), ("cells_v", ctypes.c_int * 3),
+                ("lo_x", ctypes.c_double * 3), ("hi_x", ctypes.c_double * 3),
+                ("lo_v", ctypes.c_double * 3), ("hi_v", ctypes.c_double * 3),
+                ("cg_tol", ctypes.c_double), ("cg_max_iter", ctypes.c_int), ("guess", ctypes.c_int),
+                ("learn_rank", ctypes.c_int), ("learn_history", ctypes.c_int), ("cg_rhs_relative", ctypes.c_int)]
 
 
 _lib = None
@@ -93,6 +106,23 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.hd_lsrk_stage_update.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_double, ctypes.c_double,
                                        vp, vp, vp, vp]
     L.hd_lsrk_coefficients.argtypes = [vp, dp, dp, dp]
+    llp = ctypes.POINTER(ctypes.c_longlong)
+    L.hd_vp_create.argtypes = [ctypes.POINTER(hd_vp_desc), ctypes.POINTER(vp)]
+    L.hd_vp_destroy.argtypes = [vp]
+    L.hd_vp_n_dofs.argtypes = [vp]
+    L.hd_vp_n_dofs.restype = ctypes.c_longlong
+    L.hd_vp_n_dofs_x.argtypes = [vp]
+    L.hd_vp_n_dofs_x.restype = ctypes.c_longlong
+    L.hd_vp_interpolate.argtypes = [vp, ctypes.POINTER(hd_function), ctypes.c_double, vp, vp]
+    L.hd_vp_solve_field.argtypes = [vp, vp, vp]
+    L.hd_vp_apply.argtypes = [vp, vp, vp, ctypes.c_double, vp]
+    L.hd_vp_lsrk_step.argtypes = [vp, vp, vp, vp, vp, ctypes.c_double, ctypes.c_double, vp]
+    L.hd_vp_diagnostics.argtypes = [vp, vp, dp, vp]
+    L.hd_vp_fields.argtypes = [vp, vp, vp, vp, vp]
+    L.hd_vp_cg_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int), llp, llp, dp, llp]
+    L.hd_vp_set_guess.argtypes = [vp, ctypes.c_int]
+    L.hd_vp_learn_loss_grad.argtypes = [ctypes.c_longlong, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp,
+                                        vp]
     _lib = L
     return L
 

@@ -1,0 +1,934 @@
+// hd_vp.cu -- Vlasov-Poisson right-hand side on the GPU and its C ABI
+// (hd_vp_* in include/hyperdeal_gb300.h).
+//
+// One evaluation (examples/vlasov_poisson/include/application.h:516-602):
+//   1. rho(x) = int f dv at the x-nodes (FP64 accumulation, fixed order)
+//   2. rhs = -M (rho - mean rho), mean removed (singular periodic problem)
+//   3. SIPG Poisson solve by conjugate gradients in FP64 from an initial
+//      guess (zero, the previous potential, or the learned model), one
+//      cooperative launch per solve
+//   4. E = grad(phi) at the x-nodes
+//   5. dst = ECL advection of src with the phase-space velocity (v, E)
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "../../include/hyperdeal_gb300.h"
+#include "hd_ecl.cuh"
+#include "hd_vp.cuh"
+#include "hd_vp_learn.cuh"
+
+namespace cgrp = cooperative_groups;
+
+namespace hd {
+
+namespace {
+
+constexpr int kMomChunk = 16;       // v-cells summed by one block of the moment kernel
+constexpr int kCgThreads = 64;   // small blocks: the x-space system is small, spread it over many SMs
+
+// ---------------------------------------------------------------- moments
+// partial[chunk][gx*NCx + ix] = sum over v-cells of the chunk and v-nodes of f * JxW_v
+template <typename T>
+__global__ void moment_partials(VpGeom g, const T* __restrict__ f, const double* __restrict__ wv,
+                                double* __restrict__ partial) {
+  extern __shared__ double sh[];
+  const long long gxc = blockIdx.x;  // x-cell
+  const int chunk = blockIdx.y;
+  const long long gv0 = (long long)chunk * kMomChunk;
+  const int NCv = g.NC / g.NCx;
+  for (int node = threadIdx.x; node < g.NC; node += blockDim.x) {
+    const int iv = node / g.NCx;
+    double acc = 0.0;
+    for (int k = 0; k < kMomChunk; ++k) {
+      const long long gv = gv0 + k;
+      if (gv >= g.ncv) break;
+      acc += double(f[(gxc + g.ncx * gv) * g.NC + node]) * wv[iv];
+    }
+    sh[node] = acc;
+  }
+  __syncthreads();
+  for (int ix = threadIdx.x; ix < g.NCx; ix += blockDim.x) {
+    double s = 0.0;
+    for (int iv = 0; iv < NCv; ++iv) s += sh[ix + g.NCx * iv];
+    partial[(long long)chunk * g.nx_dofs + gxc * g.NCx + ix] = s;
+  }
+}
+
+__global__ void moment_sum(long long nx, int nchunks, const double* __restrict__ partial, double* __restrict__ rho) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= nx) return;
+  double s = 0.0;
+  for (int c = 0; c < nchunks; ++c) s += partial[(long long)c * nx + i];
+  rho[i] = s;
+}
+
+// block-wide sum in a fixed order (all threads receive the result)
+__device__ double block_sum(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int k = 0; k < (int)(blockDim.x / 32); ++k) s += sh[k];
+  return s;
+}
+
+__device__ double x_jxw(const VpGeom& g, int ix) {
+  double j = 1.0;
+  for (int d = 0; d < g.dx; ++d) {
+    j *= g.h[d] * g.glw[ix % g.N];
+    ix /= g.N;
+  }
+  return j;
+}
+
+// rhs = -(rho - mean rho) JxW, then mean removed (single block; x-space is small)
+__global__ void poisson_rhs_kernel(VpGeom g, const double* __restrict__ rho, double* __restrict__ rhs) {
+  __shared__ double sh[32];
+  const long long n = g.nx_dofs;
+  double s = 0.0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) s += rho[i];
+  const double mean = block_sum(s, sh) / double(n);
+  double s2 = 0.0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+    const double v = -(rho[i] - mean) * x_jxw(g, int(i % g.NCx));
+    rhs[i] = v;
+    s2 += v;
+  }
+  const double mean2 = block_sum(s2, sh) / double(n);
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) rhs[i] -= mean2;
+}
+
+// ---------------------------------------------------------------- SIPG row
+// (A u)_i for x-DoF i: cell stiffness + for both faces of every direction the
+// SIPG terms sigma [u][v] - {d_n u}[v] - [u]{d_n v} at the Gauss-Lobatto face
+// points (poisson.h:131-255).  Constants are in the kernel, so the
+// reference's removal of the input mean does not change the result.
+__device__ double sipg_row(const VpGeom& g, const double* __restrict__ u, long long i) {
+  const int N = g.N;
+  const long long gx = i / g.NCx;
+  const int ix = int(i - gx * g.NCx);
+  int id[3], cc[3];
+  {
+    int t = ix;
+    long long c = gx;
+    for (int d = 0; d < g.dx; ++d) {
+      id[d] = t % N;
+      t /= N;
+      cc[d] = int(c % g.cells[d]);
+      c /= g.cells[d];
+    }
+  }
+  double val = 0.0;
+  int s = 1;
+  for (int d = 0; d < g.dx; ++d) {
+    const int base = ix - id[d] * s;
+    const long long cs = g.cstride[d];
+    const long long gL = cc[d] > 0 ? gx - cs : gx + (long long)(g.cells[d] - 1) * cs;
+    const long long gR = cc[d] + 1 < g.cells[d] ? gx + cs : gx - (long long)(g.cells[d] - 1) * cs;
+    double L[kMaxN], Lf[kMaxN], R[kMaxN];
+    for (int j = 0; j < N; ++j) {
+      L[j] = u[gx * g.NCx + base + j * s];
+      Lf[j] = u[gL * g.NCx + base + j * s];
+      R[j] = u[gR * g.NCx + base + j * s];
+    }
+    double wface = 1.0;
+    for (int e = 0; e < g.dx; ++e)
+      if (e != d) wface *= g.h[e] * g.glw[id[e]];
+    const double h = g.h[d];
+    double vol = 0.0;
+    for (int j = 0; j < N; ++j) vol += g.K1[id[d] * N + j] * L[j];
+    val += wface / h * vol;
+    const double sigma = (1.0 / h + 1.0 / h) * g.pen;
+    double dLk = 0.0, dR0 = 0.0, dLfk = 0.0, dL0 = 0.0;
+    for (int j = 0; j < N; ++j) {
+      dLk += g.Dm[(N - 1) * N + j] * L[j];
+      dR0 += g.Dm[j] * R[j];
+      dLfk += g.Dm[(N - 1) * N + j] * Lf[j];
+      dL0 += g.Dm[j] * L[j];
+    }
+    {  // right face: this cell is the minus side
+      const double jump = L[N - 1] - R[0], avg = 0.5 * (dLk + dR0) / h;
+      const double vt = (sigma * jump - avg) * wface, nt = -0.5 * jump * wface;
+      val += (id[d] == N - 1 ? vt : 0.0) + g.Dm[(N - 1) * N + id[d]] / h * nt;
+    }
+    {  // left face: this cell is the plus side
+      const double jump = Lf[N - 1] - L[0], avg = 0.5 * (dLfk + dL0) / h;
+      const double vt = (sigma * jump - avg) * wface, nt = -0.5 * jump * wface;
+      val += (id[d] == 0 ? -vt : 0.0) + g.Dm[id[d]] / h * nt;
+    }
+    s *= N;
+  }
+  return val;
+}
+
+struct CgArgs {
+  VpGeom g;
+  const double* rhs;
+  double* x;
+  double* r;
+  double* p;
+  double* Ap;
+  double* red;  // [2][gridDim] partial sums
+  double rel_tol;
+  int rhs_relative;  // 1: stop at ||r|| <= rel_tol ||rhs||; 0: at rel_tol ||r_0||
+  int max_iter;
+  int* iters;   // out: iterations
+  double* res;  // out: final / initial residual
+};
+
+__device__ double grid_sum(cgrp::grid_group& grid, double v, double* red, int slot, double* sh) {
+  const double b = block_sum(v, sh);
+  if (threadIdx.x == 0) red[slot * gridDim.x + blockIdx.x] = b;
+  grid.sync();
+  double s = 0.0;
+  for (int k = 0; k < (int)gridDim.x; ++k) s += red[slot * gridDim.x + k];
+  return s;
+}
+
+// conjugate gradients on the SIPG system, all iterations in one cooperative launch
+__global__ void __launch_bounds__(kCgThreads) cg_kernel(CgArgs A) {
+  cgrp::grid_group grid = cgrp::this_grid();
+  __shared__ double sh[32];
+  const long long n = A.g.nx_dofs;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x, stride = (long long)gridDim.x * blockDim.x;
+  double lrr = 0.0, lbb = 0.0;
+  for (long long i = t0; i < n; i += stride) {
+    const double ri = A.rhs[i] - sipg_row(A.g, A.x, i);
+    A.r[i] = ri;
+    A.p[i] = ri;
+    lrr += ri * ri;
+    lbb += A.rhs[i] * A.rhs[i];
+  }
+  double rr = grid_sum(grid, lrr, A.red, 0, sh);
+  const double bb = grid_sum(grid, lbb, A.red, 1, sh);
+  const double r0 = sqrt(rr);
+  const double stop = A.rhs_relative ? A.rel_tol * sqrt(bb) : fmax(A.rel_tol * r0, 1e-14 * sqrt(bb));
+  int it = 0;
+  while (sqrt(rr) > stop && it < A.max_iter) {
+    double lpap = 0.0;
+    for (long long i = t0; i < n; i += stride) {
+      const double a = sipg_row(A.g, A.p, i);
+      A.Ap[i] = a;
+      lpap += A.p[i] * a;
+    }
+    const double pap = grid_sum(grid, lpap, A.red, it & 1, sh);
+    if (!(pap > 0.0)) break;
+    const double alpha = rr / pap;
+    double lrn = 0.0;
+    for (long long i = t0; i < n; i += stride) {
+      A.x[i] += alpha * A.p[i];
+      const double ri = A.r[i] - alpha * A.Ap[i];
+      A.r[i] = ri;
+      lrn += ri * ri;
+    }
+    const double rn = grid_sum(grid, lrn, A.red, (it + 1) & 1, sh);
+    const double beta = rn / rr;
+    for (long long i = t0; i < n; i += stride) A.p[i] = A.r[i] + beta * A.p[i];
+    rr = rn;
+    ++it;
+    grid.sync();  // p complete before the next product
+  }
+  if (t0 == 0) {
+    *A.iters = it;
+    *A.res = r0 > 0.0 ? sqrt(rr) / r0 : 0.0;
+  }
+}
+
+// c = a - b (b == nullptr: c = a)
+__global__ void diff_kernel(long long n, const double* __restrict__ a, const double* __restrict__ b,
+                            double* __restrict__ c) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) c[i] = b ? a[i] - b[i] : a[i];
+}
+
+// y += x
+__global__ void add_kernel(long long n, const double* __restrict__ x, double* __restrict__ y) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) y[i] += x[i];
+}
+
+// per-block partial sums of ||rhs - A u||^2 for two candidate vectors u0, u1
+__global__ void residual_partials(VpGeom g, const double* __restrict__ rhs, const double* __restrict__ u0,
+                                  const double* __restrict__ u1, double* __restrict__ partial) {
+  __shared__ double sh[32];
+  double a = 0.0, b = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < g.nx_dofs;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double r0 = rhs[i] - sipg_row(g, u0, i), r1 = rhs[i] - sipg_row(g, u1, i);
+    a += r0 * r0;
+    b += r1 * r1;
+  }
+  a = block_sum(a, sh);
+  b = block_sum(b, sh);
+  if (threadIdx.x == 0) {
+    partial[2 * blockIdx.x] = a;
+    partial[2 * blockIdx.x + 1] = b;
+  }
+}
+
+// the judge: the candidate with the smaller initial residual starts CG
+// (u1 is copied over u0 when it wins; flag[0] = 1 then)
+__global__ void choose_guess(long long n, int nblocks, const double* __restrict__ partial, double* __restrict__ u0,
+                             const double* __restrict__ u1, int* __restrict__ flag) {
+  __shared__ int pick;
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < nblocks; ++k) {
+      a += partial[2 * k];
+      b += partial[2 * k + 1];
+    }
+    pick = b < a ? 1 : 0;
+    *flag = pick;
+  }
+  __syncthreads();
+  if (pick)
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) u0[i] = u1[i];
+}
+
+// E[(gx*NCx + ix)*dx + d] = d/dx_d phi at the x-node
+__global__ void field_kernel(VpGeom g, const double* __restrict__ phi, double* __restrict__ E) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= g.nx_dofs) return;
+  const int N = g.N;
+  const long long gx = i / g.NCx;
+  const int ix = int(i - gx * g.NCx);
+  int s = 1;
+  for (int d = 0; d < g.dx; ++d) {
+    const int idd = (ix / s) % N;
+    const int base = ix - idd * s;
+    double a = 0.0;
+    for (int j = 0; j < N; ++j) a += g.Dm[idd * N + j] * phi[gx * g.NCx + base + j * s];
+    E[i * g.dx + d] = a / g.h[d];
+    s *= N;
+  }
+}
+
+// es[i*dx + d] = E[i*dx + d] / h_{v_d} in the storage precision (advection input)
+template <typename T>
+__global__ void scale_field_kernel(VpGeom g, const double* __restrict__ E, T* __restrict__ es) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= g.nx_dofs * g.dx) return;
+  es[i] = T(E[i] / g.h[g.dx + int(i % g.dx)]);
+}
+
+// ---------------------------------------------------------------- diagnostics
+// block partials of mass, f^2, |v|^2 f, v_d f (3 + dv values) over cells
+template <typename T>
+__global__ void phase_diag_kernel(VpGeom g, const T* __restrict__ f, double* __restrict__ partial) {
+  __shared__ double sh[32];
+  const int dv = g.D - g.dx;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (long long gid = blockIdx.x; gid < g.n_cells; gid += gridDim.x) {
+    int cc[kMaxDim];
+    long long a = gid % g.ncx, b = gid / g.ncx;
+    for (int d = 0; d < g.D; ++d) {
+      if (d < g.dx) { cc[d] = int(a % g.cells[d]); a /= g.cells[d]; }
+      else { cc[d] = int(b % g.cells[d]); b /= g.cells[d]; }
+    }
+    for (int node = threadIdx.x; node < g.NC; node += blockDim.x) {
+      const double fv = double(f[gid * g.NC + node]);
+      double jxw = 1.0, vv = 0.0, vel[3] = {0, 0, 0};
+      int t = node;
+      for (int d = 0; d < g.D; ++d) {
+        const int id = t % g.N;
+        t /= g.N;
+        jxw *= g.h[d] * g.glw[id];
+        if (d >= g.dx) {
+          vel[d - g.dx] = g.lo[d] + (cc[d] + g.gl[id]) * g.h[d];
+          vv += vel[d - g.dx] * vel[d - g.dx];
+        }
+      }
+      acc[0] += fv * jxw;
+      acc[1] += fv * fv * jxw;
+      acc[2] += vv * fv * jxw;
+      for (int d = 0; d < dv; ++d) acc[3 + d] += vel[d] * fv * jxw;
+    }
+  }
+  for (int k = 0; k < 3 + dv; ++k) {
+    const double s = block_sum(acc[k], sh);
+    if (threadIdx.x == 0) partial[blockIdx.x * 6 + k] = s;
+  }
+}
+
+__global__ void energy_kernel(VpGeom g, const double* __restrict__ E, double* __restrict__ out) {
+  __shared__ double sh[32];
+  for (int d = 0; d < g.dx; ++d) {
+    double s = 0.0;
+    for (long long i = threadIdx.x; i < g.nx_dofs; i += blockDim.x) {
+      const double e = E[i * g.dx + d];
+      s += e * e * x_jxw(g, int(i % g.NCx));
+    }
+    const double t = block_sum(s, sh);
+    if (threadIdx.x == 0) out[d] = t;
+  }
+}
+
+__global__ void diag_finish(int nblocks, int nq, const double* __restrict__ partial, double* __restrict__ out) {
+  if (threadIdx.x != 0) return;
+  for (int k = 0; k < nq; ++k) {
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += partial[b * 6 + k];
+    out[k] = s;
+  }
+  out[1] = sqrt(out[1]);
+}
+
+// kind 3: (1 + amp prod_{cosine[d]==1} cos(omega_d x_d + phase_d)) prod_{cosine[d]==2} exp(-x_d^2/2)/sqrt(2 pi),
+// the perturbed Maxwellian of examples/vlasov_poisson/cases/hyperrectangle.h:45-58; kinds 0-2 as the operator's
+__device__ double vp_eval_function(const DevFunction& f, const double* x, int D, double t) {
+  if (f.kind != 3) return eval_function(f, x, D, t);
+  double pert = f.amp, r = 1.0;
+  for (int d = 0; d < D; ++d)
+    if (f.cosine[d] == 1) pert *= cos(f.omega[d] * x[d] + f.phase[d]);
+  r += pert;
+  for (int d = 0; d < D; ++d)
+    if (f.cosine[d] == 2) r = r * exp(-0.5 * x[d] * x[d]) / sqrt(2.0 * 3.14159265358979323846);
+  return r;
+}
+
+// function values: interpolation of an analytic function at the nodes (kind 0-3)
+template <typename T>
+__global__ void vp_interpolate_kernel(VpGeom g, DevFunction f, double t, T* __restrict__ dst) {
+  for (long long gid = blockIdx.x; gid < g.n_cells; gid += gridDim.x) {
+    int cc[kMaxDim];
+    long long a = gid % g.ncx, b = gid / g.ncx;
+    for (int d = 0; d < g.D; ++d) {
+      if (d < g.dx) { cc[d] = int(a % g.cells[d]); a /= g.cells[d]; }
+      else { cc[d] = int(b % g.cells[d]); b /= g.cells[d]; }
+    }
+    for (int node = threadIdx.x; node < g.NC; node += blockDim.x) {
+      double x[kMaxDim];
+      int tt = node;
+      for (int d = 0; d < g.D; ++d) {
+        x[d] = g.lo[d] + (cc[d] + g.gl[tt % g.N]) * g.h[d];
+        tt /= g.N;
+      }
+      dst[gid * g.NC + node] = T(vp_eval_function(f, x, g.D, t));
+    }
+  }
+}
+
+}  // namespace
+
+}  // namespace hd
+
+// ------------------------------------------------------------------ handle
+struct hd_vp {
+  hd_vp_desc desc;
+  hd::VpGeom g;
+  int dtype;
+  double* d_wv;       // v-node weights (NCv)
+  double* d_partial;  // moment partials (nchunks * nx)
+  int nchunks;
+  double* d_rho;
+  double* d_rhs;
+  double* d_phi;
+  double* d_E;
+  void* d_xs;         // x-line velocities / h_x in the storage precision
+  void* d_es;         // E / h_v in the storage precision
+  double* d_cg;       // r, p, Ap (3 * nx) + reductions (2 * cg_grid) + residual
+  int* d_iters;
+  double* d_diag;     // phase-space partials (blocks * 6) + outputs
+  double* d_guess;    // learned prediction (nx)
+  double* d_rho_prev; // rho and phi of the previous solve (the learned model
+  double* d_phi_prev; //   maps rho - rho_prev to phi - phi_prev)
+  double* d_dx;       // rho - rho_prev
+  double* d_dy;       // phi - phi_prev
+  bool have_prev;
+  double* d_judge;    // residual partials of the judge
+  int* d_pick;        // 1 when the learned guess started CG
+  long long learned_picked;
+  int cg_grid;
+  int guess;
+  int last_iters;
+  long long total_iters, solves;
+  double last_res;
+  hd::VpModel* model;  // learned initial guess
+};
+
+namespace {
+
+int vfail(int code, const char* msg) {
+  hd::set_last_error(msg);
+  return code;
+}
+
+int vcuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return HD_OK;
+  char buf[256];
+  std::snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+  hd::set_last_error(buf);
+  return HD_ERR_CUDA;
+}
+
+// 1D tables on [0,1] from the Gauss-Lobatto rule (same construction as the operator's)
+void vp_tables(int n, double* x, double* w, double* D) {
+  const int m = n - 1;
+  auto legendre = [](int nn, double z, double* p, double* dp) {
+    double p0 = 1.0, p1 = z;
+    for (int k = 2; k <= nn; ++k) {
+      const double pk = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+      p0 = p1;
+      p1 = pk;
+    }
+    *p = p1;
+    *dp = nn * (p0 - z * p1) / (1.0 - z * z);
+  };
+  x[0] = 0.0;
+  x[n - 1] = 1.0;
+  for (int i = 1; i < m; ++i) {
+    double z = -std::cos(M_PI * i / m);
+    for (int it = 0; it < 100; ++it) {
+      double p, dp;
+      legendre(m, z, &p, &dp);
+      const double dz = dp / ((2.0 * z * dp - m * (m + 1.0) * p) / (1.0 - z * z));
+      z -= dz;
+      if (std::fabs(dz) < 1e-17) break;
+    }
+    x[i] = 0.5 * (1.0 + z);
+  }
+  for (int i = 0; i < n; ++i) {
+    double p = 1.0, dp;
+    if (i == 0) p = (m % 2) ? -1.0 : 1.0;
+    else if (i < n - 1) legendre(m, 2.0 * x[i] - 1.0, &p, &dp);
+    w[i] = 1.0 / (m * (m + 1.0) * p * p);
+  }
+  for (int i = 0; i < n / 2; ++i) {
+    const double xs = 0.5 * (x[i] + (1.0 - x[n - 1 - i])), ws = 0.5 * (w[i] + w[n - 1 - i]);
+    x[i] = xs;
+    x[n - 1 - i] = 1.0 - xs;
+    w[i] = ws;
+    w[n - 1 - i] = ws;
+  }
+  if (n % 2) x[n / 2] = 0.5;
+  for (int q = 0; q < n; ++q)
+    for (int j = 0; j < n; ++j) {
+      double s = 0.0;
+      for (int l = 0; l < n; ++l) {
+        if (l == j) continue;
+        double t = 1.0 / (x[j] - x[l]);
+        for (int mm = 0; mm < n; ++mm)
+          if (mm != j && mm != l) t *= (x[q] - x[mm]) / (x[j] - x[mm]);
+        s += t;
+      }
+      D[q * n + j] = s;
+    }
+}
+
+void vp_free(hd_vp* v) {
+  if (!v) return;
+  cudaFree(v->d_wv);
+  cudaFree(v->d_partial);
+  cudaFree(v->d_rho);
+  cudaFree(v->d_rhs);
+  cudaFree(v->d_phi);
+  cudaFree(v->d_E);
+  cudaFree(v->d_xs);
+  cudaFree(v->d_es);
+  cudaFree(v->d_cg);
+  cudaFree(v->d_iters);
+  cudaFree(v->d_diag);
+  cudaFree(v->d_guess);
+  cudaFree(v->d_rho_prev);
+  cudaFree(v->d_phi_prev);
+  cudaFree(v->d_dx);
+  cudaFree(v->d_dy);
+  cudaFree(v->d_judge);
+  cudaFree(v->d_pick);
+  hd::vp_model_destroy(v->model);
+  delete v;
+}
+
+int solve_poisson(hd_vp* v, cudaStream_t s) {
+  hd::VpGeom& g = v->g;
+  const long long nx = g.nx_dofs;
+  // initial guess
+  if (v->guess == HD_VP_GUESS_ZERO) {
+    int rc = vcuda(cudaMemsetAsync(v->d_phi, 0, sizeof(double) * nx, s), "zero guess");
+    if (rc) return rc;
+  }
+  // learned: the solution map is linear, so the model is trained on and
+  // applied to differences to the previous solve: guess = phi_prev +
+  // model(rho - rho_prev), judged against phi_prev by the initial residual
+  // (without a previous solve both differences are taken from zero)
+  const bool learned = v->guess == HD_VP_GUESS_LEARNED && v->model;
+  const unsigned nb = unsigned((nx + 255) / 256);
+  bool judged = false;
+  if (learned) {
+    int rc;
+    if (v->have_prev) {
+      rc = vcuda(cudaMemcpyAsync(v->d_phi_prev, v->d_phi, sizeof(double) * nx, cudaMemcpyDeviceToDevice, s),
+                 "previous potential");
+    } else {
+      rc = vcuda(cudaMemsetAsync(v->d_phi_prev, 0, sizeof(double) * nx, s), "previous potential");
+      if (!rc) rc = vcuda(cudaMemsetAsync(v->d_rho_prev, 0, sizeof(double) * nx, s), "previous density");
+    }
+    if (rc) return rc;
+    hd::diff_kernel<<<nb, 256, 0, s>>>(nx, v->d_rho, v->d_rho_prev, v->d_dx);
+    if (hd::vp_model_ready(v->model)) {
+      rc = vcuda(hd::vp_model_predict(v->model, v->d_dx, v->d_guess, s), "learned guess");
+      if (rc) return rc;
+      hd::add_kernel<<<nb, 256, 0, s>>>(nx, v->d_phi_prev, v->d_guess);
+      constexpr int kJudgeBlocks = 64;
+      hd::residual_partials<<<kJudgeBlocks, 256, 0, s>>>(g, v->d_rhs, v->d_phi, v->d_guess, v->d_judge);
+      hd::choose_guess<<<1, 1024, 0, s>>>(nx, kJudgeBlocks, v->d_judge, v->d_phi, v->d_guess, v->d_pick);
+      judged = true;
+    }
+    rc = vcuda(cudaGetLastError(), "learned guess");
+    if (rc) return rc;
+  }
+  hd::CgArgs A;
+  A.g = g;
+  A.rhs = v->d_rhs;
+  A.x = v->d_phi;
+  A.r = v->d_cg;
+  A.p = v->d_cg + nx;
+  A.Ap = v->d_cg + 2 * nx;
+  A.red = v->d_cg + 3 * nx;
+  A.rel_tol = v->desc.cg_tol;
+  A.rhs_relative = v->desc.cg_rhs_relative;
+  A.max_iter = v->desc.cg_max_iter;
+  A.iters = v->d_iters;
+  A.res = v->d_cg + 3 * nx + 2 * v->cg_grid;
+  void* args[] = {&A};
+  int rc = vcuda(cudaLaunchCooperativeKernel((void*)hd::cg_kernel, dim3(v->cg_grid), dim3(hd::kCgThreads), args, 0, s),
+                 "CG launch");
+  if (rc) return rc;
+  // the solver's own (rho - rho_prev, phi - phi_prev) pair trains the learned guess
+  if (learned) {
+    hd::diff_kernel<<<nb, 256, 0, s>>>(nx, v->d_phi, v->d_phi_prev, v->d_dy);
+    rc = vcuda(hd::vp_model_observe(v->model, v->d_dx, v->d_dy, s), "learned guess update");
+    if (!rc) rc = vcuda(cudaMemcpyAsync(v->d_rho_prev, v->d_rho, sizeof(double) * nx, cudaMemcpyDeviceToDevice, s),
+                        "previous density");
+    if (rc) return rc;
+    v->have_prev = true;
+  }
+  int it = 0;
+  double res = 0.0;
+  rc = vcuda(cudaMemcpyAsync(&it, v->d_iters, sizeof(int), cudaMemcpyDeviceToHost, s), "CG iterations");
+  if (rc) return rc;
+  rc = vcuda(cudaMemcpyAsync(&res, A.res, sizeof(double), cudaMemcpyDeviceToHost, s), "CG residual");
+  if (rc) return rc;
+  int pick = 0;
+  if (judged) {
+    rc = vcuda(cudaMemcpyAsync(&pick, v->d_pick, sizeof(int), cudaMemcpyDeviceToHost, s), "judge flag");
+    if (rc) return rc;
+  }
+  rc = vcuda(cudaStreamSynchronize(s), "CG synchronize");
+  if (rc) return rc;
+  v->learned_picked += pick;
+  v->last_iters = it;
+  v->last_res = res;
+  v->total_iters += it;
+  v->solves += 1;
+  return HD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
+  if (!desc || !out) return vfail(HD_ERR_INVALID, "hd_vp_create: null argument");
+  *out = nullptr;
+  const hd_vp_desc& d = *desc;
+  if (d.dim_x < 1 || d.dim_x > 3 || d.dim_v != d.dim_x)
+    return vfail(HD_ERR_INVALID, "hd_vp_create: dim_v must equal dim_x (1..3)");
+  if (d.degree < 1 || d.degree + 1 > hd::kMaxN) return vfail(HD_ERR_UNSUPPORTED, "hd_vp_create: degree 1..5");
+  if (d.dtype != HD_F64 && d.dtype != HD_F32) return vfail(HD_ERR_INVALID, "hd_vp_create: unknown dtype");
+  if (!(d.cg_tol > 0.0) || d.cg_max_iter < 1) return vfail(HD_ERR_INVALID, "hd_vp_create: cg_tol > 0, cg_max_iter >= 1");
+  if (d.guess < HD_VP_GUESS_ZERO || d.guess > HD_VP_GUESS_LEARNED)
+    return vfail(HD_ERR_INVALID, "hd_vp_create: unknown guess");
+  hd_vp* v = new (std::nothrow) hd_vp;
+  if (!v) return vfail(HD_ERR_ALLOC, "out of host memory");
+  std::memset(v, 0, sizeof(*v));
+  v->desc = d;
+  v->dtype = d.dtype;
+  v->guess = d.guess;
+  hd::VpGeom& g = v->g;
+  g.dx = d.dim_x;
+  g.D = 2 * d.dim_x;
+  g.N = d.degree + 1;
+  g.NCx = hd::ipow(g.N, g.dx);
+  g.NC = hd::ipow(g.N, g.D);
+  g.ncx = 1;
+  g.ncv = 1;
+  long long st = 1;
+  for (int i = 0; i < g.D; ++i) {
+    const bool isx = i < g.dx;
+    const int c = isx ? d.cells_x[i] : d.cells_v[i - g.dx];
+    const double lo = isx ? d.lo_x[i] : d.lo_v[i - g.dx];
+    const double hi = isx ? d.hi_x[i] : d.hi_v[i - g.dx];
+    if (c < 1 || !(hi > lo)) { delete v; return vfail(HD_ERR_INVALID, "hd_vp_create: bad mesh"); }
+    g.cells[i] = c;
+    g.lo[i] = lo;
+    g.h[i] = (hi - lo) / c;
+    g.cstride[i] = st;
+    st *= c;
+    if (isx) g.ncx *= c;
+    else g.ncv *= c;
+  }
+  g.cstride[g.D] = st;
+  g.n_cells = st;
+  g.nx_dofs = g.ncx * g.NCx;
+  vp_tables(g.N, g.gl, g.glw, g.Dm);
+  const int N = g.N;
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j) {
+      double k = 0.0;
+      for (int q = 0; q < N; ++q) k += g.Dm[q * N + i] * g.glw[q] * g.Dm[q * N + j];
+      g.K1[i * N + j] = k;
+      g.G[i * N + j] = g.Dm[j * N + i] * g.glw[j] / g.glw[i];
+    }
+  g.pen = double(d.degree > 1 ? d.degree : 1) * (d.degree + 1.0);
+  // the advection kernel keeps two copies of CTA's cells in shared memory: 3x+3v up to degree 3
+  if (g.D == 6 && N > 4) { delete v; return vfail(HD_ERR_UNSUPPORTED, "hd_vp_create: 3x+3v only for degree <= 3"); }
+  for (int i = 0; i < g.dx; ++i)
+    if (d.cells_v[i] > 64) { delete v; return vfail(HD_ERR_UNSUPPORTED, "hd_vp_create: at most 64 v-cells per direction"); }
+  // device buffers
+  const int NCv = g.NC / g.NCx;
+  v->nchunks = int((g.ncv + hd::kMomChunk - 1) / hd::kMomChunk);
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hd::cg_kernel, hd::kCgThreads, 0);
+  long long want = (g.nx_dofs + hd::kCgThreads - 1) / hd::kCgThreads;
+  long long cap = (long long)sms * (per_sm > 0 ? per_sm : 1);
+  v->cg_grid = int(want < cap ? want : cap);
+  if (v->cg_grid < 1) v->cg_grid = 1;
+  const long long nx = g.nx_dofs;
+  cudaError_t e = cudaSuccess;
+  auto alloc = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+  };
+  alloc((void**)&v->d_wv, sizeof(double) * NCv);
+  alloc((void**)&v->d_partial, sizeof(double) * size_t(v->nchunks) * nx);
+  alloc((void**)&v->d_rho, sizeof(double) * nx);
+  alloc((void**)&v->d_rhs, sizeof(double) * nx);
+  alloc((void**)&v->d_phi, sizeof(double) * nx);
+  alloc((void**)&v->d_E, sizeof(double) * nx * g.dx);
+  alloc(&v->d_es, sizeof(double) * nx * g.dx);
+  alloc(&v->d_xs, sizeof(double) * g.dx * 64 * hd::kMaxN);
+  alloc((void**)&v->d_cg, sizeof(double) * (3 * nx + 2 * v->cg_grid + 1));
+  alloc((void**)&v->d_iters, sizeof(int));
+  alloc((void**)&v->d_diag, sizeof(double) * (152 * 16 * 6 + 16));
+  alloc((void**)&v->d_guess, sizeof(double) * nx);
+  alloc((void**)&v->d_rho_prev, sizeof(double) * nx);
+  alloc((void**)&v->d_phi_prev, sizeof(double) * nx);
+  alloc((void**)&v->d_dx, sizeof(double) * nx);
+  alloc((void**)&v->d_dy, sizeof(double) * nx);
+  alloc((void**)&v->d_judge, sizeof(double) * 2 * 64);
+  alloc((void**)&v->d_pick, sizeof(int));
+  if (e != cudaSuccess) { vp_free(v); return vcuda(e, "hd_vp_create: cudaMalloc"); }
+  {
+    double wv[4096];
+    if (NCv > 4096) { vp_free(v); return vfail(HD_ERR_UNSUPPORTED, "hd_vp_create: v-cell too large"); }
+    double jv = 1.0;
+    for (int d2 = g.dx; d2 < g.D; ++d2) jv *= g.h[d2];
+    for (int iv = 0; iv < NCv; ++iv) {
+      double w = jv;
+      int t = iv;
+      for (int d2 = 0; d2 < g.dx; ++d2) { w *= g.glw[t % N]; t /= N; }
+      wv[iv] = w;
+    }
+    e = cudaMemcpy(v->d_wv, wv, sizeof(double) * NCv, cudaMemcpyHostToDevice);
+    // x-line velocity tables: v-coordinate of node i of v-cell c along v-direction dx + d, over h_{x_d}
+    {
+      double xs64[3 * 64 * hd::kMaxN];
+      float xs32[3 * 64 * hd::kMaxN];
+      int k = 0;
+      for (int d2 = 0; d2 < g.dx; ++d2) {
+        const int e2 = g.dx + d2;
+        for (int c = 0; c < g.cells[e2]; ++c)
+          for (int i = 0; i < N; ++i, ++k) {
+            xs64[k] = (g.lo[e2] + (c + g.gl[i]) * g.h[e2]) / g.h[d2];
+            xs32[k] = float(xs64[k]);
+          }
+      }
+      if (e == cudaSuccess)
+        e = cudaMemcpy(v->d_xs, d.dtype == HD_F64 ? (const void*)xs64 : (const void*)xs32,
+                       size_t(k) * (d.dtype == HD_F64 ? 8 : 4), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) e = cudaMemset(v->d_es, 0, sizeof(double) * nx * g.dx);
+    if (e == cudaSuccess) e = cudaMemset(v->d_phi, 0, sizeof(double) * nx);
+    if (e == cudaSuccess) e = cudaMemset(v->d_E, 0, sizeof(double) * nx * g.dx);
+    if (e != cudaSuccess) { vp_free(v); return vcuda(e, "hd_vp_create: init"); }
+  }
+  if (d.guess == HD_VP_GUESS_LEARNED) {
+    v->model = hd::vp_model_create(nx, d.learn_rank > 0 ? d.learn_rank : 32, d.learn_history > 0 ? d.learn_history : 64);
+    if (!v->model) { vp_free(v); return vfail(HD_ERR_ALLOC, "hd_vp_create: learned-guess model"); }
+  }
+  *out = v;
+  return HD_OK;
+}
+
+int hd_vp_destroy(hd_vp* v) {
+  vp_free(v);
+  return HD_OK;
+}
+
+long long hd_vp_n_dofs(const hd_vp* v) { return v ? v->g.n_cells * v->g.NC : -1; }
+long long hd_vp_n_dofs_x(const hd_vp* v) { return v ? v->g.nx_dofs : -1; }
+
+int hd_vp_interpolate(hd_vp* v, const hd_function* f, double time, void* dst, void* stream) {
+  if (!v || !f || !dst) return vfail(HD_ERR_INVALID, "hd_vp_interpolate: null argument");
+  if (f->kind < 0 || f->kind > 3) return vfail(HD_ERR_INVALID, "hd_vp_interpolate: unknown function kind");
+  hd::DevFunction df;
+  std::memset(&df, 0, sizeof(df));
+  df.kind = f->kind;
+  df.amp = f->amp;
+  for (int i = 0; i < HD_MAX_DIM; ++i) {
+    df.omega[i] = f->omega[i];
+    df.speed[i] = f->speed[i];
+    df.phase[i] = f->phase[i];
+    df.cosine[i] = f->cosine[i];
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned grid = unsigned(v->g.n_cells < 152 * 32 ? v->g.n_cells : 152 * 32);
+  if (v->dtype == HD_F32) hd::vp_interpolate_kernel<float><<<grid, 256, 0, s>>>(v->g, df, time, (float*)dst);
+  else hd::vp_interpolate_kernel<double><<<grid, 256, 0, s>>>(v->g, df, time, (double*)dst);
+  return vcuda(cudaGetLastError(), "vp interpolate");
+}
+
+int hd_vp_solve_field(hd_vp* v, const void* f, void* stream) {
+  if (!v || !f) return vfail(HD_ERR_INVALID, "hd_vp_solve_field: null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  hd::VpGeom& g = v->g;
+  const dim3 grid(unsigned(g.ncx), unsigned(v->nchunks));
+  const int threads = g.NC >= 256 ? 256 : ((g.NC + 31) / 32) * 32;
+  const size_t sh = sizeof(double) * g.NC;
+  if (v->dtype == HD_F32) hd::moment_partials<float><<<grid, threads, sh, s>>>(g, (const float*)f, v->d_wv, v->d_partial);
+  else hd::moment_partials<double><<<grid, threads, sh, s>>>(g, (const double*)f, v->d_wv, v->d_partial);
+  hd::moment_sum<<<unsigned((g.nx_dofs + 255) / 256), 256, 0, s>>>(g.nx_dofs, v->nchunks, v->d_partial, v->d_rho);
+  hd::poisson_rhs_kernel<<<1, 1024, 0, s>>>(g, v->d_rho, v->d_rhs);
+  int rc = vcuda(cudaGetLastError(), "vp moments / rhs");
+  if (rc) return rc;
+  rc = solve_poisson(v, s);
+  if (rc) return rc;
+  hd::field_kernel<<<unsigned((g.nx_dofs + 255) / 256), 256, 0, s>>>(g, v->d_phi, v->d_E);
+  const unsigned ne = unsigned((g.nx_dofs * g.dx + 255) / 256);
+  if (v->dtype == HD_F32) hd::scale_field_kernel<float><<<ne, 256, 0, s>>>(g, v->d_E, (float*)v->d_es);
+  else hd::scale_field_kernel<double><<<ne, 256, 0, s>>>(g, v->d_E, (double*)v->d_es);
+  return vcuda(cudaGetLastError(), "vp field");
+}
+
+int hd_vp_apply(hd_vp* v, void* dst, const void* src, double time, void* stream) {
+  (void)time;
+  if (!v || !dst || !src) return vfail(HD_ERR_INVALID, "hd_vp_apply: null argument");
+  if (dst == src) return vfail(HD_ERR_INVALID, "hd_vp_apply: dst and src must differ");
+  int rc = hd_vp_solve_field(v, src, stream);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e;
+  if (v->dtype == HD_F32) {
+    hd::VpAdvParams<float> P{(const float*)src, (float*)dst, (const float*)v->d_xs, (const float*)v->d_es, v->g};
+    e = hd::launch_vp_advection(P, s);
+  } else {
+    hd::VpAdvParams<double> P{(const double*)src, (double*)dst, (const double*)v->d_xs, (const double*)v->d_es,
+                              v->g};
+    e = hd::launch_vp_advection(P, s);
+  }
+  return vcuda(e, "vp advection");
+}
+
+int hd_vp_lsrk_step(hd_vp* v, const hd_lsrk* rk, void* sol, void* Ki, void* Ti, double time, double dt, void* stream) {
+  if (!v || !rk || !sol || !Ki || !Ti) return vfail(HD_ERR_INVALID, "hd_vp_lsrk_step: null argument");
+  const int ns = hd_lsrk_n_stages(rk);
+  double ai[16], bi[16], ci[16];
+  int rc = hd_lsrk_coefficients(rk, ai, bi, ci);
+  if (rc) return rc;
+  const long long n = hd_vp_n_dofs(v);
+  cudaStream_t s = (cudaStream_t)stream;
+  rc = vcuda(cudaMemcpyAsync(Ti, sol, size_t(n) * (v->dtype == HD_F64 ? 8 : 4), cudaMemcpyDeviceToDevice, s),
+             "copy sol -> Ti");
+  if (rc) return rc;
+  for (int st = 0; st < ns; ++st) {
+    rc = hd_vp_apply(v, Ki, Ti, time + ci[st] * dt, stream);
+    if (rc) return rc;
+    rc = hd_lsrk_stage_update(v->dtype, n, bi[st] * dt, st == ns - 1 ? 0.0 : ai[st] * dt, Ki, sol, Ti, stream);
+    if (rc) return rc;
+  }
+  return HD_OK;
+}
+
+int hd_vp_diagnostics(hd_vp* v, const void* f, double* out, void* stream) {
+  if (!v || !f || !out) return vfail(HD_ERR_INVALID, "hd_vp_diagnostics: null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  hd::VpGeom& g = v->g;
+  const int blocks = 152 * 16, dv = g.D - g.dx;
+  double* part = v->d_diag;
+  double* res = v->d_diag + blocks * 6;
+  if (v->dtype == HD_F32) hd::phase_diag_kernel<float><<<blocks, 256, 0, s>>>(g, (const float*)f, part);
+  else hd::phase_diag_kernel<double><<<blocks, 256, 0, s>>>(g, (const double*)f, part);
+  hd::diag_finish<<<1, 32, 0, s>>>(blocks, 3 + dv, part, res);
+  hd::energy_kernel<<<1, 1024, 0, s>>>(g, v->d_E, res + 8);
+  int rc = vcuda(cudaGetLastError(), "vp diagnostics");
+  if (rc) return rc;
+  double h[16];
+  rc = vcuda(cudaMemcpyAsync(h, res, sizeof(double) * 16, cudaMemcpyDeviceToHost, s), "diagnostics copy");
+  if (rc) return rc;
+  rc = vcuda(cudaStreamSynchronize(s), "diagnostics synchronize");
+  if (rc) return rc;
+  for (int d = 0; d < g.dx; ++d) out[d] = h[8 + d];
+  for (int k = 0; k < 3 + dv; ++k) out[g.dx + k] = h[k];
+  return HD_OK;
+}
+
+int hd_vp_fields(hd_vp* v, double* rho, double* phi, double* E, void* stream) {
+  if (!v) return vfail(HD_ERR_INVALID, "hd_vp_fields: null handle");
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t nx = size_t(v->g.nx_dofs);
+  int rc = HD_OK;
+  if (rho && !rc) rc = vcuda(cudaMemcpyAsync(rho, v->d_rho, sizeof(double) * nx, cudaMemcpyDeviceToDevice, s), "rho");
+  if (phi && !rc) rc = vcuda(cudaMemcpyAsync(phi, v->d_phi, sizeof(double) * nx, cudaMemcpyDeviceToDevice, s), "phi");
+  if (E && !rc)
+    rc = vcuda(cudaMemcpyAsync(E, v->d_E, sizeof(double) * nx * v->g.dx, cudaMemcpyDeviceToDevice, s), "E");
+  return rc;
+}
+
+int hd_vp_cg_stats(const hd_vp* v, int* last_iterations, long long* total_iterations, long long* solves,
+                   double* last_residual, long long* learned_picked) {
+  if (!v) return vfail(HD_ERR_INVALID, "hd_vp_cg_stats: null handle");
+  if (learned_picked) *learned_picked = v->learned_picked;
+  if (last_iterations) *last_iterations = v->last_iters;
+  if (total_iterations) *total_iterations = v->total_iters;
+  if (solves) *solves = v->solves;
+  if (last_residual) *last_residual = v->last_res;
+  return HD_OK;
+}
+
+int hd_vp_set_guess(hd_vp* v, int guess) {
+  if (!v) return vfail(HD_ERR_INVALID, "hd_vp_set_guess: null handle");
+  if (guess < HD_VP_GUESS_ZERO || guess > HD_VP_GUESS_LEARNED) return vfail(HD_ERR_INVALID, "unknown guess");
+  if (guess == HD_VP_GUESS_LEARNED && !v->model) {
+    v->model = hd::vp_model_create(v->g.nx_dofs, v->desc.learn_rank > 0 ? v->desc.learn_rank : 32,
+                                   v->desc.learn_history > 0 ? v->desc.learn_history : 64);
+    if (!v->model) return vfail(HD_ERR_ALLOC, "learned-guess model");
+  }
+  if (guess != v->guess) v->have_prev = false;
+  v->guess = guess;
+  return HD_OK;
+}
+
+}  // extern "C"
+
+extern "C" int hd_vp_learn_loss_grad(long long n, int rank, int batch, const float* W1, const float* W2,
+                                     const float* X, const float* Y, float* dW1, float* dW2, float* loss,
+                                     void* stream) {
+  if (n < 1 || rank < 1 || batch < 1 || !W1 || !W2 || !X || !Y || !dW1 || !dW2 || !loss)
+    return vfail(HD_ERR_INVALID, "hd_vp_learn_loss_grad: bad argument");
+  float* work = nullptr;
+  cudaError_t e = cudaMalloc(&work, sizeof(float) * hd::vp_model_work_floats(n, rank, batch));
+  if (e != cudaSuccess) return vcuda(e, "hd_vp_learn_loss_grad: cudaMalloc");
+  cudaStream_t s = (cudaStream_t)stream;
+  e = hd::vp_model_loss_grad(n, rank, batch, W1, W2, X, Y, dW1, dW2, loss, work, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(work);
+  return vcuda(e, "hd_vp_learn_loss_grad");
+}

@@ -1,0 +1,52 @@
+// hd_vp.cuh -- Vlasov-Poisson pieces on the GPU (Gauss-Lobatto collocation,
+// dim_x == dim_v, periodic x- and v-meshes):
+//   * velocity moment rho(x) = int f dv (FP64 accumulation),
+//   * Poisson right-hand side, SIPG Laplacian and conjugate gradients (FP64,
+//     one cooperative launch per solve),
+//   * the field grad(phi) at the x-nodes,
+//   * the ECL advection operator with the phase-space velocity (v, grad phi),
+//   * diagnostics (field energy, mass, L2 norm, kinetic energy, momentum).
+// Reference: examples/vlasov_poisson/include/application.h:516-602,
+// poisson.h:100-255, derivative_container.h:158-251,
+// velocity_field_view.h:103-209, diagnostics.h:28-141,
+// include/hyper.deal/numerics/vector_tools.h:230-315.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "hd_ecl.cuh"
+
+namespace hd {
+
+struct VpGeom {
+  int D, dx, N, NCx, NC;
+  long long ncx, ncv, n_cells, nx_dofs;
+  int cells[kMaxDim];
+  long long cstride[kMaxDim + 1];
+  double lo[kMaxDim], h[kMaxDim];
+  double gl[kMaxN], glw[kMaxN];
+  double Dm[kMaxN * kMaxN];  // Dm[q*N + j] = l_j'(x_q) on [0,1]
+  double K1[kMaxN * kMaxN];  // 1D stiffness on [0,1]: sum_q Dm[q][i] w_q Dm[q][j]
+  double G[kMaxN * kMaxN];   // advection line matrix on [0,1]: G[i*N + q] = Dm[q][i] w_q / w_i
+  double pen;                // max(k,1) (k+1)
+};
+
+// advection with the phase-space velocity: dst = A(src).  The velocities
+// enter divided by the cell extent of the line's direction, precomputed in
+// FP64 and rounded to T once (no FP64 arithmetic in the kernel):
+//   x-direction d: xs[(d * cells_v + c) * N + i] = v_d(c, i) / h_{x_d}, the
+//                  v-coordinate of node i of v-cell c,
+//   v-direction d: es[(gid_x * NCx + i_x) * dx + d] = d_d phi(x-node) / h_{v_d}.
+template <typename T>
+struct VpAdvParams {
+  const T* src;
+  T* dst;
+  const T* xs;
+  const T* es;
+  VpGeom g;
+};
+
+cudaError_t launch_vp_advection(const VpAdvParams<float>& P, cudaStream_t s);
+cudaError_t launch_vp_advection(const VpAdvParams<double>& P, cudaStream_t s);
+
+}  // namespace hd

@@ -58,7 +58,10 @@ enum hd_bc_kind {
  * Dirichlet data (the reference passes dealii::Function objects):
  *   kind 0: 0;  kind 1: amp;
  *   kind 2: amp * prod_d trig_d(omega_d * (x_d - speed_d * t) + phase_d),
- *           trig_d = cos if cosine[d] else sin.                            */
+ *           trig_d = cos if cosine[d] else sin;
+ *   kind 3 (hd_vp_interpolate only): the perturbed Maxwellian
+ *           (1 + amp prod_{cosine[d]==1} cos(omega_d x_d + phase_d))
+ *             * prod_{cosine[d]==2} exp(-x_d^2 / 2) / sqrt(2 pi).          */
 typedef struct hd_function {
   int kind;
   double amp;
@@ -192,6 +195,74 @@ int hd_lsrk_stage_update(int dtype, long long n, double factor_bi, double factor
 /* Stage count, coefficients (ai: n_stages-1 values, bi: n_stages) and the
  * stage times c_s (n_stages values, c_0 = 0). */
 int hd_lsrk_coefficients(const hd_lsrk *rk, double *ai, double *bi, double *ci);
+
+/* ---- Vlasov-Poisson ------------------------------------------------------- */
+
+/* Electrostatic Vlasov-Poisson on periodic x- and v-meshes (dim_x == dim_v),
+ * Gauss-Lobatto collocation: one right-hand-side evaluation computes the
+ * charge density rho(x) = int f dv, solves the SIPG Poisson problem for the
+ * potential by conjugate gradients in FP64, takes E = grad(phi) at the
+ * x-nodes and applies the advection operator with the phase-space velocity
+ * (v, grad phi) -- the reference's examples/vlasov_poisson/include/
+ * application.h:516-602 (moments vector_tools.h:230-315, Poisson
+ * poisson.h:52-610, field derivative_container.h:158-251, velocity
+ * velocity_field_view.h:28-209).  f is stored in `dtype`; everything on the
+ * x-mesh is FP64. */
+enum hd_vp_guess {
+  HD_VP_GUESS_ZERO = 0,     /* CG starts from 0                                 */
+  HD_VP_GUESS_PREVIOUS = 1, /* from the previous potential (the reference's)    */
+  HD_VP_GUESS_LEARNED = 2   /* from phi_prev + net(rho - rho_prev), a network
+                               trained online on the solver's own differences
+                               between consecutive solves, judged against
+                               PREVIOUS by the initial residual               */
+};
+
+typedef struct hd_vp_desc {
+  int dim_x, dim_v, degree, dtype;
+  int cells_x[3], cells_v[3];
+  double lo_x[3], hi_x[3], lo_v[3], hi_v[3];
+  double cg_tol;        /* CG stops at ||r|| <= cg_tol ||r_0|| (deal.II
+                           ReductionControl(reduce = cg_tol), poisson.h:596),
+                           or at ||r|| <= cg_tol ||rhs|| with cg_rhs_relative */
+  int cg_max_iter;
+  int guess;            /* enum hd_vp_guess                                   */
+  int learn_rank;       /* bottleneck of the learned guess (0: 32)            */
+  int learn_history;    /* (rho, phi) pairs kept for training (0: 64)         */
+  int cg_rhs_relative;  /* 1: tolerance relative to ||rhs|| -- a fixed
+                           accuracy, so a better initial guess saves
+                           iterations                                         */
+} hd_vp_desc;
+
+typedef struct hd_vp hd_vp;
+
+int hd_vp_create(const hd_vp_desc *desc, hd_vp **out);
+int hd_vp_destroy(hd_vp *vp);
+long long hd_vp_n_dofs(const hd_vp *vp);
+long long hd_vp_n_dofs_x(const hd_vp *vp);
+/* f at the nodes of an analytic function (kind 3: perturbed Maxwellian) */
+int hd_vp_interpolate(hd_vp *vp, const hd_function *f, double time, void *dst, void *stream);
+/* steps 1-4 (rho, Poisson, field) for the distribution f; synchronises */
+int hd_vp_solve_field(hd_vp *vp, const void *f, void *stream);
+/* dst = the Vlasov-Poisson right-hand side of src (steps 1-5) */
+int hd_vp_apply(hd_vp *vp, void *dst, const void *src, double time, void *stream);
+/* one LSRK step with hd_vp_apply as the operator
+ * (time_integrators.templates.h:91-184, unfused) */
+int hd_vp_lsrk_step(hd_vp *vp, const hd_lsrk *rk, void *sol, void *Ki, void *Ti, double time, double dt,
+                    void *stream);
+/* out: field energy int (d_d phi)^2 per x-direction, mass, L2 norm, kinetic
+ * energy int |v|^2 f, momentum int v_d f per v-direction (diagnostics.h:28-141);
+ * the field is the one of the last right-hand-side evaluation */
+int hd_vp_diagnostics(hd_vp *vp, const void *f, double *out, void *stream);
+/* copies of rho, phi (x-DoFs) and E (x-DoFs * dim_x) into device buffers (NULL: skip) */
+int hd_vp_fields(hd_vp *vp, double *rho, double *phi, double *E, void *stream);
+int hd_vp_cg_stats(const hd_vp *vp, int *last_iterations, long long *total_iterations, long long *solves,
+                   double *last_residual, long long *learned_picked);
+int hd_vp_set_guess(hd_vp *vp, int guess);
+/* loss = 1/(2B) sum_b ||W2 W1 x_b - y_b||^2 and its gradients with the learned
+ * guess's own training kernels (device pointers, row-major W1: r x n,
+ * W2: n x r, X, Y: B x n) -- exposed to check them against a CPU reference */
+int hd_vp_learn_loss_grad(long long n, int rank, int batch, const float *W1, const float *W2, const float *X,
+                          const float *Y, float *dW1, float *dW2, float *loss, void *stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,198 @@
+"""Vlasov-Poisson right-hand side on the GPU (hd_vp_*) against the oracle.
+
+Gauss-Lobatto collocation, periodic, dim_x == dim_v.  FP64 pieces that do not
+involve CG (moment, Poisson right-hand side, SIPG product via the field of a
+given potential, interpolation) agree to round-off; everything downstream of
+CG agrees to the CG tolerance.  The learned CG initial guess is checked for
+its gradients (against numpy), for leaving the converged fields unchanged,
+and for its fallback to the previous potential.
+"""
+import math
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import oracle as O  # noqa: E402
+
+if torch.cuda.is_available():
+    from hyperdeal_gb300 import vlasov_poisson as V  # noqa: E402
+
+
+def _setup(dim_x, degree, cx, cv, dtype="f64", guess="previous", cg_tol=1e-12, rhs_relative=False):
+    D = 2 * dim_x
+    lo = [0.0] * dim_x + [-6.0] * dim_x
+    hi = [4 * math.pi] * dim_x + [6.0] * dim_x
+    params = V.VlasovPoissonParameters(dim_x, degree, [cx] * dim_x, [cv] * dim_x, lo[:dim_x], hi[:dim_x],
+                                       lo[dim_x:], hi[dim_x:], dtype=dtype, cg_tol=cg_tol, guess=guess,
+                                       cg_rhs_relative=rhs_relative)
+    prob = O.Problem(dim_x, dim_x, degree, [cx] * dim_x + [cv] * dim_x, lo, hi, [1.0] * dim_x + [6.0] * dim_x,
+                     collocation=True)
+    assert len(lo) == D
+    return V.VlasovPoissonOperation(params), prob
+
+
+def _rel(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300))
+
+
+CASES = [(1, 3, 8, 8), (2, 3, 4, 4), (2, 2, 3, 5), (3, 2, 2, 2)]
+
+
+@pytest.mark.parametrize("dim_x,degree,cx,cv", CASES)
+def test_interpolate_moment_rhs_field(dim_x, degree, cx, cv):
+    op, prob = _setup(dim_x, degree, cx, cv, guess="zero")
+    f0 = V.perturbed_maxwellian(dim_x, perturbed_dims=tuple(range(dim_x)))
+    f = op.initialize_dof_vector()
+    op.interpolate(f0, f)
+    fo = O.interpolate(prob, O.vp_initial_function(dim_x, dim_x, perturbed_dims=tuple(range(dim_x))))
+    assert _rel(f.cpu().numpy(), fo) <= 1e-14
+    op.solve_field(f)
+    rho, phi, E = (t.cpu().numpy() for t in op.fields())
+    rho_o = O.velocity_moment(prob, fo)
+    assert _rel(rho, rho_o) <= 1e-13
+    rhs_o = O.poisson_rhs(prob, rho_o)
+    # the GPU potential solves the oracle's system to the CG tolerance
+    res = O.poisson_apply(prob, phi) - rhs_o
+    assert np.linalg.norm(res) <= 1e-10 * np.linalg.norm(rhs_o)
+    phi_o = np.zeros_like(rho_o)
+    O.poisson_solve(prob, rhs_o, phi_o, 1e-12)
+    assert _rel(phi - phi.mean(), phi_o - phi_o.mean()) <= 1e-8
+    # the field is the exact derivative of the GPU potential
+    assert _rel(E, O.vp_field(prob, phi)) <= 1e-13
+    st = op.cg_stats()
+    assert st["solves"] == 1 and st["last_iterations"] > 0 and st["last_residual"] <= 1e-12
+
+
+@pytest.mark.parametrize("dim_x,degree,cx,cv", CASES)
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_apply_matches_oracle(dim_x, degree, cx, cv, dtype):
+    op, prob = _setup(dim_x, degree, cx, cv, dtype=dtype)
+    rng = np.random.default_rng(7 + dim_x * 10 + degree)
+    fo = O.interpolate(prob, O.vp_initial_function(dim_x, dim_x, eps=0.2))
+    fo = fo * (1.0 + 0.05 * rng.standard_normal(fo.size))
+    if dtype == "f32":
+        fo = fo.astype(np.float32).astype(np.float64)
+    tdt = torch.float64 if dtype == "f64" else torch.float32
+    src = torch.tensor(fo, dtype=tdt, device="cuda")
+    dst = op.initialize_dof_vector()
+    op.apply(dst, src, 0.0)
+    st = O.VPState(prob, 1e-12)
+    ref = np.zeros_like(fo)
+    st.operator(fo, ref, 0.0)
+    tol = 1e-9 if dtype == "f64" else 2e-5
+    assert _rel(dst.cpu().numpy(), ref) <= tol
+    # the operator is the advection with the field of f: evaluating it again gives the same result
+    dst2 = op.initialize_dof_vector()
+    op.apply(dst2, src, 0.0)
+    assert _rel(dst2.cpu().numpy(), dst.cpu().numpy()) <= (1e-10 if dtype == "f64" else 1e-5)
+
+
+def test_apply_rejects_bad_input():
+    op, _ = _setup(1, 3, 4, 4)
+    a = op.initialize_dof_vector()
+    with pytest.raises(V.HdError):
+        op.apply(a, a, 0.0)
+    with pytest.raises(V.HdError):
+        op.apply(a, torch.zeros(3, dtype=torch.float64, device="cuda"), 0.0)
+    with pytest.raises(V.HdError):
+        V.VlasovPoissonOperation(V.VlasovPoissonParameters(2, 3, [4, 4], [4, 4], [0, 0], [1, 1], [0, 0], [1, 1],
+                                                           cg_tol=0.0))
+
+
+@pytest.mark.parametrize("dim_x,degree,cells", [(1, 3, 8), (2, 3, 4)])
+def test_time_loop_diagnostics_match_oracle(dim_x, degree, cells):
+    rows, op = V.run_hyperrectangle(dim_x, degree, cells, cells, final_time=0.05, tick=0.01)
+    rows_o, st = O.run_vp_hyperrectangle(dim_x, dim_x, degree, cells, cells, collocation=True, final_time=0.05,
+                                         tick=0.01)
+    assert len(rows) == len(rows_o) and len(rows) >= 5
+    for r, ro in zip(rows, rows_o):
+        assert abs(r[0] - ro[0]) <= 1e-14
+        r, ro = np.array(r[1:]), np.array(ro[1:])
+        scale = np.maximum(np.abs(ro), 1e-12)
+        # momentum is zero up to the round-off of sums of size ~ mass * max|v|
+        assert np.all(np.abs(r - ro) <= 1e-8 * scale + 1e-12), (r, ro)
+    # mass is conserved by the scheme
+    assert abs(rows[-1][1 + dim_x] - rows[0][1 + dim_x]) <= 1e-12 * abs(rows[0][1 + dim_x])
+
+
+@pytest.mark.parametrize("n,r,B", [(200, 8, 13), (2048, 16, 10)])
+def test_learn_loss_grad_matches_numpy(n, r, B):
+    rng = np.random.default_rng(3)
+    W1 = (rng.standard_normal((r, n)) / np.sqrt(n)).astype(np.float32)
+    W2 = (rng.standard_normal((n, r)) / np.sqrt(r)).astype(np.float32)
+    X = rng.standard_normal((B, n)).astype(np.float32)
+    Y = rng.standard_normal((B, n)).astype(np.float32)
+    loss, dW1, dW2 = V.learn_loss_grad(*(torch.tensor(a, device="cuda") for a in (W1, W2, X, Y)))
+    W1d, W2d, Xd, Yd = (a.astype(np.float64) for a in (W1, W2, X, Y))
+    H = Xd @ W1d.T
+    Err = H @ W2d.T - Yd
+    ref_loss = 0.5 / B * np.sum(Err * Err)
+    ref_dW2 = Err.T @ H / B
+    ref_dW1 = (Err @ W2d).T @ Xd / B
+    assert abs(loss - ref_loss) <= 1e-5 * ref_loss
+    assert _rel(dW2.cpu().numpy(), ref_dW2) <= 1e-4
+    assert _rel(dW1.cpu().numpy(), ref_dW1) <= 1e-4
+    # finite-difference check of one entry of each gradient (float64 numpy)
+    def L(a, b):
+        e = (Xd @ a.T) @ b.T - Yd
+        return 0.5 / B * np.sum(e * e)
+    h = 1e-6
+    a = W1d.copy(); a[2, 5] += h
+    assert abs((L(a, W2d) - ref_loss) / h - ref_dW1[2, 5]) <= 1e-4 * max(1.0, abs(ref_dW1[2, 5]))
+    b = W2d.copy(); b[7, 3] += h
+    assert abs((L(W1d, b) - ref_loss) / h - ref_dW2[7, 3]) <= 1e-4 * max(1.0, abs(ref_dW2[7, 3]))
+
+
+def _run_steps(op, f, n_steps, dt):
+    Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
+    integ = V.LowStorageRungeKuttaIntegrator(Ki, Ti, "rk45")
+    for s in range(n_steps):
+        op.perform_time_step(integ, f, s * dt, dt)
+    return f
+
+
+@pytest.mark.parametrize("rhs_relative", [False, True])
+def test_learned_guess_same_solution(rhs_relative):
+    """The learned guess only changes where CG starts: the fields after a number of
+    steps agree with the previous-potential run to the CG tolerance, the judge
+    picks the learned guess at least once, and the first solves (model not
+    ready) fall back to the previous potential."""
+    dim_x, degree, cx, cv = 2, 3, 4, 6
+    runs = {}
+    for guess in ("previous", "learned"):
+        op, _ = _setup(dim_x, degree, cx, cv, guess=guess, cg_tol=1e-12, rhs_relative=rhs_relative)
+        f = op.initialize_dof_vector()
+        op.interpolate(V.perturbed_maxwellian(dim_x, eps=0.05, perturbed_dims=(0, 1)), f)
+        hx, hv = 4 * math.pi / cx, 12.0 / cv
+        dt = 0.05 * min(hx, hv / 6.0) / degree ** 1.5
+        _run_steps(op, f, 12, dt)
+        runs[guess] = (f.cpu().numpy(), op.diagnostics(f), op.cg_stats(), [t.cpu().numpy() for t in op.fields()])
+    fp, dp, sp, (rp, pp, Ep) = runs["previous"]
+    fl, dl, sl, (rl, pl, El) = runs["learned"]
+    assert _rel(fl, fp) <= 1e-10
+    assert _rel(El, Ep) <= 1e-8
+    assert _rel(pl - pl.mean(), pp - pp.mean()) <= 1e-8
+    assert abs(pl.mean()) <= 1e-12 * np.abs(pl).max()
+    assert np.allclose(dl, dp, rtol=1e-8, atol=1e-14)
+    assert sl["solves"] == sp["solves"] == 60
+    assert sp["learned_picked"] == 0
+    assert 0 < sl["learned_picked"] <= sl["solves"] - 2
+
+
+def test_rhs_relative_tolerance():
+    """cg_rhs_relative: the potential meets ||A phi - rhs|| <= tol ||rhs|| from any start."""
+    dim_x, degree, cx, cv = 2, 3, 4, 6
+    for guess in ("zero", "previous"):
+        op, prob = _setup(dim_x, degree, cx, cv, guess=guess, cg_tol=1e-9, rhs_relative=True)
+        f = op.initialize_dof_vector()
+        op.interpolate(V.perturbed_maxwellian(dim_x, eps=0.05, perturbed_dims=(0, 1)), f)
+        _run_steps(op, f, 2, 1e-3)
+        op.solve_field(f)
+        rho, phi, _ = (t.cpu().numpy() for t in op.fields())
+        rhs = O.poisson_rhs(prob, rho)
+        assert np.linalg.norm(O.poisson_apply(prob, phi) - rhs) <= 1.01e-9 * np.linalg.norm(rhs)
+        st = op.cg_stats()
+        assert st["solves"] == 11 and st["total_iterations"] >= st["last_iterations"]
