@@ -27,11 +27,19 @@ namespace hd {
 
 namespace {
 
-constexpr int kMomChunk = 16;       // v-cells summed by one block of the moment kernel
-constexpr int kCgThreads = 64;   // small blocks: the x-space system is small, spread it over many SMs
+constexpr int kMomChunk = 16;   // v-cells summed by one block of the moment kernel
+constexpr int kCgThreads = 64;  // small blocks: the x-space system is small, spread it over many SMs
+
+// device-side solver statistics (read by hd_vp_cg_stats; no host synchronisation per solve)
+struct VpStats {
+  long long total_iters, solves, learned_picked;
+  double last_res;
+  int last_iters, pad;
+};
 
 // ---------------------------------------------------------------- moments
-// partial[chunk][gx*NCx + ix] = sum over v-cells of the chunk and v-nodes of f * JxW_v
+// partial[chunk][gx*NCx + ix] = sum over the chunk's v-cells and the v-nodes of f * JxW_v
+// (the chunk's kMomChunk values of a node are loaded independently before they are summed)
 template <typename T>
 __global__ void moment_partials(VpGeom g, const T* __restrict__ f, const double* __restrict__ wv,
                                 double* __restrict__ partial) {
@@ -41,14 +49,23 @@ __global__ void moment_partials(VpGeom g, const T* __restrict__ f, const double*
   const long long gv0 = (long long)chunk * kMomChunk;
   const int NCv = g.NC / g.NCx;
   for (int node = threadIdx.x; node < g.NC; node += blockDim.x) {
-    const int iv = node / g.NCx;
-    double acc = 0.0;
+    T vals[kMomChunk];
+#pragma unroll
     for (int k = 0; k < kMomChunk; ++k) {
       const long long gv = gv0 + k;
-      if (gv >= g.ncv) break;
-      acc += double(f[(gxc + g.ncx * gv) * g.NC + node]) * wv[iv];
+      vals[k] = gv < g.ncv ? __ldg(f + (gxc + g.ncx * gv) * g.NC + node) : T(0);
     }
-    sh[node] = acc;
+    // FP32 storage: the chunk is summed pairwise in FP32 (the FP64 pipe is the
+    // scarce resource here; the values carry FP32 precision anyway);
+    // FP64 storage: summed in FP64
+    T h[kMomChunk];
+#pragma unroll
+    for (int k = 0; k < kMomChunk; ++k) h[k] = vals[k];
+#pragma unroll
+    for (int w = kMomChunk / 2; w > 0; w /= 2)
+#pragma unroll
+      for (int k = 0; k < w; ++k) h[k] += h[k + w];
+    sh[node] = double(h[0]) * wv[node / g.NCx];
   }
   __syncthreads();
   for (int ix = threadIdx.x; ix < g.NCx; ix += blockDim.x) {
@@ -56,14 +73,6 @@ __global__ void moment_partials(VpGeom g, const T* __restrict__ f, const double*
     for (int iv = 0; iv < NCv; ++iv) s += sh[ix + g.NCx * iv];
     partial[(long long)chunk * g.nx_dofs + gxc * g.NCx + ix] = s;
   }
-}
-
-__global__ void moment_sum(long long nx, int nchunks, const double* __restrict__ partial, double* __restrict__ rho) {
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= nx) return;
-  double s = 0.0;
-  for (int c = 0; c < nchunks; ++c) s += partial[(long long)c * nx + i];
-  rho[i] = s;
 }
 
 // block-wide sum in a fixed order (all threads receive the result)
@@ -78,7 +87,7 @@ __device__ double block_sum(double v, double* sh) {
   return s;
 }
 
-__device__ double x_jxw(const VpGeom& g, int ix) {
+__host__ __device__ double x_jxw(const VpGeom& g, int ix) {
   double j = 1.0;
   for (int d = 0; d < g.dx; ++d) {
     j *= g.h[d] * g.glw[ix % g.N];
@@ -87,29 +96,14 @@ __device__ double x_jxw(const VpGeom& g, int ix) {
   return j;
 }
 
-// rhs = -(rho - mean rho) JxW, then mean removed (single block; x-space is small)
-__global__ void poisson_rhs_kernel(VpGeom g, const double* __restrict__ rho, double* __restrict__ rhs) {
-  __shared__ double sh[32];
-  const long long n = g.nx_dofs;
-  double s = 0.0;
-  for (long long i = threadIdx.x; i < n; i += blockDim.x) s += rho[i];
-  const double mean = block_sum(s, sh) / double(n);
-  double s2 = 0.0;
-  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
-    const double v = -(rho[i] - mean) * x_jxw(g, int(i % g.NCx));
-    rhs[i] = v;
-    s2 += v;
-  }
-  const double mean2 = block_sum(s2, sh) / double(n);
-  for (long long i = threadIdx.x; i < n; i += blockDim.x) rhs[i] -= mean2;
-}
-
 // ---------------------------------------------------------------- SIPG row
 // (A u)_i for x-DoF i: cell stiffness + for both faces of every direction the
 // SIPG terms sigma [u][v] - {d_n u}[v] - [u]{d_n v} at the Gauss-Lobatto face
-// points (poisson.h:131-255).  Constants are in the kernel, so the
-// reference's removal of the input mean does not change the result.
-__device__ double sipg_row(const VpGeom& g, const double* __restrict__ u, long long i) {
+// points (poisson.h:131-255).  u(k) returns entry k.  Constants are in the
+// kernel, so the reference's removal of the input mean does not change the
+// result.  Used once, to assemble the matrix (ELL format, see below).
+template <class U>
+__device__ double sipg_row(const VpGeom& g, U u, long long i) {
   const int N = g.N;
   const long long gx = i / g.NCx;
   const int ix = int(i - gx * g.NCx);
@@ -133,9 +127,9 @@ __device__ double sipg_row(const VpGeom& g, const double* __restrict__ u, long l
     const long long gR = cc[d] + 1 < g.cells[d] ? gx + cs : gx - (long long)(g.cells[d] - 1) * cs;
     double L[kMaxN], Lf[kMaxN], R[kMaxN];
     for (int j = 0; j < N; ++j) {
-      L[j] = u[gx * g.NCx + base + j * s];
-      Lf[j] = u[gL * g.NCx + base + j * s];
-      R[j] = u[gR * g.NCx + base + j * s];
+      L[j] = u(gx * g.NCx + base + j * s);
+      Lf[j] = u(gL * g.NCx + base + j * s);
+      R[j] = u(gR * g.NCx + base + j * s);
     }
     double wface = 1.0;
     for (int e = 0; e < g.dx; ++e)
@@ -167,100 +161,246 @@ __device__ double sipg_row(const VpGeom& g, const double* __restrict__ u, long l
   return val;
 }
 
-struct CgArgs {
-  VpGeom g;
-  const double* rhs;
-  double* x;
-  double* r;
-  double* p;
-  double* Ap;
-  double* red;  // [2][gridDim] partial sums
-  double rel_tol;
-  int rhs_relative;  // 1: stop at ||r|| <= rel_tol ||rhs||; 0: at rel_tol ||r_0||
-  int max_iter;
-  int* iters;   // out: iterations
-  double* res;  // out: final / initial residual
-};
+// The SIPG matrix in ELL form: row i has at most W = 3 N dim_x entries (the
+// own-cell line and both neighbours' lines through i along every direction);
+// col/val are stored [k][i] so that consecutive rows read consecutive words.
+// Each coefficient is the row's linear form applied to a unit vector.
+__global__ void assemble_sipg_ell(VpGeom g, int W, int* __restrict__ col, double* __restrict__ val) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long n = g.nx_dofs;
+  if (i >= n) return;
+  const int N = g.N;
+  const long long gx = i / g.NCx;
+  const int ix = int(i - gx * g.NCx);
+  long long cand[3 * 3 * kMaxN];
+  int m = 0;
+  int s = 1;
+  long long c = gx;
+  for (int d = 0; d < g.dx; ++d) {
+    const int idd = (ix / s) % N, cd = int(c % g.cells[d]);
+    c /= g.cells[d];
+    const int base = ix - idd * s;
+    const long long cs = g.cstride[d];
+    const long long gL = cd > 0 ? gx - cs : gx + (long long)(g.cells[d] - 1) * cs;
+    const long long gR = cd + 1 < g.cells[d] ? gx + cs : gx - (long long)(g.cells[d] - 1) * cs;
+    const long long cells3[3] = {gx, gL, gR};
+    for (int q = 0; q < 3; ++q)
+      for (int j = 0; j < N; ++j) {
+        const long long k = cells3[q] * g.NCx + base + j * s;
+        bool dup = false;
+        for (int e = 0; e < m; ++e) dup |= cand[e] == k;
+        if (!dup) cand[m++] = k;
+      }
+    s *= N;
+  }
+  for (int e = 0; e < W; ++e) {
+    long long k = i;
+    double a = 0.0;
+    if (e < m) {
+      k = cand[e];
+      a = sipg_row(g, [k](long long t) { return t == k ? 1.0 : 0.0; }, i);
+    }
+    col[(long long)e * n + i] = int(k);
+    val[(long long)e * n + i] = a;
+  }
+}
 
-__device__ double grid_sum(cgrp::grid_group& grid, double v, double* red, int slot, double* sh) {
-  const double b = block_sum(v, sh);
-  if (threadIdx.x == 0) red[slot * gridDim.x + blockIdx.x] = b;
-  grid.sync();
+// (A u)_i from the ELL matrix; the matrix is read through the read-only path
+// (it stays in L1 across the CG iterations), u through L2 (other blocks write it)
+__device__ __forceinline__ double spmv_row(int W, long long n, const int* __restrict__ col,
+                                           const double* __restrict__ val, const double* u, long long i) {
   double s = 0.0;
-  for (int k = 0; k < (int)gridDim.x; ++k) s += red[slot * gridDim.x + k];
+  int e = 0;
+  for (; e + 8 <= W; e += 8) {
+    double a[8], b[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      a[q] = __ldg(val + (long long)(e + q) * n + i);
+      b[q] = __ldcg(u + __ldg(col + (long long)(e + q) * n + i));
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s = fma(a[q], b[q], s);
+  }
+  for (; e < W; ++e) s = fma(__ldg(val + (long long)e * n + i), __ldcg(u + __ldg(col + (long long)e * n + i)), s);
   return s;
 }
 
-// conjugate gradients on the SIPG system, all iterations in one cooperative launch
-__global__ void __launch_bounds__(kCgThreads) cg_kernel(CgArgs A) {
+struct PoissonArgs {
+  VpGeom g;
+  int W;
+  const int* col;
+  const double* val;
+  const double* partial;  // moment partials (nchunks x nx)
+  int nchunks;
+  int phases;             // bit 0: rho and rhs from the partials; bit 1: CG and the field
+  double* rho;
+  double* rhs;
+  double* x;              // potential: initial guess in, solution out
+  double* r;
+  double* p;
+  double* Ap;
+  double* red;            // [2][gridDim] partial sums
+  double rel_tol;
+  int rhs_relative;       // 1: stop at ||r|| <= rel_tol ||rhs||; 0: at rel_tol ||r_0||
+  int max_iter;
+  double* E;              // E[i*dx + d] = d_d phi at the x-node
+  void* es;               // E / h_v in the storage precision
+  int es_f32;
+  VpStats* stats;
+};
+
+// fixed-order grid-wide sums of two values; consecutive calls alternate
+// between the two halves of `red`, so a half is rewritten only after every
+// block has read it.  Every warp adds the block partials lane-parallel in the
+// same fixed order, so all threads of the grid obtain identical values.
+__device__ double2 grid_sum2(cgrp::grid_group& grid, double v0, double v1, double* red, int& slot, double* sh) {
+  const double b0 = block_sum(v0, sh);
+  const double b1 = block_sum(v1, sh);
+  double* half = red + slot * 2 * gridDim.x;
+  if (threadIdx.x == 0) {
+    half[2 * blockIdx.x] = b0;
+    half[2 * blockIdx.x + 1] = b1;
+  }
+  grid.sync();
+  const int lane = threadIdx.x & 31;
+  double s0 = 0.0, s1 = 0.0;
+  for (int k = lane; k < (int)gridDim.x; k += 32) {
+    s0 += __ldcg(half + 2 * k);
+    s1 += __ldcg(half + 2 * k + 1);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, o);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+  }
+  slot ^= 1;
+  return make_double2(__shfl_sync(0xffffffffu, s0, 0), __shfl_sync(0xffffffffu, s1, 0));
+}
+
+// One cooperative launch per solve (or two around the learned guess):
+// rho and the right-hand side (application.h:531-568: rho~ = rho - mean,
+// rhs = -M rho~, rhs -= mean), conjugate gradients on the SIPG system, and
+// the field E = grad(phi) at the x-nodes (derivative_container.h:158-251).
+// CG is the Chronopoulos-Gear form (one fused reduction of (r,r) and (Ar,r)
+// per iteration: two grid barriers instead of three); in exact arithmetic
+// it produces the iterates of plain CG.
+__global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
   cgrp::grid_group grid = cgrp::this_grid();
   __shared__ double sh[32];
-  const long long n = A.g.nx_dofs;
+  const VpGeom& g = A.g;
+  const long long n = g.nx_dofs;
   const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x, stride = (long long)gridDim.x * blockDim.x;
-  double lrr = 0.0, lbb = 0.0;
+  int slot = 0;
+  if (A.phases & 1) {
+    double ls = 0.0;
+    for (long long i = t0; i < n; i += stride) {
+      // eight independent partial sums (fixed order) keep eight loads in flight
+      double s8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      int c = 0;
+      for (; c + 8 <= A.nchunks; c += 8)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) s8[q] += A.partial[(long long)(c + q) * n + i];
+      for (; c < A.nchunks; ++c) s8[0] += A.partial[(long long)c * n + i];
+      const double s = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
+      A.rho[i] = s;
+      ls += s;
+    }
+    const double mean = grid_sum2(grid, ls, 0.0, A.red, slot, sh).x / double(n);
+    double l2 = 0.0;
+    for (long long i = t0; i < n; i += stride) {
+      const double v = -(A.rho[i] - mean) * x_jxw(g, int(i % g.NCx));
+      A.rhs[i] = v;
+      l2 += v;
+    }
+    const double mean2 = grid_sum2(grid, l2, 0.0, A.red, slot, sh).x / double(n);
+    for (long long i = t0; i < n; i += stride) A.rhs[i] -= mean2;
+  }
+  if (!(A.phases & 2)) return;
+  double* const r = A.r;
+  double* const p = A.p;
+  double* const w = A.Ap;    // A r
+  double* const sv = A.Ap + n;  // A p
+  double lbb = 0.0;
   for (long long i = t0; i < n; i += stride) {
-    const double ri = A.rhs[i] - sipg_row(A.g, A.x, i);
-    A.r[i] = ri;
-    A.p[i] = ri;
-    lrr += ri * ri;
+    r[i] = A.rhs[i] - spmv_row(A.W, n, A.col, A.val, A.x, i);
     lbb += A.rhs[i] * A.rhs[i];
   }
-  double rr = grid_sum(grid, lrr, A.red, 0, sh);
-  const double bb = grid_sum(grid, lbb, A.red, 1, sh);
-  const double r0 = sqrt(rr);
+  grid.sync();  // r complete before A r
+  double lrr = 0.0, lwr = 0.0;
+  for (long long i = t0; i < n; i += stride) {
+    const double wi = spmv_row(A.W, n, A.col, A.val, r, i);
+    w[i] = wi;
+    lrr += r[i] * r[i];
+    lwr += wi * r[i];
+  }
+  double2 t = grid_sum2(grid, lrr, lwr, A.red, slot, sh);
+  const double bb = grid_sum2(grid, lbb, 0.0, A.red, slot, sh).x;
+  double gamma = t.x, delta = t.y;
+  const double r0 = sqrt(gamma);
   const double stop = A.rhs_relative ? A.rel_tol * sqrt(bb) : fmax(A.rel_tol * r0, 1e-14 * sqrt(bb));
   int it = 0;
-  while (sqrt(rr) > stop && it < A.max_iter) {
-    double lpap = 0.0;
+  double alpha = delta > 0.0 ? gamma / delta : 0.0, beta = 0.0;
+  while (sqrt(gamma) > stop && it < A.max_iter && alpha > 0.0) {
     for (long long i = t0; i < n; i += stride) {
-      const double a = sipg_row(A.g, A.p, i);
-      A.Ap[i] = a;
-      lpap += A.p[i] * a;
+      const double pi = r[i] + (it ? beta * p[i] : 0.0);
+      const double si = w[i] + (it ? beta * sv[i] : 0.0);
+      p[i] = pi;
+      sv[i] = si;
+      A.x[i] += alpha * pi;
+      r[i] -= alpha * si;
     }
-    const double pap = grid_sum(grid, lpap, A.red, it & 1, sh);
-    if (!(pap > 0.0)) break;
-    const double alpha = rr / pap;
-    double lrn = 0.0;
-    for (long long i = t0; i < n; i += stride) {
-      A.x[i] += alpha * A.p[i];
-      const double ri = A.r[i] - alpha * A.Ap[i];
-      A.r[i] = ri;
-      lrn += ri * ri;
-    }
-    const double rn = grid_sum(grid, lrn, A.red, (it + 1) & 1, sh);
-    const double beta = rn / rr;
-    for (long long i = t0; i < n; i += stride) A.p[i] = A.r[i] + beta * A.p[i];
-    rr = rn;
     ++it;
-    grid.sync();  // p complete before the next product
+    grid.sync();  // r complete before A r
+    lrr = 0.0;
+    lwr = 0.0;
+    for (long long i = t0; i < n; i += stride) {
+      const double wi = spmv_row(A.W, n, A.col, A.val, r, i);
+      w[i] = wi;
+      lrr += r[i] * r[i];
+      lwr += wi * r[i];
+    }
+    t = grid_sum2(grid, lrr, lwr, A.red, slot, sh);
+    const double gn = t.x;
+    delta = t.y;
+    beta = gn / gamma;
+    const double den = delta - beta * gn / alpha;
+    alpha = den > 0.0 ? gn / den : 0.0;
+    gamma = gn;
+  }
+  grid.sync();  // x complete before the field reads it
+  const int N = g.N;
+  for (long long i = t0; i < n; i += stride) {
+    const long long gx = i / g.NCx;
+    const int ix = int(i - gx * g.NCx);
+    int s = 1;
+    for (int d = 0; d < g.dx; ++d) {
+      const int idd = (ix / s) % N;
+      const int base = ix - idd * s;
+      double a = 0.0;
+      for (int j = 0; j < N; ++j) a += g.Dm[idd * N + j] * A.x[gx * g.NCx + base + j * s];
+      const double e = a / g.h[d];
+      A.E[i * g.dx + d] = e;
+      const double es = e / g.h[g.dx + d];
+      if (A.es_f32) static_cast<float*>(A.es)[i * g.dx + d] = float(es);
+      else static_cast<double*>(A.es)[i * g.dx + d] = es;
+      s *= N;
+    }
   }
   if (t0 == 0) {
-    *A.iters = it;
-    *A.res = r0 > 0.0 ? sqrt(rr) / r0 : 0.0;
+    A.stats->last_iters = it;
+    A.stats->total_iters += it;
+    A.stats->solves += 1;
+    A.stats->last_res = r0 > 0.0 ? sqrt(gamma) / r0 : 0.0;
   }
-}
-
-// c = a - b (b == nullptr: c = a)
-__global__ void diff_kernel(long long n, const double* __restrict__ a, const double* __restrict__ b,
-                            double* __restrict__ c) {
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i < n) c[i] = b ? a[i] - b[i] : a[i];
-}
-
-// y += x
-__global__ void add_kernel(long long n, const double* __restrict__ x, double* __restrict__ y) {
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i < n) y[i] += x[i];
 }
 
 // per-block partial sums of ||rhs - A u||^2 for two candidate vectors u0, u1
-__global__ void residual_partials(VpGeom g, const double* __restrict__ rhs, const double* __restrict__ u0,
+__global__ void residual_partials(long long n, int W, const int* __restrict__ col, const double* __restrict__ val,
+                                  const double* __restrict__ rhs, const double* __restrict__ u0,
                                   const double* __restrict__ u1, double* __restrict__ partial) {
   __shared__ double sh[32];
   double a = 0.0, b = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < g.nx_dofs;
-       i += (long long)gridDim.x * blockDim.x) {
-    const double r0 = rhs[i] - sipg_row(g, u0, i), r1 = rhs[i] - sipg_row(g, u1, i);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double r0 = rhs[i] - spmv_row(W, n, col, val, u0, i), r1 = rhs[i] - spmv_row(W, n, col, val, u1, i);
     a += r0 * r0;
     b += r1 * r1;
   }
@@ -273,9 +413,9 @@ __global__ void residual_partials(VpGeom g, const double* __restrict__ rhs, cons
 }
 
 // the judge: the candidate with the smaller initial residual starts CG
-// (u1 is copied over u0 when it wins; flag[0] = 1 then)
+// (u1 is copied over u0 when it wins, and counted)
 __global__ void choose_guess(long long n, int nblocks, const double* __restrict__ partial, double* __restrict__ u0,
-                             const double* __restrict__ u1, int* __restrict__ flag) {
+                             const double* __restrict__ u1, VpStats* stats) {
   __shared__ int pick;
   if (threadIdx.x == 0) {
     double a = 0.0, b = 0.0;
@@ -284,37 +424,24 @@ __global__ void choose_guess(long long n, int nblocks, const double* __restrict_
       b += partial[2 * k + 1];
     }
     pick = b < a ? 1 : 0;
-    *flag = pick;
+    stats->learned_picked += pick;
   }
   __syncthreads();
   if (pick)
     for (long long i = threadIdx.x; i < n; i += blockDim.x) u0[i] = u1[i];
 }
 
-// E[(gx*NCx + ix)*dx + d] = d/dx_d phi at the x-node
-__global__ void field_kernel(VpGeom g, const double* __restrict__ phi, double* __restrict__ E) {
+// c = a - b
+__global__ void diff_kernel(long long n, const double* __restrict__ a, const double* __restrict__ b,
+                            double* __restrict__ c) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= g.nx_dofs) return;
-  const int N = g.N;
-  const long long gx = i / g.NCx;
-  const int ix = int(i - gx * g.NCx);
-  int s = 1;
-  for (int d = 0; d < g.dx; ++d) {
-    const int idd = (ix / s) % N;
-    const int base = ix - idd * s;
-    double a = 0.0;
-    for (int j = 0; j < N; ++j) a += g.Dm[idd * N + j] * phi[gx * g.NCx + base + j * s];
-    E[i * g.dx + d] = a / g.h[d];
-    s *= N;
-  }
+  if (i < n) c[i] = a[i] - b[i];
 }
 
-// es[i*dx + d] = E[i*dx + d] / h_{v_d} in the storage precision (advection input)
-template <typename T>
-__global__ void scale_field_kernel(VpGeom g, const double* __restrict__ E, T* __restrict__ es) {
+// y += x
+__global__ void add_kernel(long long n, const double* __restrict__ x, double* __restrict__ y) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= g.nx_dofs * g.dx) return;
-  es[i] = T(E[i] / g.h[g.dx + int(i % g.dx)]);
+  if (i < n) y[i] += x[i];
 }
 
 // ---------------------------------------------------------------- diagnostics
@@ -370,13 +497,13 @@ __global__ void energy_kernel(VpGeom g, const double* __restrict__ E, double* __
 }
 
 __global__ void diag_finish(int nblocks, int nq, const double* __restrict__ partial, double* __restrict__ out) {
-  if (threadIdx.x != 0) return;
+  __shared__ double sh[32];
   for (int k = 0; k < nq; ++k) {
     double s = 0.0;
-    for (int b = 0; b < nblocks; ++b) s += partial[b * 6 + k];
-    out[k] = s;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partial[b * 6 + k];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) out[k] = k == 1 ? sqrt(s) : s;
   }
-  out[1] = sqrt(out[1]);
 }
 
 // kind 3: (1 + amp prod_{cosine[d]==1} cos(omega_d x_d + phase_d)) prod_{cosine[d]==2} exp(-x_d^2/2)/sqrt(2 pi),
@@ -432,8 +559,11 @@ struct hd_vp {
   double* d_E;
   void* d_xs;         // x-line velocities / h_x in the storage precision
   void* d_es;         // E / h_v in the storage precision
-  double* d_cg;       // r, p, Ap (3 * nx) + reductions (2 * cg_grid) + residual
-  int* d_iters;
+  double* d_cg;       // r, p, A r, A p (4 * nx) + reductions (2 halves * 2 values * cg_grid)
+  int ell_w;          // SIPG matrix in ELL form (ell_w entries per row, [k][row])
+  int* d_ell_col;
+  double* d_ell_val;
+  hd::VpStats* d_stats;
   double* d_diag;     // phase-space partials (blocks * 6) + outputs
   double* d_guess;    // learned prediction (nx)
   double* d_rho_prev; // rho and phi of the previous solve (the learned model
@@ -442,13 +572,8 @@ struct hd_vp {
   double* d_dy;       // phi - phi_prev
   bool have_prev;
   double* d_judge;    // residual partials of the judge
-  int* d_pick;        // 1 when the learned guess started CG
-  long long learned_picked;
   int cg_grid;
   int guess;
-  int last_iters;
-  long long total_iters, solves;
-  double last_res;
   hd::VpModel* model;  // learned initial guess
 };
 
@@ -532,7 +657,9 @@ void vp_free(hd_vp* v) {
   cudaFree(v->d_xs);
   cudaFree(v->d_es);
   cudaFree(v->d_cg);
-  cudaFree(v->d_iters);
+  cudaFree(v->d_ell_col);
+  cudaFree(v->d_ell_val);
+  cudaFree(v->d_stats);
   cudaFree(v->d_diag);
   cudaFree(v->d_guess);
   cudaFree(v->d_rho_prev);
@@ -540,93 +667,91 @@ void vp_free(hd_vp* v) {
   cudaFree(v->d_dx);
   cudaFree(v->d_dy);
   cudaFree(v->d_judge);
-  cudaFree(v->d_pick);
   hd::vp_model_destroy(v->model);
   delete v;
 }
 
-int solve_poisson(hd_vp* v, cudaStream_t s) {
-  hd::VpGeom& g = v->g;
-  const long long nx = g.nx_dofs;
-  // initial guess
-  if (v->guess == HD_VP_GUESS_ZERO) {
-    int rc = vcuda(cudaMemsetAsync(v->d_phi, 0, sizeof(double) * nx, s), "zero guess");
-    if (rc) return rc;
-  }
-  // learned: the solution map is linear, so the model is trained on and
-  // applied to differences to the previous solve: guess = phi_prev +
-  // model(rho - rho_prev), judged against phi_prev by the initial residual
-  // (without a previous solve both differences are taken from zero)
-  const bool learned = v->guess == HD_VP_GUESS_LEARNED && v->model;
-  const unsigned nb = unsigned((nx + 255) / 256);
-  bool judged = false;
-  if (learned) {
-    int rc;
-    if (v->have_prev) {
-      rc = vcuda(cudaMemcpyAsync(v->d_phi_prev, v->d_phi, sizeof(double) * nx, cudaMemcpyDeviceToDevice, s),
-                 "previous potential");
-    } else {
-      rc = vcuda(cudaMemsetAsync(v->d_phi_prev, 0, sizeof(double) * nx, s), "previous potential");
-      if (!rc) rc = vcuda(cudaMemsetAsync(v->d_rho_prev, 0, sizeof(double) * nx, s), "previous density");
-    }
-    if (rc) return rc;
-    hd::diff_kernel<<<nb, 256, 0, s>>>(nx, v->d_rho, v->d_rho_prev, v->d_dx);
-    if (hd::vp_model_ready(v->model)) {
-      rc = vcuda(hd::vp_model_predict(v->model, v->d_dx, v->d_guess, s), "learned guess");
-      if (rc) return rc;
-      hd::add_kernel<<<nb, 256, 0, s>>>(nx, v->d_phi_prev, v->d_guess);
-      constexpr int kJudgeBlocks = 64;
-      hd::residual_partials<<<kJudgeBlocks, 256, 0, s>>>(g, v->d_rhs, v->d_phi, v->d_guess, v->d_judge);
-      hd::choose_guess<<<1, 1024, 0, s>>>(nx, kJudgeBlocks, v->d_judge, v->d_phi, v->d_guess, v->d_pick);
-      judged = true;
-    }
-    rc = vcuda(cudaGetLastError(), "learned guess");
-    if (rc) return rc;
-  }
-  hd::CgArgs A;
-  A.g = g;
+hd::PoissonArgs poisson_args(hd_vp* v, int phases) {
+  hd::PoissonArgs A;
+  const long long nx = v->g.nx_dofs;
+  A.g = v->g;
+  A.W = v->ell_w;
+  A.col = v->d_ell_col;
+  A.val = v->d_ell_val;
+  A.partial = v->d_partial;
+  A.nchunks = v->nchunks;
+  A.phases = phases;
+  A.rho = v->d_rho;
   A.rhs = v->d_rhs;
   A.x = v->d_phi;
   A.r = v->d_cg;
   A.p = v->d_cg + nx;
   A.Ap = v->d_cg + 2 * nx;
-  A.red = v->d_cg + 3 * nx;
+  A.red = v->d_cg + 4 * nx;
   A.rel_tol = v->desc.cg_tol;
   A.rhs_relative = v->desc.cg_rhs_relative;
   A.max_iter = v->desc.cg_max_iter;
-  A.iters = v->d_iters;
-  A.res = v->d_cg + 3 * nx + 2 * v->cg_grid;
+  A.E = v->d_E;
+  A.es = v->d_es;
+  A.es_f32 = v->dtype == HD_F32;
+  A.stats = v->d_stats;
+  return A;
+}
+
+int launch_poisson(hd_vp* v, int phases, cudaStream_t s) {
+  hd::PoissonArgs A = poisson_args(v, phases);
   void* args[] = {&A};
-  int rc = vcuda(cudaLaunchCooperativeKernel((void*)hd::cg_kernel, dim3(v->cg_grid), dim3(hd::kCgThreads), args, 0, s),
-                 "CG launch");
+  return vcuda(cudaLaunchCooperativeKernel((void*)hd::poisson_kernel, dim3(v->cg_grid), dim3(hd::kCgThreads), args, 0,
+                                           s),
+               "Poisson launch");
+}
+
+// rho (from the moment partials), the right-hand side, CG from the chosen
+// initial guess and the field; asynchronous (statistics stay on the device)
+int solve_poisson(hd_vp* v, cudaStream_t s) {
+  const long long nx = v->g.nx_dofs;
+  if (v->guess == HD_VP_GUESS_ZERO) {
+    int rc = vcuda(cudaMemsetAsync(v->d_phi, 0, sizeof(double) * nx, s), "zero guess");
+    if (rc) return rc;
+  }
+  const bool learned = v->guess == HD_VP_GUESS_LEARNED && v->model;
+  if (!learned) return launch_poisson(v, 3, s);
+  // learned: the solution map is linear, so the model is trained on and
+  // applied to differences to the previous solve: guess = phi_prev +
+  // model(rho - rho_prev), judged against phi_prev by the initial residual
+  // (without a previous solve both differences are taken from zero)
+  int rc = launch_poisson(v, 1, s);
+  if (rc) return rc;
+  const unsigned nb = unsigned((nx + 255) / 256);
+  if (v->have_prev) {
+    rc = vcuda(cudaMemcpyAsync(v->d_phi_prev, v->d_phi, sizeof(double) * nx, cudaMemcpyDeviceToDevice, s),
+               "previous potential");
+  } else {
+    rc = vcuda(cudaMemsetAsync(v->d_phi_prev, 0, sizeof(double) * nx, s), "previous potential");
+    if (!rc) rc = vcuda(cudaMemsetAsync(v->d_rho_prev, 0, sizeof(double) * nx, s), "previous density");
+  }
+  if (rc) return rc;
+  hd::diff_kernel<<<nb, 256, 0, s>>>(nx, v->d_rho, v->d_rho_prev, v->d_dx);
+  if (hd::vp_model_ready(v->model)) {
+    rc = vcuda(hd::vp_model_predict(v->model, v->d_dx, v->d_guess, s), "learned guess");
+    if (rc) return rc;
+    hd::add_kernel<<<nb, 256, 0, s>>>(nx, v->d_phi_prev, v->d_guess);
+    constexpr int kJudgeBlocks = 64;
+    hd::residual_partials<<<kJudgeBlocks, 256, 0, s>>>(nx, v->ell_w, v->d_ell_col, v->d_ell_val, v->d_rhs, v->d_phi,
+                                                       v->d_guess, v->d_judge);
+    hd::choose_guess<<<1, 1024, 0, s>>>(nx, kJudgeBlocks, v->d_judge, v->d_phi, v->d_guess, v->d_stats);
+  }
+  rc = vcuda(cudaGetLastError(), "learned guess");
+  if (rc) return rc;
+  rc = launch_poisson(v, 2, s);
   if (rc) return rc;
   // the solver's own (rho - rho_prev, phi - phi_prev) pair trains the learned guess
-  if (learned) {
-    hd::diff_kernel<<<nb, 256, 0, s>>>(nx, v->d_phi, v->d_phi_prev, v->d_dy);
-    rc = vcuda(hd::vp_model_observe(v->model, v->d_dx, v->d_dy, s), "learned guess update");
-    if (!rc) rc = vcuda(cudaMemcpyAsync(v->d_rho_prev, v->d_rho, sizeof(double) * nx, cudaMemcpyDeviceToDevice, s),
-                        "previous density");
-    if (rc) return rc;
-    v->have_prev = true;
-  }
-  int it = 0;
-  double res = 0.0;
-  rc = vcuda(cudaMemcpyAsync(&it, v->d_iters, sizeof(int), cudaMemcpyDeviceToHost, s), "CG iterations");
+  hd::diff_kernel<<<nb, 256, 0, s>>>(nx, v->d_phi, v->d_phi_prev, v->d_dy);
+  rc = vcuda(hd::vp_model_observe(v->model, v->d_dx, v->d_dy, s), "learned guess update");
+  if (!rc) rc = vcuda(cudaMemcpyAsync(v->d_rho_prev, v->d_rho, sizeof(double) * nx, cudaMemcpyDeviceToDevice, s),
+                      "previous density");
   if (rc) return rc;
-  rc = vcuda(cudaMemcpyAsync(&res, A.res, sizeof(double), cudaMemcpyDeviceToHost, s), "CG residual");
-  if (rc) return rc;
-  int pick = 0;
-  if (judged) {
-    rc = vcuda(cudaMemcpyAsync(&pick, v->d_pick, sizeof(int), cudaMemcpyDeviceToHost, s), "judge flag");
-    if (rc) return rc;
-  }
-  rc = vcuda(cudaStreamSynchronize(s), "CG synchronize");
-  if (rc) return rc;
-  v->learned_picked += pick;
-  v->last_iters = it;
-  v->last_res = res;
-  v->total_iters += it;
-  v->solves += 1;
+  v->have_prev = true;
   return HD_OK;
 }
 
@@ -697,7 +822,7 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hd::cg_kernel, hd::kCgThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hd::poisson_kernel, hd::kCgThreads, 0);
   long long want = (g.nx_dofs + hd::kCgThreads - 1) / hd::kCgThreads;
   long long cap = (long long)sms * (per_sm > 0 ? per_sm : 1);
   v->cg_grid = int(want < cap ? want : cap);
@@ -715,8 +840,11 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
   alloc((void**)&v->d_E, sizeof(double) * nx * g.dx);
   alloc(&v->d_es, sizeof(double) * nx * g.dx);
   alloc(&v->d_xs, sizeof(double) * g.dx * 64 * hd::kMaxN);
-  alloc((void**)&v->d_cg, sizeof(double) * (3 * nx + 2 * v->cg_grid + 1));
-  alloc((void**)&v->d_iters, sizeof(int));
+  alloc((void**)&v->d_cg, sizeof(double) * (4 * nx + 4 * v->cg_grid));
+  v->ell_w = 3 * N * g.dx;
+  alloc((void**)&v->d_ell_col, sizeof(int) * size_t(v->ell_w) * nx);
+  alloc((void**)&v->d_ell_val, sizeof(double) * size_t(v->ell_w) * nx);
+  alloc((void**)&v->d_stats, sizeof(hd::VpStats));
   alloc((void**)&v->d_diag, sizeof(double) * (152 * 16 * 6 + 16));
   alloc((void**)&v->d_guess, sizeof(double) * nx);
   alloc((void**)&v->d_rho_prev, sizeof(double) * nx);
@@ -724,7 +852,6 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
   alloc((void**)&v->d_dx, sizeof(double) * nx);
   alloc((void**)&v->d_dy, sizeof(double) * nx);
   alloc((void**)&v->d_judge, sizeof(double) * 2 * 64);
-  alloc((void**)&v->d_pick, sizeof(int));
   if (e != cudaSuccess) { vp_free(v); return vcuda(e, "hd_vp_create: cudaMalloc"); }
   {
     double wv[4096];
@@ -756,6 +883,12 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
                        size_t(k) * (d.dtype == HD_F64 ? 8 : 4), cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) e = cudaMemset(v->d_es, 0, sizeof(double) * nx * g.dx);
+    if (e == cudaSuccess) e = cudaMemset(v->d_stats, 0, sizeof(hd::VpStats));
+    if (e == cudaSuccess) {
+      hd::assemble_sipg_ell<<<unsigned((nx + 127) / 128), 128>>>(g, v->ell_w, v->d_ell_col, v->d_ell_val);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e == cudaSuccess) e = cudaMemset(v->d_phi, 0, sizeof(double) * nx);
     if (e == cudaSuccess) e = cudaMemset(v->d_E, 0, sizeof(double) * nx * g.dx);
     if (e != cudaSuccess) { vp_free(v); return vcuda(e, "hd_vp_create: init"); }
@@ -805,17 +938,9 @@ int hd_vp_solve_field(hd_vp* v, const void* f, void* stream) {
   const size_t sh = sizeof(double) * g.NC;
   if (v->dtype == HD_F32) hd::moment_partials<float><<<grid, threads, sh, s>>>(g, (const float*)f, v->d_wv, v->d_partial);
   else hd::moment_partials<double><<<grid, threads, sh, s>>>(g, (const double*)f, v->d_wv, v->d_partial);
-  hd::moment_sum<<<unsigned((g.nx_dofs + 255) / 256), 256, 0, s>>>(g.nx_dofs, v->nchunks, v->d_partial, v->d_rho);
-  hd::poisson_rhs_kernel<<<1, 1024, 0, s>>>(g, v->d_rho, v->d_rhs);
-  int rc = vcuda(cudaGetLastError(), "vp moments / rhs");
+  int rc = vcuda(cudaGetLastError(), "vp moments");
   if (rc) return rc;
-  rc = solve_poisson(v, s);
-  if (rc) return rc;
-  hd::field_kernel<<<unsigned((g.nx_dofs + 255) / 256), 256, 0, s>>>(g, v->d_phi, v->d_E);
-  const unsigned ne = unsigned((g.nx_dofs * g.dx + 255) / 256);
-  if (v->dtype == HD_F32) hd::scale_field_kernel<float><<<ne, 256, 0, s>>>(g, v->d_E, (float*)v->d_es);
-  else hd::scale_field_kernel<double><<<ne, 256, 0, s>>>(g, v->d_E, (double*)v->d_es);
-  return vcuda(cudaGetLastError(), "vp field");
+  return solve_poisson(v, s);
 }
 
 int hd_vp_apply(hd_vp* v, void* dst, const void* src, double time, void* stream) {
@@ -866,7 +991,7 @@ int hd_vp_diagnostics(hd_vp* v, const void* f, double* out, void* stream) {
   double* res = v->d_diag + blocks * 6;
   if (v->dtype == HD_F32) hd::phase_diag_kernel<float><<<blocks, 256, 0, s>>>(g, (const float*)f, part);
   else hd::phase_diag_kernel<double><<<blocks, 256, 0, s>>>(g, (const double*)f, part);
-  hd::diag_finish<<<1, 32, 0, s>>>(blocks, 3 + dv, part, res);
+  hd::diag_finish<<<1, 1024, 0, s>>>(blocks, 3 + dv, part, res);
   hd::energy_kernel<<<1, 1024, 0, s>>>(g, v->d_E, res + 8);
   int rc = vcuda(cudaGetLastError(), "vp diagnostics");
   if (rc) return rc;
@@ -895,11 +1020,15 @@ int hd_vp_fields(hd_vp* v, double* rho, double* phi, double* E, void* stream) {
 int hd_vp_cg_stats(const hd_vp* v, int* last_iterations, long long* total_iterations, long long* solves,
                    double* last_residual, long long* learned_picked) {
   if (!v) return vfail(HD_ERR_INVALID, "hd_vp_cg_stats: null handle");
-  if (learned_picked) *learned_picked = v->learned_picked;
-  if (last_iterations) *last_iterations = v->last_iters;
-  if (total_iterations) *total_iterations = v->total_iters;
-  if (solves) *solves = v->solves;
-  if (last_residual) *last_residual = v->last_res;
+  hd::VpStats st;
+  int rc = vcuda(cudaDeviceSynchronize(), "hd_vp_cg_stats: synchronize");
+  if (!rc) rc = vcuda(cudaMemcpy(&st, v->d_stats, sizeof(st), cudaMemcpyDeviceToHost), "hd_vp_cg_stats: copy");
+  if (rc) return rc;
+  if (learned_picked) *learned_picked = st.learned_picked;
+  if (last_iterations) *last_iterations = st.last_iters;
+  if (total_iterations) *total_iterations = st.total_iters;
+  if (solves) *solves = st.solves;
+  if (last_residual) *last_residual = st.last_res;
   return HD_OK;
 }
 
