@@ -23,7 +23,7 @@ EXPORTED_SYMBOLS = (
     "hd_adv_set_kernel", "hd_adv_kernel", "hd_adv_device_status", "hd_norm_and_error_noalloc",
     "hd_vp_create", "hd_vp_destroy", "hd_vp_n_dofs", "hd_vp_n_dofs_x", "hd_vp_interpolate", "hd_vp_solve_field",
     "hd_vp_apply", "hd_vp_lsrk_step", "hd_vp_diagnostics", "hd_vp_fields", "hd_vp_cg_stats", "hd_vp_set_guess",
-    "hd_vp_learn_loss_grad",
+    "hd_vp_learn_loss_grad", "hd_adv_set_tile", "hd_adv_tile_limits",
 )
 HD_KERNEL_AUTO, HD_KERNEL_GENERIC, HD_KERNEL_PIPELINED = 0, 1, 2
 HD_VP_GUESS_ZERO, HD_VP_GUESS_PREVIOUS, HD_VP_GUESS_LEARNED = 0, 1, 2
@@ -91,6 +91,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.hd_adv_set_kernel.argtypes = [vp, ctypes.c_int]
     L.hd_adv_kernel.argtypes = [vp]
     L.hd_adv_device_status.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+    L.hd_adv_set_tile.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    L.hd_adv_tile_limits.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.hd_adv_critical_time_step.argtypes = [vp]
     L.hd_adv_critical_time_step.restype = ctypes.c_double
     L.hd_interpolate.argtypes = [vp, ctypes.POINTER(hd_function), ctypes.c_double, vp, vp]

@@ -169,6 +169,16 @@ class AdvectionOperation:
         return {_lib.HD_KERNEL_GENERIC: "generic", _lib.HD_KERNEL_PIPELINED: "pipelined"}[
             int(self._L.hd_adv_kernel(self._h))]
 
+    def set_tile(self, cells_per_cta: int = 0, ctas_per_sm: int = 0) -> None:
+        """Tile of the generic kernel (hd_adv_set_tile); 0 = default."""
+        check(self._L.hd_adv_set_tile(self._h, int(cells_per_cta), int(ctas_per_sm)))
+
+    def tile_limits(self):
+        """(max cells per CTA, threads per cell) of the generic kernel for this operator."""
+        a, b = ctypes.c_int(0), ctypes.c_int(0)
+        check(self._L.hd_adv_tile_limits(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     def device_status(self) -> int:
         """Error code recorded by the device since the last call (0 = none); synchronises."""
         st = ctypes.c_int(0)

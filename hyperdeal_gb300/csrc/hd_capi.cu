@@ -404,6 +404,25 @@ int hd_adv_destroy(hd_adv* op) {
 
 long long hd_adv_n_dofs(const hd_adv* op) { return op ? op->n_dofs : -1; }
 
+int hd_adv_set_tile(hd_adv* op, int cells_per_cta, int ctas_per_sm) {
+  if (!op) return fail(HD_ERR_INVALID, "hd_adv_set_tile: null handle");
+  if (cells_per_cta < 0 || ctas_per_sm < 0 || ctas_per_sm > 32)
+    return fail(HD_ERR_INVALID, "hd_adv_set_tile: cells_per_cta >= 0, 0 <= ctas_per_sm <= 32");
+  op->p64.cpb = op->p32.cpb = cells_per_cta;
+  op->p64.ctas_per_sm = op->p32.ctas_per_sm = ctas_per_sm;
+  return HD_OK;
+}
+
+int hd_adv_tile_limits(const hd_adv* op, int* max_cells_per_cta, int* threads_per_cell) {
+  if (!op) return fail(HD_ERR_INVALID, "hd_adv_tile_limits: null handle");
+  const bool f64 = op->desc.dtype == HD_F64;
+  const int cpb = f64 ? op->launchers.cells_per_cta_f64 : op->launchers.cells_per_cta_f32;
+  const int thr = f64 ? op->launchers.threads_f64 : op->launchers.threads_f32;
+  if (max_cells_per_cta) *max_cells_per_cta = cpb;
+  if (threads_per_cell) *threads_per_cell = cpb > 0 ? thr / cpb : 0;
+  return HD_OK;
+}
+
 int hd_adv_set_kernel(hd_adv* op, int variant) {
   if (!op) return fail(HD_ERR_INVALID, "hd_adv_set_kernel: null handle");
   if (variant != HD_KERNEL_AUTO && variant != HD_KERNEL_GENERIC && variant != HD_KERNEL_PIPELINED)

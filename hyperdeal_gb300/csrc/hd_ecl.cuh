@@ -66,6 +66,8 @@ struct EclParams {
   double time;
   double lo[kMaxDim], h[kMaxDim];
   double gl[kMaxN];  // Gauss-Lobatto nodes on [0,1]
+  int cpb;           // generic kernel tile: cells per CTA (0 = the shape's maximum)
+  int ctas_per_sm;   //   and CTAs per SM of the persistent grid (0 = occupancy limit)
 };
 
 enum EclMode { kApply = 0, kStageFirst = 1, kStageMid = 2, kStageLast = 3 };
@@ -90,9 +92,9 @@ struct EclShape {
   static constexpr int TPC = NPLANE < TB ? NPLANE : TB;       // threads per cell
   static constexpr int CPB = TB / TPC > 0 ? TB / TPC : 1;     // cells per CTA
   static constexpr int THREADS = TPC * CPB;
-  static constexpr size_t SMEM = size_t(2) * CPB * NC * sizeof(T);
+  static constexpr size_t SMEM = size_t(3) * CPB * NC * sizeof(T);  // 2 staging buffers + accumulator
   static constexpr int NPH = (D + 1) / 2;                     // phases
-  static constexpr bool SUPPORTED = SMEM <= 200 * 1024;
+  static constexpr bool SUPPORTED = SMEM + 48 <= 220 * 1024;
 };
 
 // shared-memory index of node i (identity layout)
@@ -142,45 +144,56 @@ __device__ __forceinline__ T boundary_value(const EclParams<T>& P, const int* cc
   return T(-double(um) + 2.0 * eval_function(P.bc, x, D, P.time));
 }
 
-template <int D, int N, typename T, int MODE>
-__global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
-    ecl_kernel(const __grid_constant__ EclParams<T> P) {
-  using S = EclShape<D, N, T>;
-  constexpr int NC = S::NC, TPC = S::TPC, CPB = S::CPB;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* s_u = reinterpret_cast<T*>(smem_raw);
-  T* s_o = s_u + CPB * NC;
+// ---- asynchronous global -> shared copies (cp.async; the copies of a group
+// complete in order, so one group per cell block gives a two-stage pipeline)
+__device__ __forceinline__ void cp_async_16(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+template <int BYTES>
+__device__ __forceinline__ void cp_async_small(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory"); }
 
-  const int tid = threadIdx.x;
-  const int lc = tid / TPC, tl = tid % TPC;
-  const long long cell0 = (long long)blockIdx.x * CPB;
+// copy nval contiguous values to a 16-byte aligned shared buffer: 16-byte
+// copies when the global start is 16-byte aligned and the size a multiple
+// of 16 bytes, element copies otherwise
+template <typename T>
+__device__ __forceinline__ void stage_async(T* dst, const T* src, long long nval, int tid, int nthreads) {
+  if ((reinterpret_cast<uintptr_t>(src) & 15) == 0 && (nval * sizeof(T)) % 16 == 0) {
+    constexpr int VPV = 16 / sizeof(T);
+    const long long nvec = nval / VPV;
+    for (long long v = tid; v < nvec; v += nthreads) cp_async_16(dst + v * VPV, src + v * VPV);
+  } else {
+    for (long long i = tid; i < nval; i += nthreads) cp_async_small<sizeof(T)>(dst + i, src + i);
+  }
+}
+
+// shared-memory elements of one staging buffer (rounded to 16 bytes)
+template <int D, int N, typename T>
+__host__ __device__ __forceinline__ long long ecl_buffer_elems(int cpb) {
+  const long long bytes = (long long)cpb * EclShape<D, N, T>::NC * sizeof(T);
+  return ((bytes + 15) / 16) * 16 / (long long)sizeof(T);
+}
+
+// one block of P.cpb cells (the CTA's cells start at cell0) from the staged
+// input `su_all`: the D line operators two directions per phase, the last
+// phase writing K or the fused stage update
+template <int D, int N, typename T, int MODE>
+__device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0, int lc, int tl, const T* su_all,
+                                          T* so_all) {
+  using S = EclShape<D, N, T>;
+  constexpr int NC = S::NC, TPC = S::TPC;
+  // keep the RK solution values of a plane in registers from the start of the
+  // last phase (hides their latency behind the phase's arithmetic) when the
+  // registers allow it
+  constexpr bool kEarlyU = (N <= 4) && (MODE == kStageMid || MODE == kStageLast);
   const long long gid = cell0 + lc;
   const bool valid = gid < P.n_cells;
-  const long long ncell_here = (P.n_cells - cell0) < CPB ? (P.n_cells - cell0) : CPB;
-
-  // ---- stage the CTA's contiguous block of cells in shared memory
-  {
-    const T* src = P.tin + cell0 * NC;
-    const long long nval = ncell_here * NC;
-    if constexpr ((NC * sizeof(T)) % 16 == 0) {
-      constexpr int VPV = 16 / sizeof(T);
-      const long long nvec = nval / VPV;
-      const int4* s4 = reinterpret_cast<const int4*>(src);
-      for (long long v = tid; v < nvec; v += S::THREADS) {
-        const int4 x = __ldg(s4 + v);
-        const T* xv = reinterpret_cast<const T*>(&x);
-#pragma unroll
-        for (int j = 0; j < VPV; ++j) {
-          const long long i = v * VPV + j;
-          s_u[(i / NC) * NC + sidx<D, N, T>(int(i % NC))] = xv[j];
-        }
-      }
-    } else {
-      for (long long i = tid; i < nval; i += S::THREADS)
-        s_u[(i / NC) * NC + sidx<D, N, T>(int(i % NC))] = __ldg(src + i);
-    }
-  }
-  __syncthreads();
 
   // ---- cell coordinates
   int cc[D];
@@ -193,8 +206,8 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
       else { cc[d] = int(gv % P.cells[d]); gv /= P.cells[d]; }
     }
   }
-  T* su = s_u + lc * NC;
-  T* so = s_o + lc * NC;
+  const T* su = su_all + lc * NC;
+  T* so = so_all + lc * NC;
 
 #pragma unroll
   for (int ph = 0; ph < S::NPH; ++ph) {
@@ -204,64 +217,85 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
     const int strideB = strideA * N;
     const int nitems = dB >= 0 ? ipow(N, D - 2) : ipow(N, D - 1);
     const bool last = (ph == S::NPH - 1);
-    const long long nbA = valid && P.op[dA].active ? neighbour(P, gid, cc, dA) : -1;
-    const long long nbB = (dB >= 0 && valid && P.op[dB].active) ? neighbour(P, gid, cc, dB) : -1;
+    const bool actA = valid && P.op[dA].active;
+    const bool actB = dB >= 0 && valid && P.op[dB].active;
+    const long long nbA = actA ? neighbour(P, gid, cc, dA) : -1;
+    const long long nbB = actB ? neighbour(P, gid, cc, dB) : -1;
 
     for (int item = tl; item < nitems; item += TPC) {
       const int base = item_base<D, N>(item, dA, dB);
       if (dB >= 0) {
+        const LineOp<T>& LA = P.op[dA];
+        const LineOp<T>& LB = P.op[dB];
+        // upwind face values of the N lines of both directions, issued first
+        T upA[N], upB[N];
+#pragma unroll
+        for (int b = 0; b < N; ++b)
+          upA[b] = nbA >= 0 ? __ldg(P.tin + nbA * NC + base + LA.nb_node * strideA + b * strideB) : T(0);
+#pragma unroll
+        for (int a = 0; a < N; ++a)
+          upB[a] = nbB >= 0 ? __ldg(P.tin + nbB * NC + base + a * strideA + LB.nb_node * strideB) : T(0);
+        T uin[kEarlyU ? N : 1][kEarlyU ? N : 1];
+        if constexpr (kEarlyU) {
+          if (last && valid) {
+#pragma unroll
+            for (int a = 0; a < N; ++a)
+#pragma unroll
+              for (int b = 0; b < N; ++b) uin[a][b] = P.uin[gid * NC + base + a * strideA + b * strideB];
+          }
+        }
         T uu[N][N], acc[N][N];  // [a][b]: node base + a*strideA + b*strideB
 #pragma unroll
         for (int a = 0; a < N; ++a)
 #pragma unroll
           for (int b = 0; b < N; ++b) {
             const int node = base + a * strideA + b * strideB;
-            uu[a][b] = su[sidx<D, N, T>(node)];
-            acc[a][b] = ph == 0 ? T(0) : so[sidx<D, N, T>(node)];
+            uu[a][b] = su[node];
+            acc[a][b] = ph == 0 ? T(0) : so[node];
           }
-        if (valid && P.op[dA].active) {
-          const LineOp<T>& L = P.op[dA];
+        if (actA) {
 #pragma unroll
           for (int b = 0; b < N; ++b) {
 #pragma unroll
             for (int i = 0; i < N; ++i) {
               T s = acc[i][b];
 #pragma unroll
-              for (int q = 0; q < N; ++q) s = fma(L.M[i * N + q], uu[q][b], s);
+              for (int q = 0; q < N; ++q) s = fma(LA.M[i * N + q], uu[q][b], s);
               acc[i][b] = s;
             }
-            const bool first = L.in_node == 0;
-            const T um = first ? uu[0][b] : uu[N - 1][b];
-            const T up = nbA >= 0 ? __ldg(P.tin + nbA * NC + base + L.nb_node * strideA + b * strideB)
-                                  : boundary_value<D, N, T>(P, cc, dA, base + L.in_node * strideA + b * strideB, um);
-            acc[0][b] = fma(L.c0, up, acc[0][b]);
-            acc[N - 1][b] = fma(L.cl, up, acc[N - 1][b]);
+            T up = upA[b];
+            if (nbA < 0) {
+              const T um = LA.in_node == 0 ? uu[0][b] : uu[N - 1][b];
+              up = boundary_value<D, N, T>(P, cc, dA, base + LA.in_node * strideA + b * strideB, um);
+            }
+            acc[0][b] = fma(LA.c0, up, acc[0][b]);
+            acc[N - 1][b] = fma(LA.cl, up, acc[N - 1][b]);
           }
         }
-        if (valid && P.op[dB].active) {
-          const LineOp<T>& L = P.op[dB];
+        if (actB) {
 #pragma unroll
           for (int a = 0; a < N; ++a) {
 #pragma unroll
             for (int i = 0; i < N; ++i) {
               T s = acc[a][i];
 #pragma unroll
-              for (int q = 0; q < N; ++q) s = fma(L.M[i * N + q], uu[a][q], s);
+              for (int q = 0; q < N; ++q) s = fma(LB.M[i * N + q], uu[a][q], s);
               acc[a][i] = s;
             }
-            const bool first = L.in_node == 0;
-            const T um = first ? uu[a][0] : uu[a][N - 1];
-            const T up = nbB >= 0 ? __ldg(P.tin + nbB * NC + base + a * strideA + L.nb_node * strideB)
-                                  : boundary_value<D, N, T>(P, cc, dB, base + a * strideA + L.in_node * strideB, um);
-            acc[a][0] = fma(L.c0, up, acc[a][0]);
-            acc[a][N - 1] = fma(L.cl, up, acc[a][N - 1]);
+            T up = upB[a];
+            if (nbB < 0) {
+              const T um = LB.in_node == 0 ? uu[a][0] : uu[a][N - 1];
+              up = boundary_value<D, N, T>(P, cc, dB, base + a * strideA + LB.in_node * strideB, um);
+            }
+            acc[a][0] = fma(LB.c0, up, acc[a][0]);
+            acc[a][N - 1] = fma(LB.cl, up, acc[a][N - 1]);
           }
         }
         if (!last) {
 #pragma unroll
           for (int a = 0; a < N; ++a)
 #pragma unroll
-            for (int b = 0; b < N; ++b) so[sidx<D, N, T>(base + a * strideA + b * strideB)] = acc[a][b];
+            for (int b = 0; b < N; ++b) so[base + a * strideA + b * strideB] = acc[a][b];
         } else if (valid) {
           const long long g0 = gid * NC;
 #pragma unroll
@@ -273,7 +307,10 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
               if constexpr (MODE == kApply) {
                 P.uout[gi] = k;
               } else {
-                const T u = (MODE == kStageFirst) ? uu[a][b] : P.uin[gi];
+                T u;
+                if constexpr (MODE == kStageFirst) u = uu[a][b];
+                else if constexpr (kEarlyU) u = uin[kEarlyU ? a : 0][kEarlyU ? b : 0];
+                else u = P.uin[gi];
                 P.uout[gi] = fma(P.fb, k, u);
                 if constexpr (MODE != kStageLast) P.tout[gi] = fma(P.fa, k, u);
               }
@@ -281,31 +318,34 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
         }
       } else {
         // single-direction phase (odd D): lines along dA
+        const LineOp<T>& LA = P.op[dA];
+        const T upf = nbA >= 0 ? __ldg(P.tin + nbA * NC + base + LA.nb_node * strideA) : T(0);
         T uu[N], acc[N];
 #pragma unroll
         for (int a = 0; a < N; ++a) {
           const int node = base + a * strideA;
-          uu[a] = su[sidx<D, N, T>(node)];
-          acc[a] = ph == 0 ? T(0) : so[sidx<D, N, T>(node)];
+          uu[a] = su[node];
+          acc[a] = ph == 0 ? T(0) : so[node];
         }
-        if (valid && P.op[dA].active) {
-          const LineOp<T>& L = P.op[dA];
+        if (actA) {
 #pragma unroll
           for (int i = 0; i < N; ++i) {
             T s = acc[i];
 #pragma unroll
-            for (int q = 0; q < N; ++q) s = fma(L.M[i * N + q], uu[q], s);
+            for (int q = 0; q < N; ++q) s = fma(LA.M[i * N + q], uu[q], s);
             acc[i] = s;
           }
-          const T um = L.in_node == 0 ? uu[0] : uu[N - 1];
-          const T up = nbA >= 0 ? __ldg(P.tin + nbA * NC + base + L.nb_node * strideA)
-                                : boundary_value<D, N, T>(P, cc, dA, base + L.in_node * strideA, um);
-          acc[0] = fma(L.c0, up, acc[0]);
-          acc[N - 1] = fma(L.cl, up, acc[N - 1]);
+          T up = upf;
+          if (nbA < 0) {
+            const T um = LA.in_node == 0 ? uu[0] : uu[N - 1];
+            up = boundary_value<D, N, T>(P, cc, dA, base + LA.in_node * strideA, um);
+          }
+          acc[0] = fma(LA.c0, up, acc[0]);
+          acc[N - 1] = fma(LA.cl, up, acc[N - 1]);
         }
         if (!last) {
 #pragma unroll
-          for (int a = 0; a < N; ++a) so[sidx<D, N, T>(base + a * strideA)] = acc[a];
+          for (int a = 0; a < N; ++a) so[base + a * strideA] = acc[a];
         } else if (valid) {
           const long long g0 = gid * NC;
 #pragma unroll
@@ -327,22 +367,82 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
   }
 }
 
-// host launcher for one (D, N, T)
+// Persistent generic kernel: CTAs walk blocks of P.cpb cells with a stride of
+// the grid; the next block's input is staged by cp.async while the current
+// one is computed (two staging buffers + one accumulator tile).
+template <int D, int N, typename T, int MODE>
+__global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
+    ecl_kernel(const __grid_constant__ EclParams<T> P) {
+  using S = EclShape<D, N, T>;
+  constexpr int NC = S::NC, TPC = S::TPC;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int cpb = P.cpb;
+  const long long bufe = ecl_buffer_elems<D, N, T>(cpb);
+  T* const s_in0 = reinterpret_cast<T*>(smem_raw);
+  T* const s_in1 = s_in0 + bufe;
+  T* const s_o = s_in0 + 2 * bufe;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int lc = tid / TPC, tl = tid % TPC;
+  const long long nblk = (P.n_cells + cpb - 1) / cpb;
+  auto stage = [&](T* dst, long long blk) {
+    const long long c0 = blk * cpb;
+    const long long ncell = (P.n_cells - c0) < cpb ? (P.n_cells - c0) : cpb;
+    stage_async(dst, P.tin + c0 * NC, ncell * NC, tid, nthr);
+  };
+  long long b = blockIdx.x;
+  if (b < nblk) stage(s_in0, b);
+  cp_async_commit();
+  bool odd = false;
+  for (; b < nblk; b += gridDim.x) {
+    T* const cur = odd ? s_in1 : s_in0;
+    T* const nxt = odd ? s_in0 : s_in1;
+    const long long nb = b + gridDim.x;
+    if (nb < nblk) stage(nxt, nb);
+    cp_async_commit();
+    cp_async_wait<1>();  // this thread's copies of block b are complete
+    __syncthreads();     // ... and everybody's
+    ecl_block<D, N, T, MODE>(P, b * cpb, lc, tl, cur, s_o);
+    __syncthreads();     // cur and s_o are free for the next blocks
+    odd = !odd;
+  }
+  cp_async_wait<0>();
+}
+
+// host launcher for one (D, N, T): P.cpb cells per CTA (1..CPB; 0 = CPB) and
+// ctas_per_sm CTAs per SM (0 = as many as fit), persistent grid
 template <int D, int N, typename T>
-cudaError_t launch_ecl(const EclParams<T>& P, int mode, cudaStream_t stream) {
+cudaError_t launch_ecl(const EclParams<T>& P0, int mode, cudaStream_t stream) {
   using S = EclShape<D, N, T>;
   if constexpr (!S::SUPPORTED) {
     return cudaErrorNotSupported;
   } else {
+    EclParams<T> P = P0;
+    if (P.cpb < 1 || P.cpb > S::CPB) P.cpb = S::CPB;
+    const int threads = S::TPC * P.cpb;
+    const size_t smem = size_t(3 * ecl_buffer_elems<D, N, T>(P.cpb)) * sizeof(T);
+    // one flag per mode: the four kernels share this lambda's instantiation
     static bool attr_done[4] = {false, false, false, false};
-    const unsigned grid = unsigned((P.n_cells + S::CPB - 1) / S::CPB);
+    static int sms = 0;
     auto go = [&](auto kern) -> cudaError_t {
       if (!attr_done[mode]) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S::SMEM));
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(3 * ecl_buffer_elems<D, N, T>(S::CPB) * sizeof(T)));
         if (e != cudaSuccess) return e;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         attr_done[mode] = true;
       }
-      kern<<<grid, S::THREADS, S::SMEM, stream>>>(P);
+      int per_sm = P.ctas_per_sm;
+      if (per_sm < 1) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+      }
+      const long long nblk = (P.n_cells + P.cpb - 1) / P.cpb;
+      const long long want = (long long)sms * per_sm;
+      const unsigned grid = unsigned(nblk < want ? nblk : want);
+      kern<<<grid, threads, smem, stream>>>(P);
       return cudaGetLastError();
     };
     switch (mode) {

@@ -202,6 +202,7 @@ static cudaError_t launch_vp_dn(const VpAdvParams<T>& P, cudaStream_t s) {
   if constexpr (!S::SUPPORTED) {
     return cudaErrorNotSupported;
   } else {
+    constexpr size_t kSmem = size_t(2) * S::CPB * S::NC * sizeof(T);  // cell tile + accumulator tile
     VpLine<T> Lk;
     for (int i = 0; i < N * N; ++i) Lk.G[i] = T(P.g.G[i]);
     Lk.winv0 = T(1.0 / P.g.glw[0]);
@@ -209,12 +210,12 @@ static cudaError_t launch_vp_dn(const VpAdvParams<T>& P, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
       cudaError_t e = cudaFuncSetAttribute(vp_adv_kernel<D, N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           int(S::SMEM));
+                                           int(kSmem));
       if (e != cudaSuccess) return e;
       attr = true;
     }
     const unsigned grid = unsigned((P.g.n_cells + S::CPB - 1) / S::CPB);
-    vp_adv_kernel<D, N, T><<<grid, S::THREADS, S::SMEM, s>>>(P, Lk);
+    vp_adv_kernel<D, N, T><<<grid, S::THREADS, kSmem, s>>>(P, Lk);
     return cudaGetLastError();
   }
 }

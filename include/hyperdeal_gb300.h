@@ -110,6 +110,13 @@ int hd_adv_destroy(hd_adv *op);
 /* Number of DoFs = prod(cells) * (k+1)^(dim_x+dim_v). */
 long long hd_adv_n_dofs(const hd_adv *op);
 
+/* Tile of the generic kernel (the autotuner's knobs; no reference
+ * counterpart -- the reference's cell batching is fixed by VectorizedArray):
+ * cells per CTA (1..max, 0 = max) and CTAs per SM of the persistent grid
+ * (0 = as many as fit).  Results do not depend on the tile. */
+int hd_adv_set_tile(hd_adv *op, int cells_per_cta, int ctas_per_sm);
+int hd_adv_tile_limits(const hd_adv *op, int *max_cells_per_cta, int *threads_per_cell);
+
 /* Kernel selection: AUTO picks the persistent TMA-pipelined kernel where it
  * applies (FP32, degree 3, fully periodic 3x+3v mesh) and the generic
  * shared-memory kernel otherwise; GENERIC forces the latter.  Both compute
