@@ -24,6 +24,8 @@ EXPORTED_SYMBOLS = (
     "hd_vp_create", "hd_vp_destroy", "hd_vp_n_dofs", "hd_vp_n_dofs_x", "hd_vp_interpolate", "hd_vp_solve_field",
     "hd_vp_apply", "hd_vp_lsrk_step", "hd_vp_diagnostics", "hd_vp_fields", "hd_vp_cg_stats", "hd_vp_set_guess",
     "hd_vp_learn_loss_grad", "hd_adv_set_tile", "hd_adv_tile_limits",
+    "hd_batch_create", "hd_batch_destroy", "hd_batch_n_classes", "hd_batch_class_info", "hd_batch_set_tile",
+    "hd_batch_apply", "hd_batch_lsrk_step", "hd_batch_graph_capture", "hd_batch_graph_launch", "hd_batch_autotune",
 )
 HD_KERNEL_AUTO, HD_KERNEL_GENERIC, HD_KERNEL_PIPELINED = 0, 1, 2
 HD_VP_GUESS_ZERO, HD_VP_GUESS_PREVIOUS, HD_VP_GUESS_LEARNED = 0, 1, 2
@@ -125,6 +127,18 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.hd_vp_set_guess.argtypes = [vp, ctypes.c_int]
     L.hd_vp_learn_loss_grad.argtypes = [ctypes.c_longlong, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp,
                                         vp]
+    vpp = ctypes.POINTER(vp)
+    ip = ctypes.POINTER(ctypes.c_int)
+    L.hd_batch_create.argtypes = [vpp, ctypes.c_int, vp, vpp]
+    L.hd_batch_destroy.argtypes = [vp]
+    L.hd_batch_n_classes.argtypes = [vp]
+    L.hd_batch_class_info.argtypes = [vp, ctypes.c_int, ip, ip, ip, ip, ip, ip, ip]
+    L.hd_batch_set_tile.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.hd_batch_apply.argtypes = [vp, vpp, vpp, dp, vp]
+    L.hd_batch_lsrk_step.argtypes = [vp, vpp, vpp, vpp, dp, dp, vp]
+    L.hd_batch_graph_capture.argtypes = [vp, vpp, vpp, vpp, dp, dp]
+    L.hd_batch_graph_launch.argtypes = [vp, vp]
+    L.hd_batch_autotune.argtypes = [vp, vpp, vpp, ctypes.c_int, vp]
     _lib = L
     return L
 

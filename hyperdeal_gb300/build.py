@@ -2,7 +2,10 @@
 
 Every translation unit under ``csrc/`` is compiled for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``), in parallel, and linked with
-the shared CUDA runtime.  Objects are rebuilt when a source or header changes.
+the shared CUDA runtime.  The kernel templates are instantiated one
+(dimension, nodes per direction) pair per generated unit (``_build/gen/``,
+see ``csrc/hd_dispatch.cu``) so that the heavy instantiations compile in
+parallel.  Objects are rebuilt when a source or header changes.
 """
 from __future__ import annotations
 
@@ -40,9 +43,31 @@ def _deps_hash(extra: str = "") -> str:
     return h.hexdigest()
 
 
+# (family, header, factory) of the generated instantiation units and their (D, N) pairs
+GEN_UNITS = ([("ecl", "hd_ecl.cuh", "EclLaunchers", "make_launchers", D, N) for D in range(2, 7) for N in range(2, 7)]
+             + [("batch", "hd_batch.cuh", "BatchLaunchers", "make_batch_launchers", D, N)
+                for D in (4, 5) for N in range(3, 7)])
+
+
+def _generate_units() -> list:
+    gen = os.path.join(BUILD_DIR, "gen")
+    os.makedirs(gen, exist_ok=True)
+    out = []
+    for fam, header, ret, factory, D, N in GEN_UNITS:
+        path = os.path.join(gen, "%s_%d_%d.cu" % (fam, D, N))
+        text = ('#include "%s"\nnamespace hd {\n%s %s_launchers_%d_%d() { return %s<%d, %d>(); }\n}\n'
+                % (os.path.join(CSRC, header), ret, fam, D, N, factory, D, N))
+        if not os.path.exists(path) or open(path).read() != text:
+            with open(path, "w") as f:
+                f.write(text)
+        out.append(path)
+    return out
+
+
 def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> str:
     """Compile and link the library; returns its path."""
-    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu"))) + _generate_units()
     flags = ARCH + NVCC_FLAGS
     stamp = os.path.join(OUT_DIR, ".stamp")
     digest = _deps_hash(" ".join(flags))
@@ -53,17 +78,25 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
 
     def compile_one(src: str) -> str:
         obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
+        key = os.path.join(BUILD_DIR, os.path.basename(src) + ".key")
+        if not force and os.path.exists(obj) and os.path.exists(key) and open(key).read() == digest:
+            return obj
         cmd = [nvcc()] + flags + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))
         if verbose and (r.stdout or r.stderr):
             print(r.stdout + r.stderr)
+        with open(key, "w") as f:
+            f.write(digest)
         return obj
 
     jobs = jobs or min(len(sources), max(2, os.cpu_count() or 2))
+    # the slowest units first, so that they do not start last
+    order = sorted(sources, key=lambda p: (0 if os.path.basename(p).startswith(("ecl_5", "ecl_6", "batch_5"))
+                                           else 1 if os.path.basename(p).startswith(("ecl_4", "batch_4")) else 2))
     with ThreadPoolExecutor(max_workers=jobs) as ex:
-        objs = list(ex.map(compile_one, sources))
+        objs = list(ex.map(compile_one, order))
     tmp = LIB_PATH + ".tmp%d" % os.getpid()
     cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "shared", "-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -1,0 +1,153 @@
+// hd_batch.cuh -- many independent advection instances of one class
+// (phase-space dimension D, nodes per direction N, storage type T) advanced
+// by ONE persistent launch per stage.  The CTAs of the launch walk the
+// concatenated cell blocks of all instances of the class; each block is
+// computed with its own instance's parameters (mesh, line operators, stage
+// factors, vectors), and the next block -- of whichever instance -- is staged
+// by cp.async while the current one is computed, as in the single-instance
+// generic kernel (hd_ecl.cuh).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "hd_ecl.cuh"
+
+namespace hd {
+
+constexpr int kBatchMaxInstances = 256;
+
+// launch of the batch kernel for one class: params[i] are the instances'
+// stage parameters (device memory), prefix[i] = first cell block of instance i
+// (prefix[n] = total blocks), cpb cells per block, ctas_per_sm (0 = occupancy)
+template <typename T>
+struct BatchLaunch {
+  const EclParams<T>* params;
+  const long long* prefix;
+  int n;
+  int cpb;
+  int ctas_per_sm;
+};
+
+struct BatchLaunchers {
+  cudaError_t (*f64)(const BatchLaunch<double>&, int mode, cudaStream_t);
+  cudaError_t (*f32)(const BatchLaunch<float>&, int mode, cudaStream_t);
+  int max_cpb_f64, max_cpb_f32;
+  bool ok;
+};
+
+// classes with a batch kernel: D in {4, 5}, N in {3..6} (degree 2..5);
+// other classes return ok == false and are advanced per instance
+BatchLaunchers batch_launchers(int D, int N);
+BatchLaunchers batch_launchers_d4(int N);
+BatchLaunchers batch_launchers_d5(int N);
+
+template <int D, int N, typename T, int MODE>
+__global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
+    ecl_batch_kernel(const EclParams<T>* __restrict__ params, const long long* __restrict__ prefix, int n, int cpb) {
+  using S = EclShape<D, N, T>;
+  constexpr int NC = S::NC, TPC = S::TPC;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ long long s_prefix[kBatchMaxInstances + 1];
+  for (int i = threadIdx.x; i <= n; i += blockDim.x) s_prefix[i] = prefix[i];
+  __syncthreads();
+  const long long bufe = ecl_buffer_elems<D, N, T>(cpb);
+  T* const s_in0 = reinterpret_cast<T*>(smem_raw);
+  T* const s_in1 = s_in0 + bufe;
+  T* const s_o = s_in0 + 2 * bufe;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int lc = tid / TPC, tl = tid % TPC;
+  const long long total = s_prefix[n];
+  // instance of global block gb: the last i with prefix[i] <= gb
+  auto locate = [&](long long gb) -> int {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) / 2;
+      if (s_prefix[mid] <= gb) lo = mid;
+      else hi = mid - 1;
+    }
+    return lo;
+  };
+  auto stage = [&](T* dst, int inst, long long lb) {
+    const EclParams<T>& P = params[inst];
+    const long long c0 = lb * cpb;
+    const long long ncell = (P.n_cells - c0) < cpb ? (P.n_cells - c0) : cpb;
+    stage_async(dst, P.tin + c0 * NC, ncell * NC, tid, nthr);
+  };
+  long long b = blockIdx.x;
+  int inst = 0;
+  if (b < total) {
+    inst = locate(b);
+    stage(s_in0, inst, b - s_prefix[inst]);
+  }
+  cp_async_commit();
+  bool odd = false;
+  for (; b < total; b += gridDim.x) {
+    T* const cur = odd ? s_in1 : s_in0;
+    T* const nxt = odd ? s_in0 : s_in1;
+    const long long nb = b + gridDim.x;
+    int ninst = inst;
+    if (nb < total) {
+      ninst = locate(nb);
+      stage(nxt, ninst, nb - s_prefix[ninst]);
+    }
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    ecl_block<D, N, T, MODE>(params[inst], (b - s_prefix[inst]) * cpb, lc, tl, cur, s_o);
+    __syncthreads();
+    odd = !odd;
+    inst = ninst;
+  }
+  cp_async_wait<0>();
+}
+
+template <int D, int N, typename T>
+cudaError_t launch_batch(const BatchLaunch<T>& L, int mode, cudaStream_t stream) {
+  using S = EclShape<D, N, T>;
+  if constexpr (!S::SUPPORTED) {
+    return cudaErrorNotSupported;
+  } else {
+    if (L.n < 1 || L.n > kBatchMaxInstances) return cudaErrorInvalidValue;
+    const int cpb = (L.cpb < 1 || L.cpb > S::CPB) ? S::CPB : L.cpb;
+    const int threads = S::TPC * cpb;
+    const size_t smem = size_t(3 * ecl_buffer_elems<D, N, T>(cpb)) * sizeof(T);
+    static bool attr_done[4] = {false, false, false, false};
+    static int sms = 0;
+    auto go = [&](auto kern) -> cudaError_t {
+      if (!attr_done[mode]) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(3 * ecl_buffer_elems<D, N, T>(S::CPB) * sizeof(T)));
+        if (e != cudaSuccess) return e;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        attr_done[mode] = true;
+      }
+      int per_sm = L.ctas_per_sm;
+      if (per_sm < 1) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+      }
+      const unsigned grid = unsigned((long long)sms * per_sm);
+      kern<<<grid, threads, smem, stream>>>(L.params, L.prefix, L.n, cpb);
+      return cudaGetLastError();
+    };
+    switch (mode) {
+      case kApply: return go(ecl_batch_kernel<D, N, T, kApply>);
+      case kStageFirst: return go(ecl_batch_kernel<D, N, T, kStageFirst>);
+      case kStageMid: return go(ecl_batch_kernel<D, N, T, kStageMid>);
+      case kStageLast: return go(ecl_batch_kernel<D, N, T, kStageLast>);
+      default: return cudaErrorInvalidValue;
+    }
+  }
+}
+
+template <int D, int N>
+BatchLaunchers make_batch_launchers() {
+  return BatchLaunchers{&launch_batch<D, N, double>, &launch_batch<D, N, float>, EclShape<D, N, double>::CPB,
+                        EclShape<D, N, float>::CPB,
+                        EclShape<D, N, double>::SUPPORTED && EclShape<D, N, float>::SUPPORTED};
+}
+
+}  // namespace hd

@@ -15,6 +15,7 @@
 
 #include "../../include/hyperdeal_gb300.h"
 #include "hd_ecl.cuh"
+#include "hd_internal.h"
 #include "hd_vector.cuh"
 
 namespace {
@@ -133,11 +134,7 @@ void line_operator(int n, const double* w, const double* D, double a, double h, 
   }
 }
 
-struct LineOpD {
-  double M[hd::kMaxN * hd::kMaxN];
-  double cin;
-  int in_node, nb_node, step, active;
-};
+
 
 // linear operator coefficients by probing line_operator with unit inputs
 bool derive_line_op(int n, const double* w, const double* D, double a, double h, double s, LineOpD* op) {
@@ -190,30 +187,7 @@ namespace hd {
 void set_last_error(const char* msg) { g_last_error = msg; }
 }  // namespace hd
 
-struct hd_adv {
-  hd_adv_desc desc;
-  int D, N, NC, dtype;
-  long long n_cells, n_dofs, ncx;
-  double lo[HD_MAX_DIM], hi[HD_MAX_DIM], h[HD_MAX_DIM];
-  int cells[HD_MAX_DIM], periodic[HD_MAX_DIM];
-  double gl[hd::kMaxN], glw[hd::kMaxN], Dm[hd::kMaxN * hd::kMaxN];
-  LineOpD ops[HD_MAX_DIM];
-  hd::EclLaunchers launchers;
-  hd::EclParams<double> p64;
-  hd::EclParams<float> p32;
-  hd::VecGeom geom;
-  double* d_partials;  // norm reduction scratch (2*kNormBlocks + 2 doubles) + error flag
-  int* d_err;          // device error flag of the pipelined kernel (inside d_partials)
-  double* d_table;     // factor table of product functions (sum_d cells_d * (k+1) doubles)
-  int device;
-  int variant;         // HD_KERNEL_AUTO / _GENERIC / _PIPELINED
-};
 
-struct hd_lsrk {
-  char type[8];
-  int ns;
-  double ai[16], bi[16], ci[16];
-};
 
 namespace {
 
@@ -291,6 +265,13 @@ int launch(hd_adv* op, int mode, const void* tin, const void* uin, void* uout, v
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 }  // namespace
+
+namespace hd {
+int adv_launch(hd_adv* op, int mode, const void* tin, const void* uin, void* uout, void* tout, double fb, double fa,
+               double time, cudaStream_t s) {
+  return launch(op, mode, tin, uin, uout, tout, fb, fa, time, s);
+}
+}  // namespace hd
 
 extern "C" {
 

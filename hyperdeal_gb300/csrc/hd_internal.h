@@ -1,0 +1,47 @@
+// hd_internal.h -- library-internal definitions shared by the C ABI
+// translation units (hd_capi.cu, hd_batch.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/hyperdeal_gb300.h"
+#include "hd_ecl.cuh"
+#include "hd_vector.cuh"
+
+// per-direction line operator in FP64 (see derive_line_op in hd_capi.cu)
+struct LineOpD {
+  double M[hd::kMaxN * hd::kMaxN];
+  double cin;
+  int in_node, nb_node, step, active;
+};
+
+struct hd_adv {
+  hd_adv_desc desc;
+  int D, N, NC, dtype;
+  long long n_cells, n_dofs, ncx;
+  double lo[HD_MAX_DIM], hi[HD_MAX_DIM], h[HD_MAX_DIM];
+  int cells[HD_MAX_DIM], periodic[HD_MAX_DIM];
+  double gl[hd::kMaxN], glw[hd::kMaxN], Dm[hd::kMaxN * hd::kMaxN];
+  LineOpD ops[HD_MAX_DIM];
+  hd::EclLaunchers launchers;
+  hd::EclParams<double> p64;
+  hd::EclParams<float> p32;
+  hd::VecGeom geom;
+  double* d_partials;  // norm reduction scratch (2*kNormBlocks + 2 doubles) + error flag
+  int* d_err;          // device error flag of the pipelined kernel (inside d_partials)
+  double* d_table;     // factor table of product functions (sum_d cells_d * (k+1) doubles)
+  int device;
+  int variant;         // HD_KERNEL_AUTO / _GENERIC / _PIPELINED
+};
+
+struct hd_lsrk {
+  char type[8];
+  int ns;
+  double ai[16], bi[16], ci[16];
+};
+
+namespace hd {
+// one stage launch of an operator (the kernel hd_adv_kernel reports)
+int adv_launch(hd_adv* op, int mode, const void* tin, const void* uin, void* uout, void* tout, double fb, double fa,
+               double time, cudaStream_t s);
+}  // namespace hd

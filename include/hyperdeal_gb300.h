@@ -203,6 +203,43 @@ int hd_lsrk_stage_update(int dtype, long long n, double factor_bi, double factor
  * stage times c_s (n_stages values, c_0 = 0). */
 int hd_lsrk_coefficients(const hd_lsrk *rk, double *ai, double *bi, double *ci);
 
+/* ---- batched uneven instances --------------------------------------------- */
+
+/* Many independent advection problems (any dimension split, degree, velocity,
+ * mesh, dtype) advanced together.  The reference runs such problems one
+ * after the other (examples/advection/advection.cc:253-259), each with its
+ * own compile-time (dim, degree) instantiation (:26-48).  Here instances are
+ * grouped by class (dim_x + dim_v, degree, dtype); a class with a batch
+ * kernel (dim_x + dim_v in {4, 5}, degree 2..5) runs as ONE persistent launch
+ * per RK stage over all its instances, other classes launch per instance.
+ * The scheme is fixed at creation; the handle keeps pointers to the
+ * operators (they must outlive it).  Results equal the per-instance
+ * hd_lsrk_step / hd_adv_apply. */
+typedef struct hd_batch hd_batch;
+
+int hd_batch_create(hd_adv *const *ops, int n_ops, const hd_lsrk *rk, hd_batch **out);
+int hd_batch_destroy(hd_batch *b);
+int hd_batch_n_classes(const hd_batch *b);
+int hd_batch_class_info(const hd_batch *b, int cls, int *dim, int *degree, int *dtype, int *n_members, int *batched,
+                        int *cells_per_cta, int *ctas_per_sm);
+/* tile of class cls (-1: all classes); 0 = default */
+int hd_batch_set_tile(hd_batch *b, int cls, int cells_per_cta, int ctas_per_sm);
+/* dst[i] = A_i src[i] at time[i] (time may be NULL: 0) */
+int hd_batch_apply(hd_batch *b, void *const *dst, const void *const *src, const double *time, void *stream);
+/* one fused LSRK step of every instance: arrays of n_ops vectors, permuted
+ * per instance on return exactly like hd_lsrk_step's */
+int hd_batch_lsrk_step(hd_batch *b, void **sol, void **Ki, void **Ti, const double *time, const double *dt,
+                       void *stream);
+/* record TWO steps of every instance (after which the three vectors of each
+ * instance are back in their roles) as a CUDA graph; replays advance the
+ * stage times on the device.  hd_batch_lsrk_step invalidates the graph. */
+int hd_batch_graph_capture(hd_batch *b, void *const *sol, void *const *Ki, void *const *Ti, const double *time,
+                           const double *dt);
+int hd_batch_graph_launch(hd_batch *b, void *stream);
+/* autotuner: per class, time apply launches (src read, dst overwritten) for
+ * candidate tiles and keep the fastest */
+int hd_batch_autotune(hd_batch *b, const void *const *src, void *const *dst, int reps, void *stream);
+
 /* ---- Vlasov-Poisson ------------------------------------------------------- */
 
 /* Electrostatic Vlasov-Poisson on periodic x- and v-meshes (dim_x == dim_v),
