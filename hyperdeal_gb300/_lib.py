@@ -14,6 +14,7 @@ MAX_DIM = 6
 HD_OK, HD_ERR_INVALID, HD_ERR_UNSUPPORTED, HD_ERR_CUDA, HD_ERR_ALLOC, HD_ERR_DEVICE = range(6)
 HD_F64, HD_F32 = 0, 1
 HD_BC_HOMOGENEOUS, HD_BC_FUNCTION = 0, 1
+HD_QUAD_GAUSS_LOBATTO, HD_QUAD_GAUSS = 0, 1
 
 #: every symbol the C header declares
 EXPORTED_SYMBOLS = (
@@ -26,6 +27,7 @@ EXPORTED_SYMBOLS = (
     "hd_vp_learn_loss_grad", "hd_adv_set_tile", "hd_adv_tile_limits",
     "hd_batch_create", "hd_batch_destroy", "hd_batch_n_classes", "hd_batch_class_info", "hd_batch_set_tile",
     "hd_batch_apply", "hd_batch_lsrk_step", "hd_batch_graph_capture", "hd_batch_graph_launch", "hd_batch_autotune",
+    "hd_adv_autotune",
 )
 HD_KERNEL_AUTO, HD_KERNEL_GENERIC, HD_KERNEL_PIPELINED = 0, 1, 2
 HD_VP_GUESS_ZERO, HD_VP_GUESS_PREVIOUS, HD_VP_GUESS_LEARNED = 0, 1, 2
@@ -51,7 +53,7 @@ class hd_adv_desc(ctypes.Structure):
                 ("lo_v", ctypes.c_double * 3), ("hi_v", ctypes.c_double * 3),
                 ("periodic_x", ctypes.c_int), ("periodic_v", ctypes.c_int),
                 ("velocity", ctypes.c_double * MAX_DIM), ("skew", ctypes.c_double),
-                ("bc_kind", ctypes.c_int), ("bc", hd_function)]
+                ("bc_kind", ctypes.c_int), ("bc", hd_function), ("quadrature", ctypes.c_int)]
 
 
 class hd_vp_desc(ctypes.Structure):
@@ -94,6 +96,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.hd_adv_kernel.argtypes = [vp]
     L.hd_adv_device_status.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     L.hd_adv_set_tile.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    L.hd_adv_autotune.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                  dp, vp]
     L.hd_adv_tile_limits.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.hd_adv_critical_time_step.argtypes = [vp]
     L.hd_adv_critical_time_step.restype = ctypes.c_double

@@ -75,6 +75,7 @@ class AdvectionParameters:
     skew: float = 0.0
     dtype: str = "f64"
     boundary: Optional[Function] = None  # None: homogeneous Dirichlet on non-periodic faces
+    quadrature: str = "gauss_lobatto"  # "gauss_lobatto" (collocation) or "gauss"
 
     def c(self) -> _lib.hd_adv_desc:
         d = _lib.hd_adv_desc()
@@ -96,6 +97,7 @@ class AdvectionParameters:
         if self.boundary is not None:
             d.bc_kind = _lib.HD_BC_FUNCTION
             d.bc = self.boundary.c()
+        d.quadrature = {"gauss_lobatto": _lib.HD_QUAD_GAUSS_LOBATTO, "gauss": _lib.HD_QUAD_GAUSS}[self.quadrature]
         return d
 
 
@@ -172,6 +174,15 @@ class AdvectionOperation:
     def set_tile(self, cells_per_cta: int = 0, ctas_per_sm: int = 0) -> None:
         """Tile of the generic kernel (hd_adv_set_tile); 0 = default."""
         check(self._L.hd_adv_set_tile(self._h, int(cells_per_cta), int(ctas_per_sm)))
+
+    def autotune(self, src: torch.Tensor, dst: torch.Tensor, reps: int = 3) -> dict:
+        """Time candidate tiles with apply launches (src read, dst overwritten) and keep the fastest."""
+        self._check_vec(src, "src")
+        self._check_vec(dst, "dst")
+        c, p, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0.0)
+        check(self._L.hd_adv_autotune(self._h, _ptr(src), _ptr(dst), int(reps), ctypes.byref(c), ctypes.byref(p),
+                                      ctypes.byref(ms), _stream()))
+        return {"cells_per_cta": c.value, "ctas_per_sm": p.value, "ms_per_apply": ms.value}
 
     def tile_limits(self):
         """(max cells per CTA, threads per cell) of the generic kernel for this operator."""

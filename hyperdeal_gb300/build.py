@@ -46,7 +46,9 @@ def _deps_hash(extra: str = "") -> str:
 # (family, header, factory) of the generated instantiation units and their (D, N) pairs
 GEN_UNITS = ([("ecl", "hd_ecl.cuh", "EclLaunchers", "make_launchers", D, N) for D in range(2, 7) for N in range(2, 7)]
              + [("batch", "hd_batch.cuh", "BatchLaunchers", "make_batch_launchers", D, N)
-                for D in (4, 5) for N in range(3, 7)])
+                for D in (4, 5) for N in range(3, 7)]
+             + [("gauss", "hd_gauss.cuh", "GaussLaunchers", "make_gauss_launchers", D, N)
+                for D in range(2, 7) for N in range(2, 6)])
 
 
 def _generate_units() -> list:

@@ -28,7 +28,7 @@ namespace hd {
 BatchLaunchers batch_launchers(int D, int N) {
   if (D == 4) return batch_launchers_d4(N);
   if (D == 5) return batch_launchers_d5(N);
-  return BatchLaunchers{nullptr, nullptr, 0, 0, false};
+  return BatchLaunchers{nullptr, nullptr, 0, 0, 0, 0, false};
 }
 
 namespace {
@@ -47,7 +47,7 @@ __global__ void advance_time_kernel(EclParams<T>* slots, int n_slots, int n, con
 namespace {
 
 struct BatchClass {
-  int D, N, dtype;
+  int D, N, dtype, gauss;
   std::vector<int> members;  // instance indices
   bool batched;              // one launch per stage for the whole class
   hd::BatchLaunchers L;
@@ -232,15 +232,16 @@ int hd_batch_create(hd_adv* const* ops, int n, const hd_lsrk* rk, hd_batch** out
   for (int i = 0; i < n; ++i) {
     const hd_adv* op = ops[i];
     auto it = std::find_if(b->classes.begin(), b->classes.end(), [&](const BatchClass& c) {
-      return c.D == op->D && c.N == op->N && c.dtype == op->dtype;
+      return c.D == op->D && c.N == op->N && c.dtype == op->dtype && c.gauss == op->gauss;
     });
     if (it == b->classes.end()) {
       BatchClass c;
       c.D = op->D;
       c.N = op->N;
       c.dtype = op->dtype;
+      c.gauss = op->gauss;
       c.L = hd::batch_launchers(op->D, op->N);
-      c.batched = c.L.ok;
+      c.batched = c.L.ok && !op->gauss;  // the batch kernel is the collocation operator
       c.cpb = 0;
       c.per_sm = 0;
       c.d_prefix = nullptr;
@@ -297,7 +298,8 @@ int hd_batch_set_tile(hd_batch* b, int c, int cells_per_cta, int ctas_per_sm) {
     if (c >= 0 && ci != c) continue;
     BatchClass& k = b->classes[ci];
     const int maxc = k.dtype == HD_F64 ? k.L.max_cpb_f64 : k.L.max_cpb_f32;
-    k.cpb = (cells_per_cta < 1 || cells_per_cta > maxc) ? maxc : cells_per_cta;
+    const int defc = k.dtype == HD_F64 ? k.L.def_cpb_f64 : k.L.def_cpb_f32;
+    k.cpb = (cells_per_cta < 1 || cells_per_cta > maxc) ? defc : cells_per_cta;
     k.per_sm = ctas_per_sm;
     if (!k.batched) {
       for (int m : k.members) hd_adv_set_tile(b->ops[m], cells_per_cta, ctas_per_sm);

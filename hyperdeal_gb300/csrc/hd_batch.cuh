@@ -32,6 +32,7 @@ struct BatchLaunchers {
   cudaError_t (*f64)(const BatchLaunch<double>&, int mode, cudaStream_t);
   cudaError_t (*f32)(const BatchLaunch<float>&, int mode, cudaStream_t);
   int max_cpb_f64, max_cpb_f32;
+  int def_cpb_f64, def_cpb_f32;  // default tiles (ecl_default_cpb)
   bool ok;
 };
 
@@ -108,7 +109,7 @@ cudaError_t launch_batch(const BatchLaunch<T>& L, int mode, cudaStream_t stream)
     return cudaErrorNotSupported;
   } else {
     if (L.n < 1 || L.n > kBatchMaxInstances) return cudaErrorInvalidValue;
-    const int cpb = (L.cpb < 1 || L.cpb > S::CPB) ? S::CPB : L.cpb;
+    const int cpb = (L.cpb < 1 || L.cpb > S::CPB) ? ecl_default_cpb<D, N, T>() : L.cpb;
     const int threads = S::TPC * cpb;
     const size_t smem = size_t(3 * ecl_buffer_elems<D, N, T>(cpb)) * sizeof(T);
     static bool attr_done[4] = {false, false, false, false};
@@ -146,7 +147,7 @@ cudaError_t launch_batch(const BatchLaunch<T>& L, int mode, cudaStream_t stream)
 template <int D, int N>
 BatchLaunchers make_batch_launchers() {
   return BatchLaunchers{&launch_batch<D, N, double>, &launch_batch<D, N, float>, EclShape<D, N, double>::CPB,
-                        EclShape<D, N, float>::CPB,
+                        EclShape<D, N, float>::CPB, ecl_default_cpb<D, N, double>(), ecl_default_cpb<D, N, float>(),
                         EclShape<D, N, double>::SUPPORTED && EclShape<D, N, float>::SUPPORTED};
 }
 

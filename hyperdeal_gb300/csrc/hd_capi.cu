@@ -12,6 +12,8 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
+#include <algorithm>
 
 #include "../../include/hyperdeal_gb300.h"
 #include "hd_ecl.cuh"
@@ -102,6 +104,129 @@ void lagrange_derivative_matrix(int n, const double* x, double* D) {
       }
       D[q * n + j] = s;
     }
+}
+
+// Gauss rule with n points on [0,1]: roots of P_n (Newton), w = 1/((1-z^2) P_n'(z)^2)
+void gauss_rule(int n, double* x, double* w) {
+  for (int i = 0; i < n; ++i) {
+    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5));
+    double p = 0.0, dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      legendre(n, z, &p, &dp);
+      const double dz = p / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-17) break;
+    }
+    legendre(n, z, &p, &dp);
+    x[n - 1 - i] = 0.5 * (1.0 + z);
+    w[n - 1 - i] = 1.0 / ((1.0 - z * z) * dp * dp);
+  }
+  for (int i = 0; i < n / 2; ++i) {  // exact symmetry
+    const double xs = 0.5 * (x[i] + (1.0 - x[n - 1 - i]));
+    const double ws = 0.5 * (w[i] + w[n - 1 - i]);
+    x[i] = xs;
+    x[n - 1 - i] = 1.0 - xs;
+    w[i] = ws;
+    w[n - 1 - i] = ws;
+  }
+  if (n % 2) x[n / 2] = 0.5;
+}
+
+// L_j(t) of the Lagrange basis on the nodes x
+double lagrange_value(int n, const double* x, int j, double t) {
+  double v = 1.0;
+  for (int m = 0; m < n; ++m)
+    if (m != j) v *= (t - x[m]) / (x[j] - x[m]);
+  return v;
+}
+
+// inverse of an n x n matrix by Gauss-Jordan with partial pivoting
+bool invert(int n, const double* A, double* Ai) {
+  double a[hd::kMaxN][2 * hd::kMaxN];
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < 2 * n; ++j) a[i][j] = j < n ? A[i * n + j] : (j - n == i ? 1.0 : 0.0);
+  for (int c = 0; c < n; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < n; ++r)
+      if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+    if (std::fabs(a[piv][c]) < 1e-300) return false;
+    for (int j = 0; j < 2 * n; ++j) std::swap(a[c][j], a[piv][j]);
+    const double inv = 1.0 / a[c][c];
+    for (int j = 0; j < 2 * n; ++j) a[c][j] *= inv;
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      const double f = a[r][c];
+      for (int j = 0; j < 2 * n; ++j) a[r][j] -= f * a[c][j];
+    }
+  }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) Ai[i * n + j] = a[i][n + j];
+  return true;
+}
+
+// The same line operator in the Lagrange basis of the Gauss points (weights
+// w, derivative matrix D), whose face values are the interpolations
+// l0 . v, l1 . v and whose test functions take the values l0[i], l1[i] on
+// the faces (advection_operation.h:294-316, :426-449, :459-482 with
+// Gauss quadrature); the result is divided by the diagonal Gauss mass.
+void line_operator_gauss(int n, const double* w, const double* D, const double* l0, const double* l1, double a,
+                         double h, double s, const double* u, double uL, double uR, double* out) {
+  for (int i = 0; i < n; ++i) {
+    double vol = 0.0, skw = 0.0;
+    for (int q = 0; q < n; ++q) vol += D[q * n + i] * w[q] * u[q];
+    for (int j = 0; j < n; ++j) skw += D[i * n + j] * u[j];
+    out[i] = (1.0 - s) * (a / h) * vol / w[i] - s * (a / h) * skw;
+  }
+  double um0 = 0.0, um1 = 0.0;
+  for (int j = 0; j < n; ++j) {
+    um0 += l0[j] * u[j];
+    um1 += l1[j] * u[j];
+  }
+  {
+    const double an = -a;
+    const double flux = 0.5 * ((um0 + uL) * an + std::fabs(an) * (um0 - uL));
+    for (int i = 0; i < n; ++i) out[i] += -(flux - s * um0 * an) * l0[i] / (h * w[i]);
+  }
+  {
+    const double an = a;
+    const double flux = 0.5 * ((um1 + uR) * an + std::fabs(an) * (um1 - uR));
+    for (int i = 0; i < n; ++i) out[i] += -(flux - s * um1 * an) * l1[i] / (h * w[i]);
+  }
+}
+
+// M (Gauss basis), the inflow vector cv and the own inflow-face vector le
+bool derive_line_op_gauss(int n, const GaussTables& T, double a, double h, double s, LineOpD* op, double* cv,
+                          double* le) {
+  double u[hd::kMaxN], out[hd::kMaxN];
+  bool any = false;
+  for (int q = 0; q < n; ++q) {
+    for (int j = 0; j < n; ++j) u[j] = (j == q);
+    line_operator_gauss(n, T.w, T.D, T.l0, T.l1, a, h, s, u, 0.0, 0.0, out);
+    for (int i = 0; i < n; ++i) {
+      op->M[i * n + q] = out[i];
+      any = any || out[i] != 0.0;
+    }
+  }
+  for (int j = 0; j < n; ++j) u[j] = 0.0;
+  double cL[hd::kMaxN], cR[hd::kMaxN];
+  line_operator_gauss(n, T.w, T.D, T.l0, T.l1, a, h, s, u, 1.0, 0.0, cL);
+  line_operator_gauss(n, T.w, T.D, T.l0, T.l1, a, h, s, u, 0.0, 1.0, cR);
+  bool anyL = false, anyR = false;
+  for (int i = 0; i < n; ++i) {
+    anyL = anyL || cL[i] != 0.0;
+    anyR = anyR || cR[i] != 0.0;
+  }
+  if (anyL && anyR) return false;  // not a one-sided upwind flux
+  if (anyR) {
+    op->step = +1; op->in_node = n - 1; op->nb_node = 0;
+    for (int i = 0; i < n; ++i) { cv[i] = cR[i]; le[i] = T.l1[i]; }
+  } else {
+    op->step = -1; op->in_node = 0; op->nb_node = n - 1;
+    for (int i = 0; i < n; ++i) { cv[i] = cL[i]; le[i] = T.l0[i]; }
+  }
+  op->cin = 0.0;
+  op->active = any || anyL || anyR;
+  return true;
 }
 
 // The reference's operator restricted to one line of n nodes along direction d
@@ -234,7 +359,7 @@ hd::EclLaunchers get_launchers(int D, int N) {
 
 // kernel that runs for this operator (HD_KERNEL_GENERIC or HD_KERNEL_PIPELINED)
 int selected_kernel(const hd_adv* op) {
-  const bool pipelined_ok = op->dtype == HD_F32 && op->N == 4 && hd::ecl6_eligible(op->p32);
+  const bool pipelined_ok = !op->gauss && op->dtype == HD_F32 && op->N == 4 && hd::ecl6_eligible(op->p32);
   if (op->variant == HD_KERNEL_GENERIC) return HD_KERNEL_GENERIC;
   return pipelined_ok ? HD_KERNEL_PIPELINED : HD_KERNEL_GENERIC;
 }
@@ -242,7 +367,19 @@ int selected_kernel(const hd_adv* op) {
 int launch(hd_adv* op, int mode, const void* tin, const void* uin, void* uout, void* tout, double fb,
            double fa, double time, cudaStream_t s) {
   cudaError_t e;
-  if (selected_kernel(op) == HD_KERNEL_PIPELINED) {
+  if (op->gauss) {
+    if (op->dtype == HD_F64) {
+      hd::EclParams<double> P = op->p64;
+      P.tin = (const double*)tin; P.uin = (const double*)uin; P.uout = (double*)uout; P.tout = (double*)tout;
+      P.fb = fb; P.fa = fa; P.time = time;
+      e = op->glaunch.f64(P, op->g64, mode, s);
+    } else {
+      hd::EclParams<float> P = op->p32;
+      P.tin = (const float*)tin; P.uin = (const float*)uin; P.uout = (float*)uout; P.tout = (float*)tout;
+      P.fb = float(fb); P.fa = float(fa); P.time = time;
+      e = op->glaunch.f32(P, op->g32, mode, s);
+    }
+  } else if (selected_kernel(op) == HD_KERNEL_PIPELINED) {
     hd::EclParams<float> P = op->p32;
     P.tin = (const float*)tin; P.uin = (const float*)uin; P.uout = (float*)uout; P.tout = (float*)tout;
     P.fb = float(fb); P.fa = float(fa); P.time = time;
@@ -296,8 +433,10 @@ int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
     if (d.degree < 1 || d.degree + 1 > hd::kMaxN)
       return fail(HD_ERR_UNSUPPORTED, "degree %d not built (1..%d)", d.degree, hd::kMaxN - 1);
     if (d.n_points != d.degree + 1)
-      return fail(HD_ERR_UNSUPPORTED, "n_points must equal degree+1 (Gauss-Lobatto collocation), got %d",
+      return fail(HD_ERR_UNSUPPORTED, "n_points must equal degree+1, got %d (over-integration is not built)",
                   d.n_points);
+    if (d.quadrature != HD_QUAD_GAUSS_LOBATTO && d.quadrature != HD_QUAD_GAUSS)
+      return fail(HD_ERR_INVALID, "unknown quadrature %d", d.quadrature);
     if (d.dtype != HD_F64 && d.dtype != HD_F32) return fail(HD_ERR_INVALID, "unknown dtype %d", d.dtype);
     if (d.bc_kind != HD_BC_HOMOGENEOUS && d.bc_kind != HD_BC_FUNCTION)
       return fail(HD_ERR_INVALID, "unknown bc_kind %d", d.bc_kind);
@@ -335,11 +474,52 @@ int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
     op->n_dofs = op->n_cells * op->NC;
     gauss_lobatto(op->N, op->gl, op->glw);
     lagrange_derivative_matrix(op->N, op->gl, op->Dm);
-    for (int i = 0; i < op->D; ++i)
-      if (!derive_line_op(op->N, op->glw, op->Dm, d.velocity[i], op->h[i], d.skew, &op->ops[i])) {
-        delete op;
-        return fail(HD_ERR_UNSUPPORTED, "direction %d: flux is not one-sided upwind", i);
+    op->gauss = d.quadrature == HD_QUAD_GAUSS;
+    if (op->gauss) {
+      GaussTables& T = op->gt;
+      const int n = op->N;
+      gauss_rule(n, T.x, T.w);
+      lagrange_derivative_matrix(n, T.x, T.D);
+      for (int i = 0; i < n; ++i) {
+        T.l0[i] = lagrange_value(n, T.x, i, 0.0);
+        T.l1[i] = lagrange_value(n, T.x, i, 1.0);
+        for (int j = 0; j < n; ++j) T.S[i * n + j] = lagrange_value(n, op->gl, j, T.x[i]);
       }
+      if (!invert(n, T.S, T.Si)) { delete op; return fail(HD_ERR_INVALID, "basis change is singular"); }
+      double cv[hd::kMaxN], le[hd::kMaxN];
+      for (int i = 0; i < op->D; ++i) {
+        if (!derive_line_op_gauss(n, T, d.velocity[i], op->h[i], d.skew, &op->ops[i], cv, le)) {
+          delete op;
+          return fail(HD_ERR_UNSUPPORTED, "direction %d: flux is not one-sided upwind", i);
+        }
+        for (int j = 0; j < n; ++j) {
+          op->g64.cv[i][j] = cv[j];
+          op->g64.le[i][j] = le[j];
+          op->g32.cv[i][j] = float(cv[j]);
+          op->g32.le[i][j] = float(le[j]);
+        }
+      }
+      for (int j = 0; j < n * n; ++j) {
+        op->g64.S[j] = T.S[j];
+        op->g64.Si[j] = T.Si[j];
+        op->g32.S[j] = float(T.S[j]);
+        op->g32.Si[j] = float(T.Si[j]);
+      }
+      for (int j = 0; j < n; ++j) op->g64.gq[j] = op->g32.gq[j] = T.x[j];
+      op->glaunch = hd::gauss_launchers(op->D, op->N);
+      const bool ok = d.dtype == HD_F64 ? op->glaunch.ok_f64 : op->glaunch.ok_f32;
+      if (!op->glaunch.f64 || !ok) {
+        delete op;
+        return fail(HD_ERR_UNSUPPORTED, "no Gauss-quadrature kernel for D=%d, degree=%d, dtype=%s",
+                    d.dim_x + d.dim_v, d.degree, d.dtype == HD_F64 ? "f64" : "f32");
+      }
+    } else {
+      for (int i = 0; i < op->D; ++i)
+        if (!derive_line_op(op->N, op->glw, op->Dm, d.velocity[i], op->h[i], d.skew, &op->ops[i])) {
+          delete op;
+          return fail(HD_ERR_UNSUPPORTED, "direction %d: flux is not one-sided upwind", i);
+        }
+    }
     op->launchers = get_launchers(op->D, op->N);
     const bool ok = d.dtype == HD_F64 ? op->launchers.ok_f64 : op->launchers.ok_f32;
     if (!op->launchers.f64 || !ok) {
@@ -354,6 +534,11 @@ int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
     g.D = op->D; g.dim_x = d.dim_x; g.N = op->N; g.NC = op->NC; g.ncx = op->ncx; g.n_dofs = op->n_dofs;
     for (int i = 0; i < op->D; ++i) { g.cells[i] = op->cells[i]; g.lo[i] = op->lo[i]; g.h[i] = op->h[i]; }
     for (int i = 0; i < op->N; ++i) { g.gl[i] = op->gl[i]; g.glw[i] = op->glw[i]; }
+    g.gauss = op->gauss;
+    if (op->gauss) {
+      for (int i = 0; i < op->N; ++i) { g.gq[i] = op->gt.x[i]; g.gw[i] = op->gt.w[i]; }
+      for (int i = 0; i < op->N * op->N; ++i) g.S[i] = op->gt.S[i];
+    }
     cudaError_t e = cudaGetDevice(&op->device);
     if (e != cudaSuccess) { delete op; return cuda_fail(e, "cudaGetDevice"); }
     e = cudaMalloc(&op->d_partials, sizeof(double) * (2 * hd::kNormBlocks + 3));
@@ -394,6 +579,47 @@ int hd_adv_set_tile(hd_adv* op, int cells_per_cta, int ctas_per_sm) {
   return HD_OK;
 }
 
+int hd_adv_autotune(hd_adv* op, const void* src, void* dst, int reps, int* cells_per_cta, int* ctas_per_sm,
+                    double* ms, void* stream) {
+  if (!op || !src || !dst || src == dst) return fail(HD_ERR_INVALID, "hd_adv_autotune: bad argument");
+  if (reps < 1) reps = 3;
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool f64 = op->desc.dtype == HD_F64;
+  const int maxc = f64 ? op->launchers.cells_per_cta_f64 : op->launchers.cells_per_cta_f32;
+  std::vector<int> cands;
+  for (int v = maxc; v >= 1 && cands.size() < 5; v /= 2) cands.push_back(v);
+  if (std::find(cands.begin(), cands.end(), 1) == cands.end()) cands.push_back(1);
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    return fail(HD_ERR_CUDA, "hd_adv_autotune: events");
+  float best = 1e30f;
+  int best_c = 0, best_p = 0, rc = HD_OK;
+  for (int c : cands)
+    for (int per : {0, 2}) {
+      op->p64.cpb = op->p32.cpb = c;
+      op->p64.ctas_per_sm = op->p32.ctas_per_sm = per;
+      rc = launch(op, hd::kApply, src, src, dst, nullptr, 0.0, 0.0, 0.0, s);  // warm-up
+      if (rc) break;
+      cudaEventRecord(e0, s);
+      for (int r = 0; r < reps && !rc; ++r) rc = launch(op, hd::kApply, src, src, dst, nullptr, 0.0, 0.0, 0.0, s);
+      cudaEventRecord(e1, s);
+      if (rc) break;
+      if (cudaEventSynchronize(e1) != cudaSuccess) { rc = fail(HD_ERR_CUDA, "hd_adv_autotune: timing"); break; }
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      if (t < best) { best = t; best_c = c; best_p = per; }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  op->p64.cpb = op->p32.cpb = best_c;
+  op->p64.ctas_per_sm = op->p32.ctas_per_sm = best_p;
+  if (rc) return rc;
+  if (cells_per_cta) *cells_per_cta = best_c;
+  if (ctas_per_sm) *ctas_per_sm = best_p;
+  if (ms) *ms = best / reps;
+  return HD_OK;
+}
+
 int hd_adv_tile_limits(const hd_adv* op, int* max_cells_per_cta, int* threads_per_cell) {
   if (!op) return fail(HD_ERR_INVALID, "hd_adv_tile_limits: null handle");
   const bool f64 = op->desc.dtype == HD_F64;
@@ -408,7 +634,7 @@ int hd_adv_set_kernel(hd_adv* op, int variant) {
   if (!op) return fail(HD_ERR_INVALID, "hd_adv_set_kernel: null handle");
   if (variant != HD_KERNEL_AUTO && variant != HD_KERNEL_GENERIC && variant != HD_KERNEL_PIPELINED)
     return fail(HD_ERR_INVALID, "unknown kernel variant %d", variant);
-  if (variant == HD_KERNEL_PIPELINED && !(op->dtype == HD_F32 && op->N == 4 && hd::ecl6_eligible(op->p32)))
+  if (variant == HD_KERNEL_PIPELINED && !(!op->gauss && op->dtype == HD_F32 && op->N == 4 && hd::ecl6_eligible(op->p32)))
     return fail(HD_ERR_UNSUPPORTED, "the pipelined kernel needs a fully periodic 3x+3v mesh, degree 3, FP32");
   op->variant = variant;
   return HD_OK;

@@ -6,6 +6,7 @@
 
 #include "../../include/hyperdeal_gb300.h"
 #include "hd_ecl.cuh"
+#include "hd_gauss.cuh"
 #include "hd_vector.cuh"
 
 // per-direction line operator in FP64 (see derive_line_op in hd_capi.cu)
@@ -13,6 +14,15 @@ struct LineOpD {
   double M[hd::kMaxN * hd::kMaxN];
   double cin;
   int in_node, nb_node, step, active;
+};
+
+// one-dimensional tables of the Gauss path: Gauss points/weights, the
+// derivative matrix of their Lagrange basis, its end values l0 = l(0),
+// l1 = l(1), and S[q][j] = L_j(xi_q) (Gauss-Lobatto basis at Gauss points)
+struct GaussTables {
+  double x[hd::kMaxN], w[hd::kMaxN], D[hd::kMaxN * hd::kMaxN];
+  double l0[hd::kMaxN], l1[hd::kMaxN];
+  double S[hd::kMaxN * hd::kMaxN], Si[hd::kMaxN * hd::kMaxN];
 };
 
 struct hd_adv {
@@ -32,6 +42,11 @@ struct hd_adv {
   double* d_table;     // factor table of product functions (sum_d cells_d * (k+1) doubles)
   int device;
   int variant;         // HD_KERNEL_AUTO / _GENERIC / _PIPELINED
+  int gauss;           // 1: Gauss quadrature (non-collocation) path
+  GaussTables gt;
+  hd::GaussExtra<double> g64;
+  hd::GaussExtra<float> g32;
+  hd::GaussLaunchers glaunch;
 };
 
 struct hd_lsrk {

@@ -192,6 +192,8 @@ extern "C" int hd_norm_and_error_noalloc(const hd_adv_desc* desc, const hd_funct
   if (d.dim_x < 1 || d.dim_x > 3 || d.dim_v < 1 || d.dim_v > 3 || d.degree < 1 || d.degree + 1 > hd::kMaxN ||
       d.n_points != d.degree + 1 || (d.dtype != HD_F64 && d.dtype != HD_F32))
     return noalloc_fail(HD_ERR_INVALID, "hd_norm_and_error_noalloc: unsupported descriptor");
+  if (d.quadrature != HD_QUAD_GAUSS_LOBATTO)
+    return noalloc_fail(HD_ERR_UNSUPPORTED, "hd_norm_and_error_noalloc: Gauss-Lobatto collocation only");
   Geom g;
   std::memset(&g, 0, sizeof(g));
   g.D = d.dim_x + d.dim_v;

@@ -16,7 +16,8 @@ namespace hd {
 // values at the nodes are products of table entries: table[off_d + c*N + i]
 // holds factor d at x_d = lo_d + (c + gl_i) h_d (kind 2); the amplitude is
 // applied once per node.  One table kernel per call, then one block per cell.
-__global__ void function_table_kernel(VecGeom g, DevFunction f, double t, double* __restrict__ table, int total) {
+__global__ void function_table_kernel(VecGeom g, DevFunction f, double t, double* __restrict__ table, int total,
+                                      int at_gauss) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= total) return;
   int d = 0, off = 0;
@@ -25,7 +26,7 @@ __global__ void function_table_kernel(VecGeom g, DevFunction f, double t, double
     ++d;
   }
   const int c = (e - off) / g.N, i = (e - off) % g.N;
-  const double x = g.lo[d] + (c + g.gl[i]) * g.h[d];
+  const double x = g.lo[d] + (c + (at_gauss ? g.gq[i] : g.gl[i])) * g.h[d];
   const double arg = f.omega[d] * (x - f.speed[d] * t) + f.phase[d];
   table[e] = f.cosine[d] ? cos(arg) : sin(arg);
 }
@@ -104,6 +105,75 @@ __global__ void norm_error_kernel(VecGeom g, DevFunction f, const double* __rest
   }
 }
 
+// Gauss quadrature (vector_tools.h:144-223 with quadrature 0 = Gauss): per
+// cell the Gauss-point values (S in every direction, in shared memory), then
+// the same sums with the Gauss weights and the function at the Gauss points
+template <typename T>
+__global__ void norm_error_gauss_kernel(VecGeom g, DevFunction f, const double* __restrict__ table,
+                                        const T* __restrict__ src, long long n_cells, double* __restrict__ partials) {
+  extern __shared__ double sv[];
+  double s0 = 0.0, s1 = 0.0;
+  const int N = g.N, NC = g.NC, NL = g.NC / g.N;
+  for (long long gid = blockIdx.x; gid < n_cells; gid += gridDim.x) {
+    const T* in = src + gid * NC;
+    for (int node = threadIdx.x; node < NC; node += blockDim.x) sv[node] = double(in[node]);
+    __syncthreads();
+    int se = 1;
+    for (int e = 0; e < g.D; ++e) {
+      for (int line = threadIdx.x; line < NL; line += blockDim.x) {
+        int base = 0, stride = 1, l = line;
+        for (int f2 = 0; f2 < g.D; ++f2) {
+          if (f2 != e) {
+            base += (l % N) * stride;
+            l /= N;
+          }
+          stride *= N;
+        }
+        double u[kMaxN];
+        for (int q = 0; q < N; ++q) u[q] = sv[base + q * se];
+        for (int i = 0; i < N; ++i) {
+          double acc = 0.0;
+          for (int q = 0; q < N; ++q) acc += g.S[i * N + q] * u[q];
+          sv[base + i * se] = acc;
+        }
+      }
+      se *= N;
+      __syncthreads();
+    }
+    int toff[kMaxDim];
+    cell_offsets(g, gid, toff);
+    for (int node = threadIdx.x; node < NC; node += blockDim.x) {
+      double ex = f.kind == 0 ? 0.0 : f.amp, jxw = 1.0;
+      int t = node;
+      for (int d = 0; d < g.D; ++d) {
+        const int id = t % N;
+        t /= N;
+        if (f.kind == 2) ex *= table[toff[d] + id];
+        jxw *= g.h[d] * g.gw[id];
+      }
+      const double v = sv[node];
+      const double e = v - ex;
+      s0 += v * v * jxw;
+      s1 += e * e * jxw;
+    }
+    __syncthreads();
+  }
+  __shared__ double r0[32], r1[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, o);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+  }
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+  if (l == 0) { r0[w] = s0; r1[w] = s1; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < (int)(blockDim.x / 32); ++k) { a += r0[k]; b += r1[k]; }
+    partials[2 * blockIdx.x] = a;
+    partials[2 * blockIdx.x + 1] = b;
+  }
+}
+
 __global__ void reduce_partials_kernel(const double* __restrict__ partials, int nblocks, double* __restrict__ out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     double a = 0.0, b = 0.0;
@@ -138,10 +208,11 @@ static int table_size(const VecGeom& g) {
   return total;
 }
 
-static cudaError_t fill_table(const VecGeom& g, const DevFunction& f, double t, double* table, cudaStream_t s) {
+static cudaError_t fill_table(const VecGeom& g, const DevFunction& f, double t, double* table, cudaStream_t s,
+                              int at_gauss = 0) {
   if (f.kind != 2) return cudaSuccess;
   const int total = table_size(g);
-  function_table_kernel<<<(total + 127) / 128, 128, 0, s>>>(g, f, t, table, total);
+  function_table_kernel<<<(total + 127) / 128, 128, 0, s>>>(g, f, t, table, total, at_gauss);
   return cudaGetLastError();
 }
 
@@ -160,11 +231,25 @@ cudaError_t launch_interpolate(const VecGeom& g, const DevFunction& f, double t,
 
 cudaError_t launch_norm_error(const VecGeom& g, const DevFunction& f, double t, const void* src, int is_f32,
                               double* table, double* partials, double* out, cudaStream_t s) {
-  cudaError_t e = fill_table(g, f, t, table, s);
+  cudaError_t e = fill_table(g, f, t, table, s, g.gauss);
   if (e != cudaSuccess) return e;
   const long long n_cells = g.n_dofs / g.NC;
   const unsigned grid = kNormBlocks;
-  if (is_f32)
+  if (g.gauss) {
+    const size_t smem = sizeof(double) * g.NC;
+    if (smem > 48 * 1024) {
+      e = cudaFuncSetAttribute(is_f32 ? (const void*)norm_error_gauss_kernel<float>
+                                      : (const void*)norm_error_gauss_kernel<double>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+      if (e != cudaSuccess) return e;
+    }
+    if (is_f32)
+      norm_error_gauss_kernel<float><<<grid, node_threads(g), smem, s>>>(g, f, table, (const float*)src, n_cells,
+                                                                         partials);
+    else
+      norm_error_gauss_kernel<double><<<grid, node_threads(g), smem, s>>>(g, f, table, (const double*)src, n_cells,
+                                                                          partials);
+  } else if (is_f32)
     norm_error_kernel<float><<<grid, node_threads(g), 0, s>>>(g, f, table, (const float*)src, n_cells, partials);
   else
     norm_error_kernel<double><<<grid, node_threads(g), 0, s>>>(g, f, table, (const double*)src, n_cells, partials);

@@ -16,6 +16,8 @@ struct VecGeom {
   int cells[kMaxDim];
   double lo[kMaxDim], h[kMaxDim];
   double gl[kMaxN], glw[kMaxN];
+  int gauss;                                // Gauss quadrature: norms at the Gauss points
+  double gq[kMaxN], gw[kMaxN], S[kMaxN * kMaxN];  // points, weights, nodal -> Gauss-point values
 };
 
 // `table` holds sum_d cells_d * (k+1) doubles (the factors of a product function)

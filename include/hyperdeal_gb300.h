@@ -75,9 +75,14 @@ typedef struct hd_function {
  * AdvectionOperation::reinit, BoundaryDescriptor and ConstantVelocityFieldView
  * (include/hyper.deal/operators/advection/advection_operation.h:97-129,
  *  boundary_descriptor.h:77-104, velocity_field_view.h:64-166).           */
+enum hd_quadrature {
+  HD_QUAD_GAUSS_LOBATTO = 0, /* collocation: diagonal mass, no basis change   */
+  HD_QUAD_GAUSS = 1          /* Gauss points: basis change and its inverse    */
+};
+
 typedef struct hd_adv_desc {
   int dim_x, dim_v;     /* 1..3 each                                       */
-  int degree;           /* k; n_points must be k+1 (collocation)           */
+  int degree;           /* k; n_points must be k+1                         */
   int n_points;
   int dtype;            /* HD_F64 or HD_F32 (storage and arithmetic)       */
   int cells_x[3], cells_v[3];
@@ -87,6 +92,9 @@ typedef struct hd_adv_desc {
   double skew;          /* AdvectionOperationParamters::factor_skew        */
   int bc_kind;          /* enum hd_bc_kind, used on non-periodic faces     */
   hd_function bc;       /* g for HD_BC_FUNCTION                            */
+  int quadrature;       /* enum hd_quadrature: Gauss-Lobatto collocation (0,
+                           default) or Gauss (1); the reference's
+                           quadrature 0 of MatrixFree (application.h:218-219) */
 } hd_adv_desc;
 
 typedef struct hd_adv hd_adv;
@@ -116,6 +124,10 @@ long long hd_adv_n_dofs(const hd_adv *op);
  * (0 = as many as fit).  Results do not depend on the tile. */
 int hd_adv_set_tile(hd_adv *op, int cells_per_cta, int ctas_per_sm);
 int hd_adv_tile_limits(const hd_adv *op, int *max_cells_per_cta, int *threads_per_cell);
+/* time apply launches (src read, dst overwritten) for candidate tiles and
+ * keep the fastest; returns it and its time per apply */
+int hd_adv_autotune(hd_adv *op, const void *src, void *dst, int reps, int *cells_per_cta, int *ctas_per_sm,
+                    double *ms, void *stream);
 
 /* Kernel selection: AUTO picks the persistent TMA-pipelined kernel where it
  * applies (FP32, degree 3, fully periodic 3x+3v mesh) and the generic

@@ -167,3 +167,15 @@ def test_bad_arguments():
         batch.apply(us, us)  # dst == src
     with pytest.raises(A.HdError):
         batch.replay_graph()  # nothing recorded
+
+
+def test_single_operator_autotune_keeps_results():
+    ops, us, _ = _setup()
+    for op, u in zip(ops[:3], us[:3]):
+        ref = op.initialize_dof_vector()
+        op.apply(ref, u, 0.0)
+        dst = op.initialize_dof_vector()
+        tile = op.autotune(u, dst, reps=2)
+        assert tile["cells_per_cta"] >= 1 and tile["ms_per_apply"] > 0
+        op.apply(dst, u, 0.0)
+        assert torch.equal(dst, ref)
