@@ -43,7 +43,7 @@ BatchLaunchers batch_launchers_d4(int N);
 BatchLaunchers batch_launchers_d5(int N);
 
 template <int D, int N, typename T, int MODE>
-__global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
+__global__ void __launch_bounds__(EclShape<D, N, T>::THREADS, EclShape<D, N, T>::MINB)
     ecl_batch_kernel(const EclParams<T>* __restrict__ params, const long long* __restrict__ prefix, int n, int cpb) {
   using S = EclShape<D, N, T>;
   constexpr int NC = S::NC, TPC = S::TPC;
@@ -51,10 +51,13 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
   __shared__ long long s_prefix[kBatchMaxInstances + 1];
   for (int i = threadIdx.x; i <= n; i += blockDim.x) s_prefix[i] = prefix[i];
   __syncthreads();
+  constexpr bool SU = EclStaging<D, N, T, MODE>::STAGE_U;
   const long long bufe = ecl_buffer_elems<D, N, T>(cpb);
   T* const s_in0 = reinterpret_cast<T*>(smem_raw);
   T* const s_in1 = s_in0 + bufe;
   T* const s_o = s_in0 + 2 * bufe;
+  T* const s_u0 = s_in0 + 3 * bufe;
+  T* const s_u1 = s_in0 + 4 * bufe;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lc = tid / TPC, tl = tid % TPC;
   const long long total = s_prefix[n];
@@ -68,33 +71,36 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
     }
     return lo;
   };
-  auto stage = [&](T* dst, int inst, long long lb) {
+  auto stage = [&](T* dst, T* dstu, int inst, long long lb) {
     const EclParams<T>& P = params[inst];
     const long long c0 = lb * cpb;
     const long long ncell = (P.n_cells - c0) < cpb ? (P.n_cells - c0) : cpb;
     stage_async(dst, P.tin + c0 * NC, ncell * NC, tid, nthr);
+    if constexpr (SU) stage_async(dstu, P.uin + c0 * NC, ncell * NC, tid, nthr);
   };
   long long b = blockIdx.x;
   int inst = 0;
   if (b < total) {
     inst = locate(b);
-    stage(s_in0, inst, b - s_prefix[inst]);
+    stage(s_in0, s_u0, inst, b - s_prefix[inst]);
   }
   cp_async_commit();
   bool odd = false;
   for (; b < total; b += gridDim.x) {
     T* const cur = odd ? s_in1 : s_in0;
     T* const nxt = odd ? s_in0 : s_in1;
+    T* const curu = odd ? s_u1 : s_u0;
+    T* const nxtu = odd ? s_u0 : s_u1;
     const long long nb = b + gridDim.x;
     int ninst = inst;
     if (nb < total) {
       ninst = locate(nb);
-      stage(nxt, ninst, nb - s_prefix[ninst]);
+      stage(nxt, nxtu, ninst, nb - s_prefix[ninst]);
     }
     cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
-    ecl_block<D, N, T, MODE>(params[inst], (b - s_prefix[inst]) * cpb, lc, tl, cur, s_o);
+    ecl_block<D, N, T, MODE>(params[inst], (b - s_prefix[inst]) * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
     __syncthreads();
     odd = !odd;
     inst = ninst;
@@ -109,15 +115,23 @@ cudaError_t launch_batch(const BatchLaunch<T>& L, int mode, cudaStream_t stream)
     return cudaErrorNotSupported;
   } else {
     if (L.n < 1 || L.n > kBatchMaxInstances) return cudaErrorInvalidValue;
-    const int cpb = (L.cpb < 1 || L.cpb > S::CPB) ? ecl_default_cpb<D, N, T>() : L.cpb;
+    if (mode < kApply || mode > kStageLast) return cudaErrorInvalidValue;
+    int cpb = (L.cpb < 1 || L.cpb > S::CPB) ? ecl_default_cpb<D, N, T>() : L.cpb;
+    const int nbuf = mode == kStageMid ? EclStaging<D, N, T, kStageMid>::NBUF
+                     : mode == kStageLast ? EclStaging<D, N, T, kStageLast>::NBUF : 3;
+    // (the static prefix table takes 2 KiB beside the dynamic tiles); the
+    // block offsets were made for this cpb, so it must fit as it is
+    if (size_t(nbuf * ecl_buffer_elems<D, N, T>(cpb)) * sizeof(T) > 218 * 1024) return cudaErrorInvalidValue;
     const int threads = S::TPC * cpb;
-    const size_t smem = size_t(3 * ecl_buffer_elems<D, N, T>(cpb)) * sizeof(T);
+    const size_t smem = size_t(nbuf * ecl_buffer_elems<D, N, T>(cpb)) * sizeof(T);
     static bool attr_done[4] = {false, false, false, false};
     static int sms = 0;
     auto go = [&](auto kern) -> cudaError_t {
       if (!attr_done[mode]) {
+        int cmax = S::CPB;
+        while (cmax > 1 && size_t(nbuf * ecl_buffer_elems<D, N, T>(cmax)) * sizeof(T) > 218 * 1024) --cmax;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             int(3 * ecl_buffer_elems<D, N, T>(S::CPB) * sizeof(T)));
+                                             int(nbuf * ecl_buffer_elems<D, N, T>(cmax) * sizeof(T)));
         if (e != cudaSuccess) return e;
         int dev = 0;
         cudaGetDevice(&dev);
@@ -144,11 +158,21 @@ cudaError_t launch_batch(const BatchLaunch<T>& L, int mode, cudaStream_t stream)
   }
 }
 
+// the largest tile whose staging (five buffers in the stage modes) fits
+template <int D, int N, typename T>
+constexpr int batch_max_cpb() {
+  int c = EclShape<D, N, T>::CPB;
+  while (c > 1 && size_t(EclStaging<D, N, T, kStageMid>::NBUF * ecl_buffer_elems<D, N, T>(c)) * sizeof(T) > 218 * 1024)
+    --c;
+  return c;
+}
+
 template <int D, int N>
 BatchLaunchers make_batch_launchers() {
-  return BatchLaunchers{&launch_batch<D, N, double>, &launch_batch<D, N, float>, EclShape<D, N, double>::CPB,
-                        EclShape<D, N, float>::CPB, ecl_default_cpb<D, N, double>(), ecl_default_cpb<D, N, float>(),
-                        EclShape<D, N, double>::SUPPORTED && EclShape<D, N, float>::SUPPORTED};
+  constexpr int m64 = batch_max_cpb<D, N, double>(), m32 = batch_max_cpb<D, N, float>();
+  constexpr int d64 = ecl_default_cpb<D, N, double>(), d32 = ecl_default_cpb<D, N, float>();
+  return BatchLaunchers{&launch_batch<D, N, double>, &launch_batch<D, N, float>, m64, m32, d64 < m64 ? d64 : m64,
+                        d32 < m32 ? d32 : m32, EclShape<D, N, double>::SUPPORTED && EclShape<D, N, float>::SUPPORTED};
 }
 
 }  // namespace hd

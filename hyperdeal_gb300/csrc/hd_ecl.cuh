@@ -94,6 +94,9 @@ struct EclShape {
   static constexpr int THREADS = TPC * CPB;
   static constexpr size_t SMEM = size_t(3) * CPB * NC * sizeof(T);  // 2 staging buffers + accumulator
   static constexpr int NPH = (D + 1) / 2;                     // phases
+  // FP32: at least two CTAs of the largest shape per SM (caps registers at
+  // 128; more registers cost occupancy the bandwidth-bound kernel needs)
+  static constexpr int MINB = sizeof(T) == 4 ? 2 : 1;
   static constexpr bool SUPPORTED = SMEM + 48 <= 220 * 1024;
 };
 
@@ -175,7 +178,7 @@ __device__ __forceinline__ void stage_async(T* dst, const T* src, long long nval
 
 // shared-memory elements of one staging buffer (rounded to 16 bytes)
 template <int D, int N, typename T>
-__host__ __device__ __forceinline__ long long ecl_buffer_elems(int cpb) {
+__host__ __device__ constexpr long long ecl_buffer_elems(int cpb) {
   const long long bytes = (long long)cpb * EclShape<D, N, T>::NC * sizeof(T);
   return ((bytes + 15) / 16) * 16 / (long long)sizeof(T);
 }
@@ -183,15 +186,13 @@ __host__ __device__ __forceinline__ long long ecl_buffer_elems(int cpb) {
 // one block of P.cpb cells (the CTA's cells start at cell0) from the staged
 // input `su_all`: the D line operators two directions per phase, the last
 // phase writing K or the fused stage update
+// (stage modes mid/last: `uu_all` is the block's RK solution staged in shared
+// memory next to the operator input, or nullptr to read it from global memory)
 template <int D, int N, typename T, int MODE>
 __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0, int lc, int tl, const T* su_all,
-                                          T* so_all) {
+                                          T* so_all, const T* uu_all) {
   using S = EclShape<D, N, T>;
   constexpr int NC = S::NC, TPC = S::TPC;
-  // keep the RK solution values of a plane in registers from the start of the
-  // last phase (hides their latency behind the phase's arithmetic) when the
-  // registers allow it
-  constexpr bool kEarlyU = (N <= 4) && (MODE == kStageMid || MODE == kStageLast);
   const long long gid = cell0 + lc;
   const bool valid = gid < P.n_cells;
 
@@ -235,15 +236,6 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
 #pragma unroll
         for (int a = 0; a < N; ++a)
           upB[a] = nbB >= 0 ? __ldg(P.tin + nbB * NC + base + a * strideA + LB.nb_node * strideB) : T(0);
-        T uin[kEarlyU ? N : 1][kEarlyU ? N : 1];
-        if constexpr (kEarlyU) {
-          if (last && valid) {
-#pragma unroll
-            for (int a = 0; a < N; ++a)
-#pragma unroll
-              for (int b = 0; b < N; ++b) uin[a][b] = P.uin[gid * NC + base + a * strideA + b * strideB];
-          }
-        }
         T uu[N][N], acc[N][N];  // [a][b]: node base + a*strideA + b*strideB
 #pragma unroll
         for (int a = 0; a < N; ++a)
@@ -309,8 +301,7 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
               } else {
                 T u;
                 if constexpr (MODE == kStageFirst) u = uu[a][b];
-                else if constexpr (kEarlyU) u = uin[kEarlyU ? a : 0][kEarlyU ? b : 0];
-                else u = P.uin[gi];
+                else u = uu_all ? uu_all[lc * NC + base + a * strideA + b * strideB] : P.uin[gi];
                 P.uout[gi] = fma(P.fb, k, u);
                 if constexpr (MODE != kStageLast) P.tout[gi] = fma(P.fa, k, u);
               }
@@ -355,7 +346,7 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
             if constexpr (MODE == kApply) {
               P.uout[gi] = k;
             } else {
-              const T u = (MODE == kStageFirst) ? uu[a] : P.uin[gi];
+              const T u = (MODE == kStageFirst) ? uu[a] : (uu_all ? uu_all[lc * NC + base + a * strideA] : P.uin[gi]);
               P.uout[gi] = fma(P.fb, k, u);
               if constexpr (MODE != kStageLast) P.tout[gi] = fma(P.fa, k, u);
             }
@@ -367,41 +358,56 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
   }
 }
 
+// stage modes mid/last also stage the RK solution of the block (two more
+// buffers) when five buffers of one cell fit in shared memory
+template <int D, int N, typename T, int MODE>
+struct EclStaging {
+  static constexpr bool STAGE_U = (MODE == kStageMid || MODE == kStageLast) &&
+                                  size_t(5) * EclShape<D, N, T>::NC * sizeof(T) + 64 <= 220 * 1024;
+  static constexpr int NBUF = STAGE_U ? 5 : 3;
+};
+
 // Persistent generic kernel: CTAs walk blocks of P.cpb cells with a stride of
 // the grid; the next block's input is staged by cp.async while the current
 // one is computed (two staging buffers + one accumulator tile).
 template <int D, int N, typename T, int MODE>
-__global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
+__global__ void __launch_bounds__(EclShape<D, N, T>::THREADS, EclShape<D, N, T>::MINB)
     ecl_kernel(const __grid_constant__ EclParams<T> P) {
   using S = EclShape<D, N, T>;
   constexpr int NC = S::NC, TPC = S::TPC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int cpb = P.cpb;
+  constexpr bool SU = EclStaging<D, N, T, MODE>::STAGE_U;
   const long long bufe = ecl_buffer_elems<D, N, T>(cpb);
   T* const s_in0 = reinterpret_cast<T*>(smem_raw);
   T* const s_in1 = s_in0 + bufe;
   T* const s_o = s_in0 + 2 * bufe;
+  T* const s_u0 = s_in0 + 3 * bufe;  // (stage modes with STAGE_U only)
+  T* const s_u1 = s_in0 + 4 * bufe;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lc = tid / TPC, tl = tid % TPC;
   const long long nblk = (P.n_cells + cpb - 1) / cpb;
-  auto stage = [&](T* dst, long long blk) {
+  auto stage = [&](T* dst, T* dstu, long long blk) {
     const long long c0 = blk * cpb;
     const long long ncell = (P.n_cells - c0) < cpb ? (P.n_cells - c0) : cpb;
     stage_async(dst, P.tin + c0 * NC, ncell * NC, tid, nthr);
+    if constexpr (SU) stage_async(dstu, P.uin + c0 * NC, ncell * NC, tid, nthr);
   };
   long long b = blockIdx.x;
-  if (b < nblk) stage(s_in0, b);
+  if (b < nblk) stage(s_in0, s_u0, b);
   cp_async_commit();
   bool odd = false;
   for (; b < nblk; b += gridDim.x) {
     T* const cur = odd ? s_in1 : s_in0;
     T* const nxt = odd ? s_in0 : s_in1;
+    T* const curu = odd ? s_u1 : s_u0;
+    T* const nxtu = odd ? s_u0 : s_u1;
     const long long nb = b + gridDim.x;
-    if (nb < nblk) stage(nxt, nb);
+    if (nb < nblk) stage(nxt, nxtu, nb);
     cp_async_commit();
     cp_async_wait<1>();  // this thread's copies of block b are complete
     __syncthreads();     // ... and everybody's
-    ecl_block<D, N, T, MODE>(P, b * cpb, lc, tl, cur, s_o);
+    ecl_block<D, N, T, MODE>(P, b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
     __syncthreads();     // cur and s_o are free for the next blocks
     odd = !odd;
   }
@@ -427,15 +433,22 @@ cudaError_t launch_ecl(const EclParams<T>& P0, int mode, cudaStream_t stream) {
   } else {
     EclParams<T> P = P0;
     if (P.cpb < 1 || P.cpb > S::CPB) P.cpb = ecl_default_cpb<D, N, T>();
+    if (mode < kApply || mode > kStageLast) return cudaErrorInvalidValue;
+    const int nbuf = mode == kStageMid ? EclStaging<D, N, T, kStageMid>::NBUF
+                     : mode == kStageLast ? EclStaging<D, N, T, kStageLast>::NBUF : 3;
+    // the staged tiles of the largest shape may not fit five times: shrink the tile
+    while (P.cpb > 1 && size_t(nbuf * ecl_buffer_elems<D, N, T>(P.cpb)) * sizeof(T) > 220 * 1024) --P.cpb;
     const int threads = S::TPC * P.cpb;
-    const size_t smem = size_t(3 * ecl_buffer_elems<D, N, T>(P.cpb)) * sizeof(T);
+    const size_t smem = size_t(nbuf * ecl_buffer_elems<D, N, T>(P.cpb)) * sizeof(T);
     // one flag per mode: the four kernels share this lambda's instantiation
     static bool attr_done[4] = {false, false, false, false};
     static int sms = 0;
     auto go = [&](auto kern) -> cudaError_t {
       if (!attr_done[mode]) {
+        int cmax = S::CPB;
+        while (cmax > 1 && size_t(nbuf * ecl_buffer_elems<D, N, T>(cmax)) * sizeof(T) > 220 * 1024) --cmax;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             int(3 * ecl_buffer_elems<D, N, T>(S::CPB) * sizeof(T)));
+                                             int(nbuf * ecl_buffer_elems<D, N, T>(cmax) * sizeof(T)));
         if (e != cudaSuccess) return e;
         int dev = 0;
         cudaGetDevice(&dev);
