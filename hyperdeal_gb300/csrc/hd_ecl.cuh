@@ -94,9 +94,12 @@ struct EclShape {
   static constexpr int THREADS = TPC * CPB;
   static constexpr size_t SMEM = size_t(3) * CPB * NC * sizeof(T);  // 2 staging buffers + accumulator
   static constexpr int NPH = (D + 1) / 2;                     // phases
-  // FP32: at least two CTAs of the largest shape per SM (caps registers at
-  // 128; more registers cost occupancy the bandwidth-bound kernel needs)
-  static constexpr int MINB = sizeof(T) == 4 ? 2 : 1;
+  // at least two CTAs of the largest shape per SM (caps registers at 128)
+  // for FP32, which is bandwidth-bound and needs the occupancy, and for the
+  // FP64 6D shapes up to degree 3, whose FP64-pipe-bound arithmetic needs the
+  // warps more than the registers (measured on GB300: 331 vs 359 ms per rk45
+  // step at 8^3 x 8^3 cells, k = 3); other FP64 shapes are faster without the cap
+  static constexpr int MINB = (sizeof(T) == 4 || (D == 6 && N <= 4)) ? 2 : 1;
   static constexpr bool SUPPORTED = SMEM + 48 <= 220 * 1024;
 };
 
@@ -359,10 +362,11 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
 }
 
 // stage modes mid/last also stage the RK solution of the block (two more
-// buffers) when five buffers of one cell fit in shared memory
+// buffers) when five buffers of one cell fit in shared memory (not for the
+// FP64 6D shapes: their 32 KiB+ cell tiles would leave one CTA per SM)
 template <int D, int N, typename T, int MODE>
 struct EclStaging {
-  static constexpr bool STAGE_U = (MODE == kStageMid || MODE == kStageLast) &&
+  static constexpr bool STAGE_U = (MODE == kStageMid || MODE == kStageLast) && !(sizeof(T) == 8 && D == 6) &&
                                   size_t(5) * EclShape<D, N, T>::NC * sizeof(T) + 64 <= 220 * 1024;
   static constexpr int NBUF = STAGE_U ? 5 : 3;
 };
