@@ -7,6 +7,7 @@ definition, DoFs * stages * steps / time
 (examples/advection/include/application.h:540-543).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  python bench.py --workload adv4d    (4D k=3 16^2 x 16^2, FP32 and FP64, its own JSON line)
   python bench.py --workload vp2x2v   (the Vlasov-Poisson configuration, its own JSON line)
   python bench.py --workload batch64  (64 batched uneven instances, its own JSON line)
 
@@ -412,6 +413,84 @@ def run_batch(args):
     return 0
 
 
+def run_adv4d(args):
+    """4D (2x+2v) k=3, 16^2 x 16^2 cells (16,777,216 DoFs), velocity (1.0, 0.7, 0.5, 0.3),
+    f0 = prod sin(2 pi coord): fused rk45 steps in FP32 and FP64 storage through the generic
+    kernel, the FP32 - FP64 difference after the same steps, and the oracle's FP64 step time."""
+    import numpy as np
+    import torch
+
+    from hyperdeal_gb300 import advection as A
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    vel = [1.0, 0.7, 0.5, 0.3]
+    f0 = A.Function(2, 1.0, omega=[2 * math.pi] * 4, speed=[0.0] * 4)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    res, sols = {}, {}
+    clocks = None
+    for dtype in ("f32", "f64"):
+        p = A.AdvectionParameters(2, 2, 3, [16, 16], [16, 16], [0.0] * 2, [1.0] * 2, [0.0] * 2, [1.0] * 2, vel,
+                                  dtype=dtype)
+        op = A.AdvectionOperation(p)
+        sol = op.initialize_dof_vector()
+        A.VectorTools.interpolate(op, f0, sol, 0.0)
+        Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
+        integ = A.LowStorageRungeKuttaIntegrator(Ki, Ti, "rk45")
+        dt = CFL * op.critical_time_step() / DEGREE ** 1.5
+        t = 0.0
+        for _ in range(args.warmup):
+            integ.perform_time_step(sol, t, dt, op)
+            t += dt
+        sampler = None
+        if dtype == "f32":
+            sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+            sampler.start()
+            time.sleep(0.3)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            integ.perform_time_step(sol, t, dt, op)
+            t += dt
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if sampler is not None:
+            clocks = sampler.stop()
+        ms = e0.elapsed_time(e1) / args.steps
+        S = 4 if dtype == "f32" else 8
+        res[dtype] = {"ms_per_step": round(ms, 4), "gdof_per_s": round(op.n_dofs * N_STAGES / (ms / 1e3) / 1e9, 2),
+                      "hbm_gb_per_s": round(18 * S * op.n_dofs / (ms / 1e3) / 1e9, 1),
+                      "tile": op.tile_limits()}
+        sols[dtype] = sol.double()
+        n = op.n_dofs
+    l2 = float(torch.linalg.vector_norm(sols["f32"] - sols["f64"]) / torch.linalg.vector_norm(sols["f64"]))
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+        prob = O.Problem(2, 2, 3, [16] * 4, [0.0] * 4, [1.0] * 4, vel)
+        u = O.interpolate(prob, O.make_func(2, 1.0, omega=[2 * math.pi] * 4, speed=[0.0] * 4))
+        c0 = time.perf_counter()
+        O.lsrk_step(prob, "rk45", u, 0.0, 1e-4)
+        cpu_s = time.perf_counter() - c0
+        cpu = {"value": round(n * N_STAGES / cpu_s / 1e9, 4), "unit": "GDoF/s", "cores": os.cpu_count(),
+               "kind": "port", "sample": "one rk45 step of the full 16^2 x 16^2 mesh by the oracle (FP64, OpenMP)"}
+    peak, peak_kind = measured_peak_hbm()
+    out = {"metric": "advection GDoF/s (4D k=3, 16^2 x 16^2) FP32 and FP64 fused rk45", "value": res["f32"]["gdof_per_s"],
+           "unit": "GDoF/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": res["f32"]["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "4D (2x+2v) upwind DG advection, k=3 Gauss-Lobatto collocation, 16^2 x 16^2 cells "
+                                  "(65,536 cells, 16,777,216 DoFs), periodic unit box, velocity (1.0, 0.7, 0.5, 0.3), "
+                                  "f0 = prod sin(2 pi coord), fused rk45, CFL 0.2",
+                      "l2_flush": "none: 67 MB per FP32 vector (3 vectors 201 MB > 129 MB L2)"},
+           "f32": res["f32"], "f64": res["f64"], "l2_rel_err_f32_vs_f64": l2,
+           "roofline": {"bound": "hbm", "achieved": res["f32"]["hbm_gb_per_s"], "peak": peak, "unit": "GB/s",
+                        "frac": round(res["f32"]["hbm_gb_per_s"] / peak, 4), "peak_source": peak_kind},
+           "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": N_STAGES * args.steps}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -423,7 +502,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cells-x", type=int, default=CELLS,
                     help="x-cells per direction (8 = the benchmark workload; smaller only for profiling)")
-    ap.add_argument("--workload", default="advection6d", choices=["advection6d", "vp2x2v", "batch64"])
+    ap.add_argument("--workload", default="advection6d", choices=["advection6d", "adv4d", "vp2x2v", "batch64"])
     ap.add_argument("--vp-tol", type=float, default=1e-10, help="CG: ||r|| <= tol ||rhs|| (vp2x2v)")
     ap.add_argument("--vp-oracle-steps", type=int, default=2, help="steps compared with the FP64 oracle (vp2x2v)")
     ap.add_argument("--vp-runs", default="f64/previous,f64/zero,f64/learned,f32/previous,f32/zero,f32/learned",
@@ -435,6 +514,11 @@ def main():
                               "default arm (oracle host time in field_energy_vs_oracle)"}))
             return 0
         return run_vp(args)
+    if args.workload == "adv4d":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the 4D line is reported by the default arm"}))
+            return 0
+        return run_adv4d(args)
     if args.workload == "batch64":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the batched line is reported by the default arm"}))
