@@ -7,6 +7,7 @@ definition, DoFs * stages * steps / time
 (examples/advection/include/application.h:540-543).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  python bench.py --workload adv2d    (2D k=3 32 x 32, 100 steps, per-step launches vs CUDA graph)
   python bench.py --workload adv4d    (4D k=3 16^2 x 16^2, FP32 and FP64, its own JSON line)
   python bench.py --workload vp2x2v   (the Vlasov-Poisson configuration, its own JSON line)
   python bench.py --workload batch64  (64 batched uneven instances, its own JSON line)
@@ -413,6 +414,78 @@ def run_batch(args):
     return 0
 
 
+def run_adv2d(args):
+    """2D (1x+1v) k=3, 32 x 32 cells (16,384 DoFs), velocity (1.0, 0.5), f0 = sin(2 pi x) sin(2 pi v):
+    100 fused rk45 steps at CFL 0.2, launched one step at a time and as replays of a recorded
+    two-step CUDA graph; the error against the exact translated solution after the steps."""
+    import torch
+
+    from hyperdeal_gb300 import advection as A
+    from hyperdeal_gb300 import batch as Bt
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    vel = [1.0, 0.5]
+    p = A.AdvectionParameters(1, 1, 3, [32], [32], [0.0], [1.0], [0.0], [1.0], vel, dtype="f64")
+    op = A.AdvectionOperation(p)
+    f0 = A.Function(2, 1.0, omega=[2 * math.pi] * 2, speed=[0.0, 0.0])
+    dt = 0.2 * op.critical_time_step() / DEGREE ** 1.5
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nsteps = 100
+
+    def fresh():
+        u = op.initialize_dof_vector()
+        A.VectorTools.interpolate(op, f0, u, 0.0)
+        return u, op.initialize_dof_vector(), op.initialize_dof_vector()
+
+    u, K, T = fresh()
+    integ = A.LowStorageRungeKuttaIntegrator(K, T, "rk45")
+    for _ in range(args.warmup):
+        integ.perform_time_step(u, 0.0, dt, op)
+    u, K, T = fresh()
+    integ = A.LowStorageRungeKuttaIntegrator(K, T, "rk45")
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for s_ in range(nsteps):
+        integ.perform_time_step(u, s_ * dt, dt, op)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_plain = e0.elapsed_time(e1) / nsteps
+    exact = A.Function(2, 1.0, omega=[2 * math.pi] * 2, speed=vel)
+    _, err_plain = A.VectorTools.norm_and_error(op, exact, u, nsteps * dt)
+
+    ug, Kg, Tg = fresh()
+    batch = Bt.AdvectionBatch([op])
+    batch.capture_graph([ug], [Kg], [Tg], [0.0], [dt])
+    for _ in range(max(1, args.warmup // 2)):  # warm-up replays on a copy, then restart from f0
+        batch.replay_graph()
+    torch.cuda.synchronize()
+    A.VectorTools.interpolate(op, f0, ug, 0.0)
+    batch.capture_graph([ug], [Kg], [Tg], [0.0], [dt])
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(nsteps // 2):
+        batch.replay_graph()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_graph = e0.elapsed_time(e1) / nsteps
+    _, err_graph = A.VectorTools.norm_and_error(op, exact, ug, nsteps * dt)
+    n = op.n_dofs
+    out = {"metric": "advection GDoF/s (2D k=3, 32 x 32, FP64) over 100 rk45 steps", "value":
+           round(n * N_STAGES / (ms_graph / 1e3) / 1e9, 3), "unit": "GDoF/s", "n_gpus": 1, "steps": nsteps,
+           "warmup": args.warmup, "ms_per_step": round(ms_graph, 5), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "2D (1x+1v) upwind DG advection, k=3 Gauss-Lobatto collocation, 32 x 32 cells "
+                                  "(16,384 DoFs), periodic unit square, velocity (1.0, 0.5), f0 = sin(2 pi x) "
+                                  "sin(2 pi v), 100 rk45 steps at CFL 0.2", "l2_flush": "none (launch-bound size)"},
+           "graph_replay": {"ms_per_step": round(ms_graph, 5), "error_vs_exact": err_graph},
+           "per_step_launches": {"ms_per_step": round(ms_plain, 5), "error_vs_exact": err_plain,
+                                 "gdof_per_s": round(n * N_STAGES / (ms_plain / 1e3) / 1e9, 3)},
+           "gpu_launches": N_STAGES * nsteps + 1}
+    print(json.dumps(out))
+    return 0
+
+
 def run_adv4d(args):
     """4D (2x+2v) k=3, 16^2 x 16^2 cells (16,777,216 DoFs), velocity (1.0, 0.7, 0.5, 0.3),
     f0 = prod sin(2 pi coord): fused rk45 steps in FP32 and FP64 storage through the generic
@@ -502,7 +575,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cells-x", type=int, default=CELLS,
                     help="x-cells per direction (8 = the benchmark workload; smaller only for profiling)")
-    ap.add_argument("--workload", default="advection6d", choices=["advection6d", "adv4d", "vp2x2v", "batch64"])
+    ap.add_argument("--workload", default="advection6d",
+                    choices=["advection6d", "adv2d", "adv4d", "vp2x2v", "batch64"])
     ap.add_argument("--vp-tol", type=float, default=1e-10, help="CG: ||r|| <= tol ||rhs|| (vp2x2v)")
     ap.add_argument("--vp-oracle-steps", type=int, default=2, help="steps compared with the FP64 oracle (vp2x2v)")
     ap.add_argument("--vp-runs", default="f64/previous,f64/zero,f64/learned,f32/previous,f32/zero,f32/learned",
@@ -514,6 +588,11 @@ def main():
                               "default arm (oracle host time in field_energy_vs_oracle)"}))
             return 0
         return run_vp(args)
+    if args.workload == "adv2d":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the 2D line is reported by the default arm"}))
+            return 0
+        return run_adv2d(args)
     if args.workload == "adv4d":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the 4D line is reported by the default arm"}))

@@ -27,7 +27,7 @@ EXPORTED_SYMBOLS = (
     "hd_vp_learn_loss_grad", "hd_adv_set_tile", "hd_adv_tile_limits",
     "hd_batch_create", "hd_batch_destroy", "hd_batch_n_classes", "hd_batch_class_info", "hd_batch_set_tile",
     "hd_batch_apply", "hd_batch_lsrk_step", "hd_batch_graph_capture", "hd_batch_graph_launch", "hd_batch_autotune",
-    "hd_adv_autotune",
+    "hd_adv_autotune", "hd_vp_lsrk_step_fused",
 )
 HD_KERNEL_AUTO, HD_KERNEL_GENERIC, HD_KERNEL_PIPELINED = 0, 1, 2
 HD_VP_GUESS_ZERO, HD_VP_GUESS_PREVIOUS, HD_VP_GUESS_LEARNED = 0, 1, 2
@@ -125,6 +125,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.hd_vp_solve_field.argtypes = [vp, vp, vp]
     L.hd_vp_apply.argtypes = [vp, vp, vp, ctypes.c_double, vp]
     L.hd_vp_lsrk_step.argtypes = [vp, vp, vp, vp, vp, ctypes.c_double, ctypes.c_double, vp]
+    L.hd_vp_lsrk_step_fused.argtypes = [vp, vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                        ctypes.c_double, ctypes.c_double, vp]
     L.hd_vp_diagnostics.argtypes = [vp, vp, dp, vp]
     L.hd_vp_fields.argtypes = [vp, vp, vp, vp, vp]
     L.hd_vp_cg_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int), llp, llp, dp, llp]

@@ -755,6 +755,22 @@ int solve_poisson(hd_vp* v, cudaStream_t s) {
   return HD_OK;
 }
 
+// the phase-space advection with the current field: apply, or a fused LSRK stage
+int vp_advect(hd_vp* v, int mode, const void* src, const void* uin, void* dst, void* tout, double fb, double fa,
+              cudaStream_t s) {
+  cudaError_t e;
+  if (v->dtype == HD_F32) {
+    hd::VpAdvParams<float> P{(const float*)src, (float*)dst, (const float*)uin, (float*)tout, float(fb), float(fa),
+                             (const float*)v->d_xs, (const float*)v->d_es, v->g};
+    e = hd::launch_vp_advection(P, mode, s);
+  } else {
+    hd::VpAdvParams<double> P{(const double*)src, (double*)dst, (const double*)uin, (double*)tout, fb, fa,
+                              (const double*)v->d_xs, (const double*)v->d_es, v->g};
+    e = hd::launch_vp_advection(P, mode, s);
+  }
+  return vcuda(e, "vp advection");
+}
+
 }  // namespace
 
 extern "C" {
@@ -949,17 +965,7 @@ int hd_vp_apply(hd_vp* v, void* dst, const void* src, double time, void* stream)
   if (dst == src) return vfail(HD_ERR_INVALID, "hd_vp_apply: dst and src must differ");
   int rc = hd_vp_solve_field(v, src, stream);
   if (rc) return rc;
-  cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e;
-  if (v->dtype == HD_F32) {
-    hd::VpAdvParams<float> P{(const float*)src, (float*)dst, (const float*)v->d_xs, (const float*)v->d_es, v->g};
-    e = hd::launch_vp_advection(P, s);
-  } else {
-    hd::VpAdvParams<double> P{(const double*)src, (double*)dst, (const double*)v->d_xs, (const double*)v->d_es,
-                              v->g};
-    e = hd::launch_vp_advection(P, s);
-  }
-  return vcuda(e, "vp advection");
+  return vp_advect(v, hd::kApply, src, nullptr, dst, nullptr, 0.0, 0.0, (cudaStream_t)stream);
 }
 
 int hd_vp_lsrk_step(hd_vp* v, const hd_lsrk* rk, void* sol, void* Ki, void* Ti, double time, double dt, void* stream) {
@@ -979,6 +985,46 @@ int hd_vp_lsrk_step(hd_vp* v, const hd_lsrk* rk, void* sol, void* Ki, void* Ti, 
     rc = hd_lsrk_stage_update(v->dtype, n, bi[st] * dt, st == ns - 1 ? 0.0 : ai[st] * dt, Ki, sol, Ti, stream);
     if (rc) return rc;
   }
+  return HD_OK;
+}
+
+int hd_vp_lsrk_step_fused(hd_vp* v, const hd_lsrk* rk, void** sol, void** Ki, void** Ti, double time, double dt,
+                          void* stream) {
+  if (!v || !rk || !sol || !Ki || !Ti || !*sol || !*Ki || !*Ti)
+    return vfail(HD_ERR_INVALID, "hd_vp_lsrk_step_fused: null argument");
+  if (*sol == *Ki || *sol == *Ti || *Ki == *Ti) return vfail(HD_ERR_INVALID, "hd_vp_lsrk_step_fused: vectors must differ");
+  const int ns = hd_lsrk_n_stages(rk);
+  if (ns < 2) return vfail(HD_ERR_INVALID, "hd_vp_lsrk_step_fused: the scheme needs at least two stages");
+  double ai[16], bi[16], ci[16];
+  int rc = hd_lsrk_coefficients(rk, ai, bi, ci);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  // the rotation of hd_lsrk_step: X0 holds U and T_1, the new solution
+  // accumulates in X1, the stage inputs alternate between X2 and X0; every
+  // stage first solves for the field of its input
+  void* X0 = *sol;
+  void* X1 = *Ki;
+  void* X2 = *Ti;
+  void* t_in = X0;
+  void* t_free = X2;
+  for (int st = 0; st < ns; ++st) {
+    const bool last = st == ns - 1;
+    const int mode = st == 0 ? hd::kStageFirst : (last ? hd::kStageLast : hd::kStageMid);
+    rc = hd_vp_solve_field(v, t_in, stream);
+    if (rc) return rc;
+    rc = vp_advect(v, mode, t_in, st == 0 ? t_in : X1, X1, last ? nullptr : t_free, bi[st] * dt,
+                   last ? 0.0 : ai[st] * dt, s);
+    if (rc) return rc;
+    if (!last) {
+      void* next = t_free;
+      t_free = (st == 0) ? X0 : t_in;
+      t_in = next;
+    }
+  }
+  (void)time;
+  *sol = X1;
+  *Ki = X0;
+  *Ti = X2;
   return HD_OK;
 }
 

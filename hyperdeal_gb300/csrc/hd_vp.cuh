@@ -37,16 +37,23 @@ struct VpGeom {
 //   x-direction d: xs[(d * cells_v + c) * N + i] = v_d(c, i) / h_{x_d}, the
 //                  v-coordinate of node i of v-cell c,
 //   v-direction d: es[(gid_x * NCx + i_x) * dx + d] = d_d phi(x-node) / h_{v_d}.
+//
+// mode kApply: dst = A(src); stage modes (fused LSRK stage, as hd_ecl.cuh):
+// uout = uin + fb A(src), tout = uin + fa A(src) (kStageFirst: uin = src;
+// kStageLast: no tout).
 template <typename T>
 struct VpAdvParams {
   const T* src;
-  T* dst;
+  T* dst;        // apply: the result; stage modes: uout
+  const T* uin;
+  T* tout;
+  T fb, fa;
   const T* xs;
   const T* es;
   VpGeom g;
 };
 
-cudaError_t launch_vp_advection(const VpAdvParams<float>& P, cudaStream_t s);
-cudaError_t launch_vp_advection(const VpAdvParams<double>& P, cudaStream_t s);
+cudaError_t launch_vp_advection(const VpAdvParams<float>& P, int mode, cudaStream_t s);
+cudaError_t launch_vp_advection(const VpAdvParams<double>& P, int mode, cudaStream_t s);
 
 }  // namespace hd

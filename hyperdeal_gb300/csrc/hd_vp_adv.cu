@@ -8,6 +8,12 @@
 // the sign of a -- the reference's flux 0.5((u-+u+)a.n + |a.n|(u- - u+))
 // evaluated at the line's face points (advection_operation.h:325-526 with
 // the velocities of velocity_field_view.h:103-209 of the VP example).
+//
+// The kernel has the structure of the generic advection kernel (hd_ecl.cuh):
+// persistent CTAs walk blocks of cells, the next block's input (and, in the
+// middle/last RK stages, its RK solution) is staged by cp.async while the
+// current block is computed, and the LSRK stage update is fused into the
+// last phase.
 #include <cuda_runtime.h>
 
 #include "hd_ecl.cuh"
@@ -21,29 +27,14 @@ struct VpLine {
   T winv0, winvk;      // 1/w_0, 1/w_{N-1}
 };
 
-template <int D, int N, typename T>
-__global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
-    vp_adv_kernel(const __grid_constant__ VpAdvParams<T> P, const __grid_constant__ VpLine<T> Lk) {
+template <int D, int N, typename T, int MODE>
+__device__ __forceinline__ void vp_block(const VpAdvParams<T>& P, const VpLine<T>& Lk, long long cell0, int lc,
+                                         int tl, const T* su_all, T* so_all, const T* uu_all) {
   using S = EclShape<D, N, T>;
-  constexpr int NC = S::NC, TPC = S::TPC, CPB = S::CPB, DX = D / 2;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* s_u = reinterpret_cast<T*>(smem_raw);
-  T* s_o = s_u + CPB * NC;
+  constexpr int NC = S::NC, TPC = S::TPC, DX = D / 2;
   const VpGeom& g = P.g;
-
-  const int tid = threadIdx.x;
-  const int lc = tid / TPC, tl = tid % TPC;
-  const long long cell0 = (long long)blockIdx.x * CPB;
   const long long gid = cell0 + lc;
   const bool valid = gid < g.n_cells;
-  const long long ncell_here = (g.n_cells - cell0) < CPB ? (g.n_cells - cell0) : CPB;
-  {
-    const T* src = P.src + cell0 * NC;
-    const long long nval = ncell_here * NC;
-    for (long long i = tid; i < nval; i += S::THREADS) s_u[i] = __ldg(src + i);
-  }
-  __syncthreads();
-
   int cc[D];
   long long nbL[D], nbR[D];
   long long gx = 0;
@@ -60,8 +51,8 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
       nbR[d] = cc[d] + 1 < g.cells[d] ? gg + cs : gg - (long long)(g.cells[d] - 1) * cs;
     }
   }
-  T* su = s_u + lc * NC;
-  T* so = s_o + lc * NC;
+  const T* su = su_all + lc * NC;
+  T* so = so_all + lc * NC;
 
   // velocity / h of the line along d through node `bnode` (any node of the line)
   auto line_scale = [&](int d, int bnode) -> T {
@@ -71,6 +62,17 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
       return __ldg(P.xs + (d * g.cells[e] + cc[e]) * N + ie);
     }
     return __ldg(P.es + (gx * g.NCx + (bnode % ipow(N, DX))) * DX + (d - DX));
+  };
+  // the result of node `node` (local index) with value k
+  auto emit = [&](int node, T k, T uval) {
+    const long long gi = gid * NC + node;
+    if constexpr (MODE == kApply) {
+      P.dst[gi] = k;
+    } else {
+      const T u = (MODE == kStageFirst) ? uval : (uu_all ? uu_all[lc * NC + node] : P.uin[gi]);
+      P.dst[gi] = fma(P.fb, k, u);
+      if constexpr (MODE != kStageLast) P.tout[gi] = fma(P.fa, k, u);
+    }
   };
 
   // phases of two directions; each line: out += (a/h) [G u + upwind face terms]
@@ -85,6 +87,26 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
     for (int item = tl; item < nitems; item += TPC) {
       const int base = item_base<D, N>(item, dA, dB);
       if (dB >= 0) {
+        // scales and the upwind values of every line, issued first; both
+        // neighbours' face values are loaded (independent of the scale's
+        // sign, so no load waits for another) and the upwind one is selected
+        T scA[N], scB[N], upA[N], upB[N];
+#pragma unroll
+        for (int b = 0; b < N; ++b) {
+          const int bn = base + b * strideB;
+          scA[b] = valid ? line_scale(dA, bn) : T(0);
+          const T l = valid ? __ldg(P.src + nbL[dA] * NC + bn + (N - 1) * strideA) : T(0);
+          const T r = valid ? __ldg(P.src + nbR[dA] * NC + bn) : T(0);
+          upA[b] = scA[b] > T(0) ? l : r;
+        }
+#pragma unroll
+        for (int a = 0; a < N; ++a) {
+          const int bn = base + a * strideA;
+          scB[a] = valid ? line_scale(dB, bn) : T(0);
+          const T l = valid ? __ldg(P.src + nbL[dB] * NC + bn + (N - 1) * strideB) : T(0);
+          const T r = valid ? __ldg(P.src + nbR[dB] * NC + bn) : T(0);
+          upB[a] = scB[a] > T(0) ? l : r;
+        }
         T uu[N][N], acc[N][N];
 #pragma unroll
         for (int a = 0; a < N; ++a)
@@ -95,11 +117,9 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
             acc[a][b] = ph == 0 ? T(0) : so[node];
           }
         if (valid) {
-          // direction A: lines indexed by b
 #pragma unroll
           for (int b = 0; b < N; ++b) {
-            const int bn = base + b * strideB;
-            const T sc = line_scale(dA, bn);
+            const T sc = scA[b];
 #pragma unroll
             for (int i = 0; i < N; ++i) {
               T s = T(0);
@@ -107,23 +127,17 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
               for (int q = 0; q < N; ++q) s = fma(Lk.G[i * N + q], uu[q][b], s);
               acc[i][b] = fma(sc, s, acc[i][b]);
             }
-            const bool pos = sc > T(0);
-            const T up = __ldg(P.src + (pos ? nbL[dA] * NC + bn + (N - 1) * strideA : nbR[dA] * NC + bn));
-            if (sc != T(0)) {
-              if (pos) {
-                acc[N - 1][b] = fma(-sc * Lk.winvk, uu[N - 1][b], acc[N - 1][b]);
-                acc[0][b] = fma(sc * Lk.winv0, up, acc[0][b]);
-              } else {
-                acc[0][b] = fma(sc * Lk.winv0, uu[0][b], acc[0][b]);
-                acc[N - 1][b] = fma(-sc * Lk.winvk, up, acc[N - 1][b]);
-              }
+            if (sc > T(0)) {
+              acc[N - 1][b] = fma(-sc * Lk.winvk, uu[N - 1][b], acc[N - 1][b]);
+              acc[0][b] = fma(sc * Lk.winv0, upA[b], acc[0][b]);
+            } else if (sc < T(0)) {
+              acc[0][b] = fma(sc * Lk.winv0, uu[0][b], acc[0][b]);
+              acc[N - 1][b] = fma(-sc * Lk.winvk, upA[b], acc[N - 1][b]);
             }
           }
-          // direction B: lines indexed by a
 #pragma unroll
           for (int a = 0; a < N; ++a) {
-            const int bn = base + a * strideA;
-            const T sc = line_scale(dB, bn);
+            const T sc = scB[a];
 #pragma unroll
             for (int i = 0; i < N; ++i) {
               T s = T(0);
@@ -131,16 +145,12 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
               for (int q = 0; q < N; ++q) s = fma(Lk.G[i * N + q], uu[a][q], s);
               acc[a][i] = fma(sc, s, acc[a][i]);
             }
-            const bool pos = sc > T(0);
-            const T up = __ldg(P.src + (pos ? nbL[dB] * NC + bn + (N - 1) * strideB : nbR[dB] * NC + bn));
-            if (sc != T(0)) {
-              if (pos) {
-                acc[a][N - 1] = fma(-sc * Lk.winvk, uu[a][N - 1], acc[a][N - 1]);
-                acc[a][0] = fma(sc * Lk.winv0, up, acc[a][0]);
-              } else {
-                acc[a][0] = fma(sc * Lk.winv0, uu[a][0], acc[a][0]);
-                acc[a][N - 1] = fma(-sc * Lk.winvk, up, acc[a][N - 1]);
-              }
+            if (sc > T(0)) {
+              acc[a][N - 1] = fma(-sc * Lk.winvk, uu[a][N - 1], acc[a][N - 1]);
+              acc[a][0] = fma(sc * Lk.winv0, upB[a], acc[a][0]);
+            } else if (sc < T(0)) {
+              acc[a][0] = fma(sc * Lk.winv0, uu[a][0], acc[a][0]);
+              acc[a][N - 1] = fma(-sc * Lk.winvk, upB[a], acc[a][N - 1]);
             }
           }
         }
@@ -153,7 +163,7 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
 #pragma unroll
           for (int a = 0; a < N; ++a)
 #pragma unroll
-            for (int b = 0; b < N; ++b) P.dst[gid * NC + base + a * strideA + b * strideB] = acc[a][b];
+            for (int b = 0; b < N; ++b) emit(base + a * strideA + b * strideB, acc[a][b], uu[a][b]);
         }
       } else {
         T uu[N], acc[N];
@@ -164,6 +174,7 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
         }
         if (valid) {
           const T sc = line_scale(dA, base);
+          const T up = __ldg(P.src + (sc > T(0) ? nbL[dA] * NC + base + (N - 1) * strideA : nbR[dA] * NC + base));
 #pragma unroll
           for (int i = 0; i < N; ++i) {
             T s = T(0);
@@ -171,16 +182,12 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
             for (int q = 0; q < N; ++q) s = fma(Lk.G[i * N + q], uu[q], s);
             acc[i] = fma(sc, s, acc[i]);
           }
-          const bool pos = sc > T(0);
-          const T up = __ldg(P.src + (pos ? nbL[dA] * NC + base + (N - 1) * strideA : nbR[dA] * NC + base));
-          if (sc != T(0)) {
-            if (pos) {
-              acc[N - 1] = fma(-sc * Lk.winvk, uu[N - 1], acc[N - 1]);
-              acc[0] = fma(sc * Lk.winv0, up, acc[0]);
-            } else {
-              acc[0] = fma(sc * Lk.winv0, uu[0], acc[0]);
-              acc[N - 1] = fma(-sc * Lk.winvk, up, acc[N - 1]);
-            }
+          if (sc > T(0)) {
+            acc[N - 1] = fma(-sc * Lk.winvk, uu[N - 1], acc[N - 1]);
+            acc[0] = fma(sc * Lk.winv0, up, acc[0]);
+          } else if (sc < T(0)) {
+            acc[0] = fma(sc * Lk.winv0, uu[0], acc[0]);
+            acc[N - 1] = fma(-sc * Lk.winvk, up, acc[N - 1]);
           }
         }
         if (!last) {
@@ -188,7 +195,7 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
           for (int a = 0; a < N; ++a) so[base + a * strideA] = acc[a];
         } else if (valid) {
 #pragma unroll
-          for (int a = 0; a < N; ++a) P.dst[gid * NC + base + a * strideA] = acc[a];
+          for (int a = 0; a < N; ++a) emit(base + a * strideA, acc[a], uu[a]);
         }
       }
     }
@@ -196,34 +203,101 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
   }
 }
 
+template <int D, int N, typename T, int MODE>
+__global__ void __launch_bounds__(EclShape<D, N, T>::THREADS, EclShape<D, N, T>::MINB)
+    vp_adv_kernel(const __grid_constant__ VpAdvParams<T> P, const __grid_constant__ VpLine<T> Lk, int cpb) {
+  using S = EclShape<D, N, T>;
+  constexpr int NC = S::NC, TPC = S::TPC;
+  constexpr bool SU = EclStaging<D, N, T, MODE>::STAGE_U;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const long long bufe = ecl_buffer_elems<D, N, T>(cpb);
+  T* const s_in0 = reinterpret_cast<T*>(smem_raw);
+  T* const s_in1 = s_in0 + bufe;
+  T* const s_o = s_in0 + 2 * bufe;
+  T* const s_u0 = s_in0 + 3 * bufe;
+  T* const s_u1 = s_in0 + 4 * bufe;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int lc = tid / TPC, tl = tid % TPC;
+  const long long n_cells = P.g.n_cells;
+  const long long nblk = (n_cells + cpb - 1) / cpb;
+  auto stage = [&](T* dst, T* dstu, long long blk) {
+    const long long c0 = blk * cpb;
+    const long long ncell = (n_cells - c0) < cpb ? (n_cells - c0) : cpb;
+    stage_async(dst, P.src + c0 * NC, ncell * NC, tid, nthr);
+    if constexpr (SU) stage_async(dstu, P.uin + c0 * NC, ncell * NC, tid, nthr);
+  };
+  long long b = blockIdx.x;
+  if (b < nblk) stage(s_in0, s_u0, b);
+  cp_async_commit();
+  bool odd = false;
+  for (; b < nblk; b += gridDim.x) {
+    T* const cur = odd ? s_in1 : s_in0;
+    T* const nxt = odd ? s_in0 : s_in1;
+    T* const curu = odd ? s_u1 : s_u0;
+    T* const nxtu = odd ? s_u0 : s_u1;
+    const long long nb = b + gridDim.x;
+    if (nb < nblk) stage(nxt, nxtu, nb);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    vp_block<D, N, T, MODE>(P, Lk, b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+    __syncthreads();
+    odd = !odd;
+  }
+  cp_async_wait<0>();
+}
+
 template <int D, int N, typename T>
-static cudaError_t launch_vp_dn(const VpAdvParams<T>& P, cudaStream_t s) {
+static cudaError_t launch_vp_dn(const VpAdvParams<T>& P, int mode, cudaStream_t s) {
   using S = EclShape<D, N, T>;
   if constexpr (!S::SUPPORTED) {
     return cudaErrorNotSupported;
   } else {
-    constexpr size_t kSmem = size_t(2) * S::CPB * S::NC * sizeof(T);  // cell tile + accumulator tile
+    if (mode < kApply || mode > kStageLast) return cudaErrorInvalidValue;
     VpLine<T> Lk;
     for (int i = 0; i < N * N; ++i) Lk.G[i] = T(P.g.G[i]);
     Lk.winv0 = T(1.0 / P.g.glw[0]);
     Lk.winvk = T(1.0 / P.g.glw[N - 1]);
-    static bool attr = false;
-    if (!attr) {
-      cudaError_t e = cudaFuncSetAttribute(vp_adv_kernel<D, N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           int(kSmem));
+    const int nbuf = mode == kStageMid ? EclStaging<D, N, T, kStageMid>::NBUF
+                     : mode == kStageLast ? EclStaging<D, N, T, kStageLast>::NBUF : 3;
+    // measured on GB300: FP32 is fastest with the largest tile, FP64 with the default one
+    int cpb = sizeof(T) == 4 ? S::CPB : ecl_default_cpb<D, N, T>();
+    while (cpb > 1 && size_t(nbuf * ecl_buffer_elems<D, N, T>(cpb)) * sizeof(T) > 220 * 1024) --cpb;
+    const int threads = S::TPC * cpb;
+    const size_t smem = size_t(nbuf * ecl_buffer_elems<D, N, T>(cpb)) * sizeof(T);
+    static bool attr_done[4] = {false, false, false, false};
+    static int sms = 0;
+    auto go = [&](auto kern) -> cudaError_t {
+      if (!attr_done[mode]) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        attr_done[mode] = true;
+      }
+      int per_sm = 0;
+      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
       if (e != cudaSuccess) return e;
-      attr = true;
+      if (per_sm < 1) per_sm = 1;
+      const long long nblk = (P.g.n_cells + cpb - 1) / cpb;
+      const long long want = (long long)sms * per_sm;
+      kern<<<unsigned(nblk < want ? nblk : want), threads, smem, s>>>(P, Lk, cpb);
+      return cudaGetLastError();
+    };
+    switch (mode) {
+      case kApply: return go(vp_adv_kernel<D, N, T, kApply>);
+      case kStageFirst: return go(vp_adv_kernel<D, N, T, kStageFirst>);
+      case kStageMid: return go(vp_adv_kernel<D, N, T, kStageMid>);
+      default: return go(vp_adv_kernel<D, N, T, kStageLast>);
     }
-    const unsigned grid = unsigned((P.g.n_cells + S::CPB - 1) / S::CPB);
-    vp_adv_kernel<D, N, T><<<grid, S::THREADS, kSmem, s>>>(P, Lk);
-    return cudaGetLastError();
   }
 }
 
 template <typename T>
-static cudaError_t launch_vp_any(const VpAdvParams<T>& P, cudaStream_t s) {
+static cudaError_t launch_vp_any(const VpAdvParams<T>& P, int mode, cudaStream_t s) {
 #define HD_VP_CASE(DD, NN) \
-  if (P.g.D == DD && P.g.N == NN) return launch_vp_dn<DD, NN, T>(P, s);
+  if (P.g.D == DD && P.g.N == NN) return launch_vp_dn<DD, NN, T>(P, mode, s);
   HD_VP_CASE(2, 2) HD_VP_CASE(2, 3) HD_VP_CASE(2, 4) HD_VP_CASE(2, 5) HD_VP_CASE(2, 6)
   HD_VP_CASE(4, 2) HD_VP_CASE(4, 3) HD_VP_CASE(4, 4) HD_VP_CASE(4, 5) HD_VP_CASE(4, 6)
   HD_VP_CASE(6, 2) HD_VP_CASE(6, 3) HD_VP_CASE(6, 4)
@@ -231,7 +305,11 @@ static cudaError_t launch_vp_any(const VpAdvParams<T>& P, cudaStream_t s) {
   return cudaErrorNotSupported;
 }
 
-cudaError_t launch_vp_advection(const VpAdvParams<float>& P, cudaStream_t s) { return launch_vp_any(P, s); }
-cudaError_t launch_vp_advection(const VpAdvParams<double>& P, cudaStream_t s) { return launch_vp_any(P, s); }
+cudaError_t launch_vp_advection(const VpAdvParams<float>& P, int mode, cudaStream_t s) {
+  return launch_vp_any(P, mode, s);
+}
+cudaError_t launch_vp_advection(const VpAdvParams<double>& P, int mode, cudaStream_t s) {
+  return launch_vp_any(P, mode, s);
+}
 
 }  // namespace hd

@@ -24,7 +24,8 @@ import torch
 
 from . import _lib
 from ._lib import HdError, check
-from .advection import Function, LowStorageRungeKuttaIntegrator, TimeLoop, _ptr, _stream, time_step_rule
+from .advection import (Function, LowStorageRungeKuttaIntegrator, TimeLoop, _ptr, _stream, _swap_storage,
+                        time_step_rule)
 
 __all__ = ["VlasovPoissonParameters", "VlasovPoissonOperation", "perturbed_maxwellian", "run_hyperrectangle",
            "learn_loss_grad"]
@@ -137,11 +138,24 @@ class VlasovPoissonOperation:
 
     def perform_time_step(self, rk: LowStorageRungeKuttaIntegrator, solution: torch.Tensor, time: float,
                           dt: float) -> None:
-        """One LSRK step with this operator entirely inside the library (hd_vp_lsrk_step)."""
+        """One LSRK step with this operator entirely inside the library: the stage update fused
+        into the advection kernel (hd_vp_lsrk_step_fused; the storages of solution and vec_Ki
+        rotate as in LowStorageRungeKuttaIntegrator) unless the integrator was made with
+        fused=False (hd_vp_lsrk_step: the reference's unfused stage sequence)."""
         for v, n in ((solution, "solution"), (rk.vec_Ki, "vec_Ki"), (rk.vec_Ti, "vec_Ti")):
             self._check_vec(v, n)
-        check(self._L.hd_vp_lsrk_step(self._h, rk._h, _ptr(solution), _ptr(rk.vec_Ki), _ptr(rk.vec_Ti),
-                                      float(time), float(dt), _stream()))
+        if not rk.fused:
+            check(self._L.hd_vp_lsrk_step(self._h, rk._h, _ptr(solution), _ptr(rk.vec_Ki), _ptr(rk.vec_Ti),
+                                          float(time), float(dt), _stream()))
+            return
+        X = [ctypes.c_void_p(solution.data_ptr()), ctypes.c_void_p(rk.vec_Ki.data_ptr()),
+             ctypes.c_void_p(rk.vec_Ti.data_ptr())]
+        orig = [x.value for x in X]
+        check(self._L.hd_vp_lsrk_step_fused(self._h, rk._h, ctypes.byref(X[0]), ctypes.byref(X[1]),
+                                            ctypes.byref(X[2]), float(time), float(dt), _stream()))
+        if X[0].value != orig[0]:
+            assert X[0].value == orig[1] and X[1].value == orig[0]
+            _swap_storage(solution, rk.vec_Ki)
 
     def fields(self) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
         """(rho, phi, E) of the last evaluation; E[(cell_x * n^dim_x + node) * dim_x + d] = d_d phi."""

@@ -305,6 +305,11 @@ int hd_vp_apply(hd_vp *vp, void *dst, const void *src, double time, void *stream
  * (time_integrators.templates.h:91-184, unfused) */
 int hd_vp_lsrk_step(hd_vp *vp, const hd_lsrk *rk, void *sol, void *Ki, void *Ti, double time, double dt,
                     void *stream);
+/* the same step with the stage update fused into the advection kernel; the
+ * three vectors rotate roles as in hd_lsrk_step (the new solution is in
+ * *sol on return) */
+int hd_vp_lsrk_step_fused(hd_vp *vp, const hd_lsrk *rk, void **sol, void **Ki, void **Ti, double time, double dt,
+                          void *stream);
 /* out: field energy int (d_d phi)^2 per x-direction, mass, L2 norm, kinetic
  * energy int |v|^2 f, momentum int v_d f per v-direction (diagnostics.h:28-141);
  * the field is the one of the last right-hand-side evaluation */

@@ -196,3 +196,21 @@ def test_rhs_relative_tolerance():
         assert np.linalg.norm(O.poisson_apply(prob, phi) - rhs) <= 1.01e-9 * np.linalg.norm(rhs)
         st = op.cg_stats()
         assert st["solves"] == 11 and st["total_iterations"] >= st["last_iterations"]
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_fused_step_equals_unfused(dtype):
+    """hd_vp_lsrk_step_fused (stage update inside the advection kernel, rotating vectors) against the
+    reference's unfused stage sequence (hd_vp_lsrk_step)."""
+    dim_x, degree, cx, cv = 2, 3, 4, 6
+    out = {}
+    for fused in (True, False):
+        op, _ = _setup(dim_x, degree, cx, cv, dtype=dtype, guess="zero")
+        f = op.initialize_dof_vector()
+        op.interpolate(V.perturbed_maxwellian(dim_x, eps=0.05, perturbed_dims=(0, 1)), f)
+        Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
+        integ = V.LowStorageRungeKuttaIntegrator(Ki, Ti, "rk45", fused=fused)
+        for s in range(4):
+            op.perform_time_step(integ, f, s * 1e-3, 1e-3)
+        out[fused] = f.double().cpu().numpy()
+    assert _rel(out[True], out[False]) <= (1e-12 if dtype == "f64" else 2e-6)
