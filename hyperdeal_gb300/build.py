@@ -58,7 +58,7 @@ def _generate_units() -> list:
     for fam, header, ret, factory, D, N in GEN_UNITS:
         path = os.path.join(gen, "%s_%d_%d.cu" % (fam, D, N))
         text = ('#include "%s"\nnamespace hd {\n%s %s_launchers_%d_%d() { return %s<%d, %d>(); }\n}\n'
-                % (os.path.join(CSRC, header), ret, fam, D, N, factory, D, N))
+                % (header, ret, fam, D, N, factory, D, N))
         if not os.path.exists(path) or open(path).read() != text:
             with open(path, "w") as f:
                 f.write(text)
@@ -70,7 +70,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     """Compile and link the library; returns its path."""
     os.makedirs(BUILD_DIR, exist_ok=True)
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu"))) + _generate_units()
-    flags = ARCH + NVCC_FLAGS
+    flags = ARCH + NVCC_FLAGS + ["-I", CSRC]
     stamp = os.path.join(OUT_DIR, ".stamp")
     digest = _deps_hash(" ".join(flags))
     if not force and os.path.exists(LIB_PATH) and os.path.exists(stamp) and open(stamp).read() == digest:

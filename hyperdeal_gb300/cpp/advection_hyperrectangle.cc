@@ -6,10 +6,11 @@
 //
 // Prints the diagnostics lines of the reference ("Time, norm, error" at every
 // DiagnosticsTick) so its output can be compared with the reference's .out
-// files.  Gauss-Lobatto collocation only (DoCollocation = true).
+// files.  Gauss-Lobatto collocation (DoCollocation = true) or, with the
+// `gauss` argument, Gauss quadrature.
 //
 // usage: advection_hyperrectangle dim_x dim_v degree subdivisions periodic(0|1)
-//                                 final_time rk_type [f64|f32] [time_step cfl tick]
+//                                 final_time rk_type [f64|f32] [time_step cfl tick] [gauss]
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -22,7 +23,7 @@ using namespace hyperdeal_gb300;
 
 template <typename Number>
 int run(int dim_x, int dim_v, int degree, int subdivisions, bool periodic, double final_time, const std::string& rk,
-        double time_step, double cfl, double tick) {
+        double time_step, double cfl, double tick, bool gauss) {
   const int dim = dim_x + dim_v;
   // ExactSolution: sin(2 pi (x0 - a0 t)) prod_{d>=1} cos(2 pi (x_d - a_d t)), a = (1, 0.15, -0.05, 0, ...),
   // domain [-1, 1]^dim, Dirichlet data = the exact solution (hyperrectangle.h:29-66, :220-235)
@@ -45,6 +46,7 @@ int run(int dim_x, int dim_v, int degree, int subdivisions, bool periodic, doubl
   for (int d = 0; d < dim; ++d) desc.velocity[d] = adv[d];
   desc.bc_kind = periodic ? HD_BC_HOMOGENEOUS : HD_BC_FUNCTION;
   desc.bc = exact;
+  desc.quadrature = gauss ? HD_QUAD_GAUSS : HD_QUAD_GAUSS_LOBATTO;
 
   AdvectionOperation<Number> op(desc);
   DeviceVector<Number> solution = op.create_vector(), Ki = op.create_vector(), Ti = op.create_vector();
@@ -84,9 +86,11 @@ int main(int argc, char** argv) {
   const double time_step = argc > 9 ? std::atof(argv[9]) : 0.1;
   const double cfl = argc > 10 ? std::atof(argv[10]) : 0.3;
   const double tick = argc > 11 ? std::atof(argv[11]) : 0.1;
+  const bool gauss = argc > 12 && std::string(argv[12]) == "gauss";
   try {
-    if (dtype == "f32") return run<float>(dim_x, dim_v, degree, sub, periodic, final_time, rk, time_step, cfl, tick);
-    return run<double>(dim_x, dim_v, degree, sub, periodic, final_time, rk, time_step, cfl, tick);
+    if (dtype == "f32")
+      return run<float>(dim_x, dim_v, degree, sub, periodic, final_time, rk, time_step, cfl, tick, gauss);
+    return run<double>(dim_x, dim_v, degree, sub, periodic, final_time, rk, time_step, cfl, tick, gauss);
   } catch (const std::exception& e) {
     std::fprintf(stderr, "error: %s\n", e.what());
     return 1;

@@ -571,6 +571,7 @@ struct hd_vp {
   double* d_dx;       // rho - rho_prev
   double* d_dy;       // phi - phi_prev
   bool have_prev;
+  long long observed;  // pairs given to the learned model
   double* d_judge;    // residual partials of the judge
   int cg_grid;
   int guess;
@@ -747,7 +748,9 @@ int solve_poisson(hd_vp* v, cudaStream_t s) {
   if (rc) return rc;
   // the solver's own (rho - rho_prev, phi - phi_prev) pair trains the learned guess
   hd::diff_kernel<<<nb, 256, 0, s>>>(nx, v->d_phi, v->d_phi_prev, v->d_dy);
-  rc = vcuda(hd::vp_model_observe(v->model, v->d_dx, v->d_dy, s), "learned guess update");
+  const int every = v->desc.learn_every > 0 ? v->desc.learn_every : 5;
+  rc = vcuda(hd::vp_model_observe(v->model, v->d_dx, v->d_dy, s, (v->observed++ % every) == 0),
+             "learned guess update");
   if (!rc) rc = vcuda(cudaMemcpyAsync(v->d_rho_prev, v->d_rho, sizeof(double) * nx, cudaMemcpyDeviceToDevice, s),
                       "previous density");
   if (rc) return rc;

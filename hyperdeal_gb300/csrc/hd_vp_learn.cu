@@ -284,11 +284,12 @@ cudaError_t vp_model_predict(VpModel* m, const double* rho, double* phi_out, cud
   return cudaGetLastError();
 }
 
-cudaError_t vp_model_observe(VpModel* m, const double* rho, const double* phi, cudaStream_t s) {
+cudaError_t vp_model_observe(VpModel* m, const double* rho, const double* phi, cudaStream_t s, bool train) {
   const long long n = m->n;
   store_pair<<<1, 1024, 0, s>>>(n, rho, phi, m->X, m->Y, m->head);
   m->head = (m->head + 1) % m->H;
   if (m->count < m->H) ++m->count;
+  if (!train) return cudaGetLastError();
   const int B = m->count;
   const size_t nw = size_t(2) * m->r * n;
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;

@@ -21,8 +21,8 @@ void vp_model_destroy(VpModel* m);
 bool vp_model_ready(const VpModel* m);
 // y_out = model(x) (FP64 in / out; mean-free)
 cudaError_t vp_model_predict(VpModel* m, const double* x, double* y_out, cudaStream_t s);
-// store the pair and run the configured number of Adam steps
-cudaError_t vp_model_observe(VpModel* m, const double* x, const double* y, cudaStream_t s);
+// store the pair; with `train`, run the configured number of Adam steps
+cudaError_t vp_model_observe(VpModel* m, const double* x, const double* y, cudaStream_t s, bool train = true);
 long long vp_model_steps(const VpModel* m);
 
 // loss = 1/(2B) sum_b ||W2 W1 x_b - y_b||^2 (skipped when loss is null) and its gradients (device pointers, column-major

@@ -51,6 +51,7 @@ class VlasovPoissonParameters:
     learn_rank: int = 0
     learn_history: int = 0
     cg_rhs_relative: bool = False  # False: ||r|| <= cg_tol ||r_0|| as deal.II's ReductionControl
+    learn_every: int = 0  # Adam steps every n-th solve (0: 5)
 
     def c(self) -> _lib.hd_vp_desc:
         d = _lib.hd_vp_desc()
@@ -68,6 +69,7 @@ class VlasovPoissonParameters:
         d.learn_rank = int(self.learn_rank)
         d.learn_history = int(self.learn_history)
         d.cg_rhs_relative = int(bool(self.cg_rhs_relative))
+        d.learn_every = int(self.learn_every)
         return d
 
 

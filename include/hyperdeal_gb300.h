@@ -287,6 +287,9 @@ typedef struct hd_vp_desc {
   int cg_rhs_relative;  /* 1: tolerance relative to ||rhs|| -- a fixed
                            accuracy, so a better initial guess saves
                            iterations                                         */
+  int learn_every;      /* the learned guess stores every solve's pair and
+                           takes its Adam steps every learn_every-th solve
+                           (0: 5, once per rk45 step)                         */
 } hd_vp_desc;
 
 typedef struct hd_vp hd_vp;

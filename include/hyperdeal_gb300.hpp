@@ -10,6 +10,9 @@
 //       source/base/time_loop.cc:33-67
 //   VectorTools::interpolate / norm_and_error
 //       include/hyper.deal/numerics/vector_tools.h:81-223
+//   VlasovPoissonOperation (the right-hand side of the Vlasov-Poisson
+//   application: moments, Poisson solve, field, advection)
+//       examples/vlasov_poisson/include/application.h:516-602
 //
 // Vectors are DeviceVector<Number> (device memory, the reference's DoF
 // numbering).  Errors throw std::runtime_error with hd_last_error()'s message,
@@ -143,6 +146,12 @@ class AdvectionOperation {
 
   long long n_dofs() const { return hd_adv_n_dofs(h_); }
   double critical_time_step() const { return hd_adv_critical_time_step(h_); }
+  // pick the generic kernel's tile by timing (src read, dst overwritten)
+  void autotune(const DeviceVector<Number>& src, DeviceVector<Number>& dst, int reps = 3) {
+    int c = 0, p = 0;
+    double ms = 0.0;
+    check(hd_adv_autotune(h_, src.data(), dst.data(), reps, &c, &p, &ms, stream_));
+  }
   hd_adv* handle() const { return h_; }
   cudaStream_t stream() const { return stream_; }
   DeviceVector<Number> create_vector() const { return DeviceVector<Number>(n_dofs()); }
@@ -151,6 +160,60 @@ class AdvectionOperation {
   hd_adv* h_ = nullptr;
   cudaStream_t stream_;
 };
+
+// The Vlasov-Poisson right-hand side f -> A(f) with the field of f
+// (application.h:516-602); Gauss-Lobatto collocation, periodic meshes.
+template <typename Number>
+class VlasovPoissonOperation {
+ public:
+  explicit VlasovPoissonOperation(hd_vp_desc desc, cudaStream_t stream = nullptr)
+      : stream_(stream), dim_x_(desc.dim_x) {
+    desc.dtype = dtype_of<Number>::value;
+    check(hd_vp_create(&desc, &h_));
+  }
+  ~VlasovPoissonOperation() { hd_vp_destroy(h_); }
+  VlasovPoissonOperation(const VlasovPoissonOperation&) = delete;
+  VlasovPoissonOperation& operator=(const VlasovPoissonOperation&) = delete;
+
+  // dst = A(src) with the field of src (moments, Poisson solve, field, advection)
+  void apply(DeviceVector<Number>& dst, const DeviceVector<Number>& src, const Number time) const {
+    check(hd_vp_apply(h_, dst.data(), src.data(), double(time), stream_));
+  }
+  void operator()(const DeviceVector<Number>& src, DeviceVector<Number>& dst, const Number time) const {
+    apply(dst, src, time);
+  }
+  void interpolate(const hd_function& f, DeviceVector<Number>& dst, double time = 0.0) const {
+    check(hd_vp_interpolate(h_, &f, time, dst.data(), stream_));
+  }
+  // field energy per x-direction, mass, L2 norm, kinetic energy, momentum per
+  // v-direction (diagnostics.h:28-141); the field is the last evaluation's
+  std::vector<double> diagnostics(const DeviceVector<Number>& f) const {
+    std::vector<double> out(size_t(2 * dim_x_ + 3), 0.0);
+    check(hd_vp_diagnostics(h_, f.data(), out.data(), stream_));
+    return out;
+  }
+  long long n_dofs() const { return hd_vp_n_dofs(h_); }
+  hd_vp* handle() const { return h_; }
+  cudaStream_t stream() const { return stream_; }
+  DeviceVector<Number> create_vector() const { return DeviceVector<Number>(n_dofs()); }
+
+ private:
+  hd_vp* h_ = nullptr;
+  cudaStream_t stream_;
+  int dim_x_;
+};
+
+// perturbed Maxwellian (1 + amp prod_{d in pert} cos(k x_d)) prod_v exp(-v^2/2)/sqrt(2 pi)
+// (examples/vlasov_poisson/cases/hyperrectangle.h:45-58)
+inline hd_function perturbed_maxwellian(int dim_x, double amp, double k, const std::vector<int>& perturbed_dims) {
+  hd_function f{};
+  f.kind = 3;
+  f.amp = amp;
+  for (int d = 0; d < dim_x; ++d) f.omega[d] = k;
+  for (int d : perturbed_dims) f.cosine[d] = 1;
+  for (int d = 0; d < dim_x; ++d) f.cosine[dim_x + d] = 2;
+  return f;
+}
 
 template <typename Number>
 class LowStorageRungeKuttaIntegrator {
@@ -183,6 +246,18 @@ class LowStorageRungeKuttaIntegrator {
     void* t = Ti_.data();
     void* ki_storage = k;
     check(hd_lsrk_step(op.handle(), rk_, &s, &k, &t, double(current_time), double(time_step), op.stream()));
+    if (s == ki_storage) solution.swap(Ki_);
+  }
+
+  // The Vlasov-Poisson operator: the stage update fused into its advection
+  // kernel (hd_vp_lsrk_step_fused), vectors rotating as above.
+  void perform_time_step(DeviceVector<Number>& solution, const Number current_time, const Number time_step,
+                         const VlasovPoissonOperation<Number>& op) {
+    void* s = solution.data();
+    void* k = Ki_.data();
+    void* t = Ti_.data();
+    void* ki_storage = k;
+    check(hd_vp_lsrk_step_fused(op.handle(), rk_, &s, &k, &t, double(current_time), double(time_step), op.stream()));
     if (s == ki_storage) solution.swap(Ki_);
   }
 

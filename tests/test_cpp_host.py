@@ -44,3 +44,42 @@ def test_cpp_application_reproduces_reference_golden(name, args):
     assert r32.returncode == 0, r32.stderr
     for (t, n, e), (t2, n2, e2) in zip(rows, _rows(r32.stdout)):
         assert abs(n2 - n) / n < 1e-5
+
+
+@pytest.mark.gpu
+def test_cpp_application_gauss_golden():
+    """A Gauss-quadrature golden (adv_2D_2D_k3.hyperrectangle_01, periodic) from the C++ host."""
+    exe = B.build_cpp_app()
+    r = subprocess.run([exe, "2", "2", "3", "4", "1", "1.0", "rk45", "f64", "0.1", "0.3", "0.1", "gauss"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    rows = _rows(r.stdout)
+    ref = [c for c in GOLD["advection"] if c["name"] == "adv_2D_2D_k3.hyperrectangle_01"][0]["rows"]
+    assert len(rows) == len(ref)
+    for (t, n, e), (rt, rn, re_) in zip(rows, ref):
+        assert abs(n - rn) <= max(1e-5, 1e-8 * abs(rn))
+        assert abs(e - re_) <= max(1e-5, 1e-8 * abs(re_))
+
+
+def test_cpp_vp_application_builds_and_reports_usage():
+    exe = B.build_cpp_app("vlasov_poisson_hyperrectangle")
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 2 and "usage" in r.stderr
+
+
+@pytest.mark.gpu
+def test_cpp_vp_application_matches_oracle():
+    """The Vlasov-Poisson application through the C++ interface against the oracle's run of the same
+    case (collocation, 1x1v k=3, 8x8 cells)."""
+    from oracle import oracle as O
+    exe = B.build_cpp_app("vlasov_poisson_hyperrectangle")
+    r = subprocess.run([exe, "1", "3", "8", "8", "0.05", "f64", "0.05", "0.01"], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr
+    rows = _rows(r.stdout)
+    rows_o, _ = O.run_vp_hyperrectangle(1, 1, 3, 8, 8, collocation=True, final_time=0.05, tick=0.01)
+    assert len(rows) == len(rows_o) and len(rows) >= 5
+    for a, b in zip(rows, rows_o):
+        assert abs(a[0] - b[0]) <= 1e-12
+        for x, y in zip(a[1:], b[1:]):
+            assert abs(x - y) <= 1e-8 * abs(y) + 1e-12
