@@ -75,8 +75,8 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS, EclShape<D, N, T>:
     const EclParams<T>& P = params[inst];
     const long long c0 = lb * cpb;
     const long long ncell = (P.n_cells - c0) < cpb ? (P.n_cells - c0) : cpb;
-    stage_async(dst, P.tin + c0 * NC, ncell * NC, tid, nthr);
-    if constexpr (SU) stage_async(dstu, P.uin + c0 * NC, ncell * NC, tid, nthr);
+    stage_cells<D, N, T>(dst, P.tin + c0 * NC, ncell, tid, nthr);
+    if constexpr (SU) stage_cells<D, N, T>(dstu, P.uin + c0 * NC, ncell, tid, nthr);
   };
   long long b = blockIdx.x;
   int inst = 0;

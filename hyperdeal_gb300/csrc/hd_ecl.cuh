@@ -1,11 +1,11 @@
 // hd_ecl.cuh -- element-centric (ECL) upwind-DG advection kernels for sm_103a.
 //
-// One CTA owns CPB whole cells.  Each cell's (k+1)^D nodal values are staged
-// in shared memory with coalesced 16-byte loads; the D one-dimensional line
-// operators are applied two directions at a time ("plane phases") with the
-// plane's N x N values held in registers, and the upwind neighbour's face
-// trace is read straight from global memory (L2) -- there is no face loop and
-// no atomics.  The inverse (diagonal) mass, the upwind flux and the downwind
+// Persistent CTAs walk blocks of whole cells.  Each block's (k+1)^D nodal
+// values per cell are staged in shared memory by 16-byte cp.async copies one
+// block ahead; the D one-dimensional line operators are applied two
+// directions at a time ("plane phases") with the plane's N x N values held
+// in registers, and the upwind neighbour's face trace is read from global
+// memory (L2) -- there is no face loop and no atomics.  The inverse (diagonal) mass, the upwind flux and the downwind
 // self-term are folded into the per-direction line operator M_d and the
 // inflow coefficient c_d that the host derives from the reference's formulas,
 // so one phase does  acc_line += M_d u_line  and  acc[in_node] += c_d u+.
@@ -103,9 +103,33 @@ struct EclShape {
   static constexpr bool SUPPORTED = SMEM + 48 <= 220 * 1024;
 };
 
-// shared-memory index of node i (identity layout)
+// Per-cell stride of the shared-memory tiles: when cells share a warp (fewer
+// than 32 threads per cell) consecutive cells are offset by 64 extra bytes, so
+// that the same access of two cells falls into different banks.
 template <int D, int N, typename T>
-__device__ __forceinline__ int sidx(int i) { return i; }
+struct EclTile {
+  static constexpr int NC = ipow(N, D);
+  static constexpr bool PAD = EclShape<D, N, T>::TPC < 32 && (NC * sizeof(T)) % 16 == 0;
+  static constexpr int CST = NC + (PAD ? int(64 / sizeof(T)) : 0);
+};
+
+// 16-byte vector of T (shared-memory plane loads/stores)
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using type = float4;
+  static constexpr int n = 4;
+  __device__ static float get(const float4& v, int j) { return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w; }
+  __device__ static float4 make(const float* p) { return make_float4(p[0], p[1], p[2], p[3]); }
+};
+template <>
+struct Vec16<double> {
+  using type = double2;
+  static constexpr int n = 2;
+  __device__ static double get(const double2& v, int j) { return j == 0 ? v.x : v.y; }
+  __device__ static double2 make(const double* p) { return make_double2(p[0], p[1]); }
+};
 
 // node index of the plane/line base for work item `item` in phase with
 // directions (dA, dB) (dB = -1 for a single-direction phase): the digits of
@@ -182,8 +206,31 @@ __device__ __forceinline__ void stage_async(T* dst, const T* src, long long nval
 // shared-memory elements of one staging buffer (rounded to 16 bytes)
 template <int D, int N, typename T>
 __host__ __device__ constexpr long long ecl_buffer_elems(int cpb) {
-  const long long bytes = (long long)cpb * EclShape<D, N, T>::NC * sizeof(T);
+  const long long bytes = (long long)cpb * EclTile<D, N, T>::CST * sizeof(T);
   return ((bytes + 15) / 16) * 16 / (long long)sizeof(T);
+}
+
+// stage `ncell` consecutive cells into a shared buffer with the cell stride
+// of EclTile (16-byte copies when the source is 16-byte aligned)
+template <int D, int N, typename T>
+__device__ __forceinline__ void stage_cells(T* dst, const T* src, long long ncell, int tid, int nthreads) {
+  using TL = EclTile<D, N, T>;
+  if constexpr (!TL::PAD) {
+    stage_async(dst, src, ncell * TL::NC, tid, nthreads);
+  } else {
+    constexpr int VPV = 16 / sizeof(T), CPC = TL::NC / VPV;  // chunks per cell
+    if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+      for (long long v = tid; v < ncell * CPC; v += nthreads) {
+        const long long c = v / CPC;
+        cp_async_16(dst + c * TL::CST + (v - c * CPC) * VPV, src + v * VPV);
+      }
+    } else {
+      for (long long i = tid; i < ncell * TL::NC; i += nthreads) {
+        const long long c = i / TL::NC;
+        cp_async_small<sizeof(T)>(dst + c * TL::CST + (i - c * TL::NC), src + i);
+      }
+    }
+  }
 }
 
 // one block of P.cpb cells (the CTA's cells start at cell0) from the staged
@@ -210,8 +257,9 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
       else { cc[d] = int(gv % P.cells[d]); gv /= P.cells[d]; }
     }
   }
-  const T* su = su_all + lc * NC;
-  T* so = so_all + lc * NC;
+  constexpr int CST = EclTile<D, N, T>::CST;
+  const T* su = su_all + lc * CST;
+  T* so = so_all + lc * CST;
 
 #pragma unroll
   for (int ph = 0; ph < S::NPH; ++ph) {
@@ -240,14 +288,37 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
         for (int a = 0; a < N; ++a)
           upB[a] = nbB >= 0 ? __ldg(P.tin + nbB * NC + base + a * strideA + LB.nb_node * strideB) : T(0);
         T uu[N][N], acc[N][N];  // [a][b]: node base + a*strideA + b*strideB
+        // phase 0: the plane of directions 0, 1 is N*N contiguous values; when
+        // that is a whole number of 16-byte words it is read as such (far
+        // fewer shared-memory wavefronts than scalar loads of the strided plane)
+        // (not for the register-capped FP64 6D shapes: the extra live values spill)
+        constexpr bool kVec = (N * N * sizeof(T)) % 16 == 0 && !(sizeof(T) == 8 && D == 6);
+        if (kVec && ph == 0) {
+          using V = Vec16<T>;
+          T flat[N * N];
 #pragma unroll
-        for (int a = 0; a < N; ++a)
+          for (int k = 0; k < N * N / V::n; ++k) {
+            const typename V::type w = *reinterpret_cast<const typename V::type*>(su + base + k * V::n);
 #pragma unroll
-          for (int b = 0; b < N; ++b) {
-            const int node = base + a * strideA + b * strideB;
-            uu[a][b] = su[node];
-            acc[a][b] = ph == 0 ? T(0) : so[node];
+            for (int j = 0; j < V::n; ++j) flat[k * V::n + j] = V::get(w, j);
           }
+#pragma unroll
+          for (int a = 0; a < N; ++a)
+#pragma unroll
+            for (int b = 0; b < N; ++b) {
+              uu[a][b] = flat[a + N * b];
+              acc[a][b] = T(0);
+            }
+        } else {
+#pragma unroll
+          for (int a = 0; a < N; ++a)
+#pragma unroll
+            for (int b = 0; b < N; ++b) {
+              const int node = base + a * strideA + b * strideB;
+              uu[a][b] = su[node];
+              acc[a][b] = ph == 0 ? T(0) : so[node];
+            }
+        }
         if (actA) {
 #pragma unroll
           for (int b = 0; b < N; ++b) {
@@ -287,10 +358,22 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
           }
         }
         if (!last) {
+          if (kVec && ph == 0) {
+            using V = Vec16<T>;
+            T flat[N * N];
 #pragma unroll
-          for (int a = 0; a < N; ++a)
+            for (int a = 0; a < N; ++a)
 #pragma unroll
-            for (int b = 0; b < N; ++b) so[base + a * strideA + b * strideB] = acc[a][b];
+              for (int b = 0; b < N; ++b) flat[a + N * b] = acc[a][b];
+#pragma unroll
+            for (int k = 0; k < N * N / V::n; ++k)
+              *reinterpret_cast<typename V::type*>(so + base + k * V::n) = V::make(flat + k * V::n);
+          } else {
+#pragma unroll
+            for (int a = 0; a < N; ++a)
+#pragma unroll
+              for (int b = 0; b < N; ++b) so[base + a * strideA + b * strideB] = acc[a][b];
+          }
         } else if (valid) {
           const long long g0 = gid * NC;
 #pragma unroll
@@ -304,7 +387,7 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
               } else {
                 T u;
                 if constexpr (MODE == kStageFirst) u = uu[a][b];
-                else u = uu_all ? uu_all[lc * NC + base + a * strideA + b * strideB] : P.uin[gi];
+                else u = uu_all ? uu_all[lc * CST + base + a * strideA + b * strideB] : P.uin[gi];
                 P.uout[gi] = fma(P.fb, k, u);
                 if constexpr (MODE != kStageLast) P.tout[gi] = fma(P.fa, k, u);
               }
@@ -349,7 +432,7 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
             if constexpr (MODE == kApply) {
               P.uout[gi] = k;
             } else {
-              const T u = (MODE == kStageFirst) ? uu[a] : (uu_all ? uu_all[lc * NC + base + a * strideA] : P.uin[gi]);
+              const T u = (MODE == kStageFirst) ? uu[a] : (uu_all ? uu_all[lc * CST + base + a * strideA] : P.uin[gi]);
               P.uout[gi] = fma(P.fb, k, u);
               if constexpr (MODE != kStageLast) P.tout[gi] = fma(P.fa, k, u);
             }
@@ -394,8 +477,8 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS, EclShape<D, N, T>:
   auto stage = [&](T* dst, T* dstu, long long blk) {
     const long long c0 = blk * cpb;
     const long long ncell = (P.n_cells - c0) < cpb ? (P.n_cells - c0) : cpb;
-    stage_async(dst, P.tin + c0 * NC, ncell * NC, tid, nthr);
-    if constexpr (SU) stage_async(dstu, P.uin + c0 * NC, ncell * NC, tid, nthr);
+    stage_cells<D, N, T>(dst, P.tin + c0 * NC, ncell, tid, nthr);
+    if constexpr (SU) stage_cells<D, N, T>(dstu, P.uin + c0 * NC, ncell, tid, nthr);
   };
   long long b = blockIdx.x;
   if (b < nblk) stage(s_in0, s_u0, b);

@@ -41,6 +41,13 @@ struct GaussShape {
   static constexpr bool SUPPORTED = size_t(5) * CPB * NC * sizeof(T) + 48 <= 220 * 1024;
 };
 
+// elements of one (unpadded) cell tile buffer of this path, rounded to 16 bytes
+template <int D, int N, typename T>
+__host__ __device__ constexpr long long gauss_buffer_elems(int cpb) {
+  const long long bytes = (long long)cpb * EclShape<D, N, T>::NC * sizeof(T);
+  return ((bytes + 15) / 16) * 16 / (long long)sizeof(T);
+}
+
 // apply the N x N matrix A (row-major, A[i*N + q]) along direction e to every
 // line of the cell tile x (in place); threads tl of TPC share the lines
 template <int D, int N, typename T>
@@ -241,7 +248,7 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS)
   constexpr int NC = S::NC, TPC = S::TPC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int cpb = P.cpb;
-  const long long bufe = ecl_buffer_elems<D, N, T>(cpb);
+  const long long bufe = gauss_buffer_elems<D, N, T>(cpb);
   T* const s_in0 = reinterpret_cast<T*>(smem_raw);
   T* const s_in1 = s_in0 + bufe;
   T* const s_v = s_in0 + 2 * bufe;
@@ -284,14 +291,14 @@ cudaError_t launch_gauss(const EclParams<T>& P0, const GaussExtra<T>& G, int mod
     EclParams<T> P = P0;
     if (P.cpb < 1 || P.cpb > S::CPB) P.cpb = ecl_default_cpb<D, N, T>();
     const int threads = S::TPC * P.cpb;
-    const size_t smem = size_t(5 * ecl_buffer_elems<D, N, T>(P.cpb)) * sizeof(T);
+    const size_t smem = size_t(5 * gauss_buffer_elems<D, N, T>(P.cpb)) * sizeof(T);
     if (mode < kApply || mode > kStageLast) return cudaErrorInvalidValue;
     static bool attr_done = false;
     static int sms = 0;
     auto kern = gauss_kernel<D, N, T>;
     if (!attr_done) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           int(5 * ecl_buffer_elems<D, N, T>(S::CPB) * sizeof(T)));
+                                           int(5 * gauss_buffer_elems<D, N, T>(S::CPB) * sizeof(T)));
       if (e != cudaSuccess) return e;
       int dev = 0;
       cudaGetDevice(&dev);

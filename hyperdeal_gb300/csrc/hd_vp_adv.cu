@@ -51,8 +51,9 @@ __device__ __forceinline__ void vp_block(const VpAdvParams<T>& P, const VpLine<T
       nbR[d] = cc[d] + 1 < g.cells[d] ? gg + cs : gg - (long long)(g.cells[d] - 1) * cs;
     }
   }
-  const T* su = su_all + lc * NC;
-  T* so = so_all + lc * NC;
+  constexpr int CST = EclTile<D, N, T>::CST;
+  const T* su = su_all + lc * CST;
+  T* so = so_all + lc * CST;
 
   // velocity / h of the line along d through node `bnode` (any node of the line)
   auto line_scale = [&](int d, int bnode) -> T {
@@ -69,7 +70,7 @@ __device__ __forceinline__ void vp_block(const VpAdvParams<T>& P, const VpLine<T
     if constexpr (MODE == kApply) {
       P.dst[gi] = k;
     } else {
-      const T u = (MODE == kStageFirst) ? uval : (uu_all ? uu_all[lc * NC + node] : P.uin[gi]);
+      const T u = (MODE == kStageFirst) ? uval : (uu_all ? uu_all[lc * CST + node] : P.uin[gi]);
       P.dst[gi] = fma(P.fb, k, u);
       if constexpr (MODE != kStageLast) P.tout[gi] = fma(P.fa, k, u);
     }
@@ -108,14 +109,33 @@ __device__ __forceinline__ void vp_block(const VpAdvParams<T>& P, const VpLine<T
           upB[a] = scB[a] > T(0) ? l : r;
         }
         T uu[N][N], acc[N][N];
+        constexpr bool kVec = (N * N * sizeof(T)) % 16 == 0;  // phase 0: N*N contiguous values per plane
+        if (kVec && ph == 0) {
+          using V = Vec16<T>;
+          T flat[N * N];
 #pragma unroll
-        for (int a = 0; a < N; ++a)
+          for (int k = 0; k < N * N / V::n; ++k) {
+            const typename V::type w = *reinterpret_cast<const typename V::type*>(su + base + k * V::n);
 #pragma unroll
-          for (int b = 0; b < N; ++b) {
-            const int node = base + a * strideA + b * strideB;
-            uu[a][b] = su[node];
-            acc[a][b] = ph == 0 ? T(0) : so[node];
+            for (int j = 0; j < V::n; ++j) flat[k * V::n + j] = V::get(w, j);
           }
+#pragma unroll
+          for (int a = 0; a < N; ++a)
+#pragma unroll
+            for (int b = 0; b < N; ++b) {
+              uu[a][b] = flat[a + N * b];
+              acc[a][b] = T(0);
+            }
+        } else {
+#pragma unroll
+          for (int a = 0; a < N; ++a)
+#pragma unroll
+            for (int b = 0; b < N; ++b) {
+              const int node = base + a * strideA + b * strideB;
+              uu[a][b] = su[node];
+              acc[a][b] = ph == 0 ? T(0) : so[node];
+            }
+        }
         if (valid) {
 #pragma unroll
           for (int b = 0; b < N; ++b) {
@@ -155,10 +175,22 @@ __device__ __forceinline__ void vp_block(const VpAdvParams<T>& P, const VpLine<T
           }
         }
         if (!last) {
+          if (kVec && ph == 0) {
+            using V = Vec16<T>;
+            T flat[N * N];
 #pragma unroll
-          for (int a = 0; a < N; ++a)
+            for (int a = 0; a < N; ++a)
 #pragma unroll
-            for (int b = 0; b < N; ++b) so[base + a * strideA + b * strideB] = acc[a][b];
+              for (int b = 0; b < N; ++b) flat[a + N * b] = acc[a][b];
+#pragma unroll
+            for (int k = 0; k < N * N / V::n; ++k)
+              *reinterpret_cast<typename V::type*>(so + base + k * V::n) = V::make(flat + k * V::n);
+          } else {
+#pragma unroll
+            for (int a = 0; a < N; ++a)
+#pragma unroll
+              for (int b = 0; b < N; ++b) so[base + a * strideA + b * strideB] = acc[a][b];
+          }
         } else if (valid) {
 #pragma unroll
           for (int a = 0; a < N; ++a)
@@ -223,8 +255,8 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS, EclShape<D, N, T>:
   auto stage = [&](T* dst, T* dstu, long long blk) {
     const long long c0 = blk * cpb;
     const long long ncell = (n_cells - c0) < cpb ? (n_cells - c0) : cpb;
-    stage_async(dst, P.src + c0 * NC, ncell * NC, tid, nthr);
-    if constexpr (SU) stage_async(dstu, P.uin + c0 * NC, ncell * NC, tid, nthr);
+    stage_cells<D, N, T>(dst, P.src + c0 * NC, ncell, tid, nthr);
+    if constexpr (SU) stage_cells<D, N, T>(dstu, P.uin + c0 * NC, ncell, tid, nthr);
   };
   long long b = blockIdx.x;
   if (b < nblk) stage(s_in0, s_u0, b);
