@@ -27,9 +27,10 @@ EXPORTED_SYMBOLS = (
     "hd_vp_learn_loss_grad", "hd_adv_set_tile", "hd_adv_tile_limits",
     "hd_batch_create", "hd_batch_destroy", "hd_batch_n_classes", "hd_batch_class_info", "hd_batch_set_tile",
     "hd_batch_apply", "hd_batch_lsrk_step", "hd_batch_graph_capture", "hd_batch_graph_launch", "hd_batch_autotune",
-    "hd_adv_autotune", "hd_vp_lsrk_step_fused",
+    "hd_adv_autotune", "hd_vp_lsrk_step_fused", "hd_adv_set_arithmetic", "hd_adv_arithmetic",
 )
 HD_KERNEL_AUTO, HD_KERNEL_GENERIC, HD_KERNEL_PIPELINED = 0, 1, 2
+HD_ARITH_NATIVE, HD_ARITH_FP32X2 = 0, 1
 HD_VP_GUESS_ZERO, HD_VP_GUESS_PREVIOUS, HD_VP_GUESS_LEARNED = 0, 1, 2
 
 
@@ -95,6 +96,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.hd_adv_apply.argtypes = [vp, vp, vp, ctypes.c_double, vp]
     L.hd_adv_set_kernel.argtypes = [vp, ctypes.c_int]
     L.hd_adv_kernel.argtypes = [vp]
+    L.hd_adv_set_arithmetic.argtypes = [vp, ctypes.c_int]
+    L.hd_adv_arithmetic.argtypes = [vp]
     L.hd_adv_device_status.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     L.hd_adv_set_tile.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     L.hd_adv_autotune.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),

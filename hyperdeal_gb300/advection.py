@@ -171,6 +171,17 @@ class AdvectionOperation:
         return {_lib.HD_KERNEL_GENERIC: "generic", _lib.HD_KERNEL_PIPELINED: "pipelined"}[
             int(self._L.hd_adv_kernel(self._h))]
 
+    def set_arithmetic(self, arithmetic: str) -> None:
+        """'native' (FP64 contractions) or 'fp32x2' (double-word FP32 contractions
+        on FP64 storage; see hd_adv_set_arithmetic)."""
+        v = {"native": _lib.HD_ARITH_NATIVE, "fp32x2": _lib.HD_ARITH_FP32X2}[arithmetic]
+        check(self._L.hd_adv_set_arithmetic(self._h, v))
+
+    @property
+    def arithmetic(self) -> str:
+        return {_lib.HD_ARITH_NATIVE: "native", _lib.HD_ARITH_FP32X2: "fp32x2"}[
+            int(self._L.hd_adv_arithmetic(self._h))]
+
     def set_tile(self, cells_per_cta: int = 0, ctas_per_sm: int = 0) -> None:
         """Tile of the generic kernel (hd_adv_set_tile); 0 = default."""
         check(self._L.hd_adv_set_tile(self._h, int(cells_per_cta), int(ctas_per_sm)))

@@ -339,6 +339,17 @@ void fill_params(const hd_adv* op, hd::EclParams<T>* P) {
     P->op[d].nb_node = L.nb_node;
     P->op[d].step = L.step;
     P->op[d].active = L.active;
+    if constexpr (sizeof(T) == 8) {
+      hd::LineOp<hd::f32x2>& X = P->opx[d];
+      for (int i = 0; i < op->N * op->N; ++i) X.M[i] = hd::x2_split_host(L.M[i]);
+      X.cin = hd::x2_split_host(L.cin);
+      X.c0 = L.in_node == 0 ? X.cin : hd::f32x2{0.f, 0.f};
+      X.cl = L.in_node == op->N - 1 ? X.cin : hd::f32x2{0.f, 0.f};
+      X.in_node = L.in_node;
+      X.nb_node = L.nb_node;
+      X.step = L.step;
+      X.active = L.active;
+    }
   }
   if (op->D < hd::kMaxDim) P->cstride[op->D] = st;
   for (int i = 0; i < op->N; ++i) P->gl[i] = op->gl[i];
@@ -388,7 +399,7 @@ int launch(hd_adv* op, int mode, const void* tin, const void* uin, void* uout, v
     hd::EclParams<double> P = op->p64;
     P.tin = (const double*)tin; P.uin = (const double*)uin; P.uout = (double*)uout; P.tout = (double*)tout;
     P.fb = fb; P.fa = fa; P.time = time;
-    e = op->launchers.f64(P, mode, s);
+    e = (op->arith == HD_ARITH_FP32X2 ? op->launchers.f64x : op->launchers.f64)(P, mode, s);
   } else {
     hd::EclParams<float> P = op->p32;
     P.tin = (const float*)tin; P.uin = (const float*)uin; P.uout = (float*)uout; P.tout = (float*)tout;
@@ -547,6 +558,7 @@ int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
     e = cudaMemset(op->d_err, 0, sizeof(int));
     if (e != cudaSuccess) { cudaFree(op->d_partials); delete op; return cuda_fail(e, "cudaMemset (error flag)"); }
     op->variant = HD_KERNEL_AUTO;
+    op->arith = HD_ARITH_NATIVE;
     {
       size_t tsize = 0;
       for (int i = 0; i < op->D; ++i) tsize += size_t(op->cells[i]) * op->N;
@@ -641,6 +653,18 @@ int hd_adv_set_kernel(hd_adv* op, int variant) {
 }
 
 int hd_adv_kernel(const hd_adv* op) { return op ? selected_kernel(op) : -1; }
+
+int hd_adv_set_arithmetic(hd_adv* op, int arithmetic) {
+  if (!op) return fail(HD_ERR_INVALID, "hd_adv_set_arithmetic: null handle");
+  if (arithmetic != HD_ARITH_NATIVE && arithmetic != HD_ARITH_FP32X2)
+    return fail(HD_ERR_INVALID, "unknown arithmetic %d", arithmetic);
+  if (arithmetic == HD_ARITH_FP32X2 && (op->dtype != HD_F64 || op->gauss || !op->launchers.f64x))
+    return fail(HD_ERR_UNSUPPORTED, "FP32x2 arithmetic needs FP64 storage and Gauss-Lobatto collocation");
+  op->arith = arithmetic;
+  return HD_OK;
+}
+
+int hd_adv_arithmetic(const hd_adv* op) { return op ? op->arith : -1; }
 
 int hd_adv_device_status(hd_adv* op, int* status) {
   if (!op || !status) return fail(HD_ERR_INVALID, "hd_adv_device_status: null argument");

@@ -20,6 +20,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
+#include "hd_df.cuh"
+
 namespace hd {
 
 constexpr int kMaxDim = 6;
@@ -61,6 +65,9 @@ struct EclParams {
   long long cstride[kMaxDim];
   int periodic[kMaxDim];
   LineOp<T> op[kMaxDim];
+  // FP64 storage only: the same operators as FP32x2 words (hd_df.cuh) for the
+  // FP32x2-arithmetic kernels
+  std::conditional_t<sizeof(T) == 8, LineOp<f32x2>, char> opx[kMaxDim];
   int bc_inhom;
   DevFunction bc;
   double time;
@@ -273,6 +280,9 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
     const bool actB = dB >= 0 && valid && P.op[dB].active;
     const long long nbA = actA ? neighbour(P, gid, cc, dA) : -1;
     const long long nbB = actB ? neighbour(P, gid, cc, dB) : -1;
+    // face-load cells: the neighbour, or cell 0 where there is none, so that
+    // every load address is valid even if the compiler issues it unconditionally
+    const long long fA = nbA >= 0 ? nbA : 0, fB = nbB >= 0 ? nbB : 0;
 
     for (int item = tl; item < nitems; item += TPC) {
       const int base = item_base<D, N>(item, dA, dB);
@@ -283,10 +293,10 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
         T upA[N], upB[N];
 #pragma unroll
         for (int b = 0; b < N; ++b)
-          upA[b] = nbA >= 0 ? __ldg(P.tin + nbA * NC + base + LA.nb_node * strideA + b * strideB) : T(0);
+          upA[b] = nbA >= 0 ? __ldg(P.tin + fA * NC + base + LA.nb_node * strideA + b * strideB) : T(0);
 #pragma unroll
         for (int a = 0; a < N; ++a)
-          upB[a] = nbB >= 0 ? __ldg(P.tin + nbB * NC + base + a * strideA + LB.nb_node * strideB) : T(0);
+          upB[a] = nbB >= 0 ? __ldg(P.tin + fB * NC + base + a * strideA + LB.nb_node * strideB) : T(0);
         T uu[N][N], acc[N][N];  // [a][b]: node base + a*strideA + b*strideB
         // phase 0: the plane of directions 0, 1 is N*N contiguous values; when
         // that is a whole number of 16-byte words it is read as such (far
@@ -396,7 +406,7 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
       } else {
         // single-direction phase (odd D): lines along dA
         const LineOp<T>& LA = P.op[dA];
-        const T upf = nbA >= 0 ? __ldg(P.tin + nbA * NC + base + LA.nb_node * strideA) : T(0);
+        const T upf = nbA >= 0 ? __ldg(P.tin + fA * NC + base + LA.nb_node * strideA) : T(0);
         T uu[N], acc[N];
 #pragma unroll
         for (int a = 0; a < N; ++a) {
@@ -444,6 +454,146 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
   }
 }
 
+// The block in FP32x2 arithmetic on FP64 storage (hd_df.cuh), organised line
+// by line instead of plane by plane: a line's N values and N accumulators are
+// read from shared memory, its N x N double-word multiply-adds and inflow
+// term applied, and the accumulators written back -- or, after the last
+// direction of the last phase, the result written to global memory.  The line
+// loop is not unrolled: a double-word multiply-add is about twelve FP32
+// instructions, and fully unrolled planes overflow the instruction cache; the
+// phase and direction loops are not unrolled either (one copy of the line code).
+// A cell's threads visit their lines in a rotated order (planes of the first
+// phase lie N*N values apart, a multiple of the bank count), and lines along
+// direction 0 (contiguous, 16-byte aligned for even N) are read as 16-byte words.
+template <int D, int N, int MODE>
+__device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long long cell0, int lc, int tl,
+                                             const double* su_all, double* so_all, const double* uu_all) {
+  using S = EclShape<D, N, double>;
+  constexpr int NC = S::NC, TPC = S::TPC;
+  constexpr int CST = EclTile<D, N, double>::CST;
+  const long long gid = cell0 + lc;
+  const bool valid = gid < P.n_cells;
+  int cc[D];
+  {
+    long long g = valid ? gid : 0;
+    long long gx = g % (P.cstride[P.dim_x]), gv = g / (P.cstride[P.dim_x]);
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      if (d < P.dim_x) { cc[d] = int(gx % P.cells[d]); gx /= P.cells[d]; }
+      else { cc[d] = int(gv % P.cells[d]); gv /= P.cells[d]; }
+    }
+  }
+  const double* su = su_all + lc * CST;
+  f32x2* so = reinterpret_cast<f32x2*>(so_all + lc * CST);
+  const double* uu = uu_all ? uu_all + lc * CST : nullptr;
+  const long long g0 = gid * NC;
+
+#pragma unroll 1
+  for (int ph = 0; ph < S::NPH; ++ph) {
+    const int dA = 2 * ph;
+    const int dB = (2 * ph + 1 < D) ? 2 * ph + 1 : -1;
+    int strideA = 1;
+    for (int e = 0; e < dA; ++e) strideA *= N;
+    const int strideB = strideA * N;
+    const int nitems = dB >= 0 ? ipow(N, D - 2) : ipow(N, D - 1);
+    const int ndir = dB >= 0 ? 2 : 1;
+    const int nl = dB >= 0 ? N : 1;      // lines per direction in a work item
+    const int rot = nl > 1 ? tl % N : 0;
+    const bool lastph = ph == S::NPH - 1;
+    for (int item = tl; item < nitems; item += TPC) {
+      const int base = item_base<D, N>(item, dA, dB);
+#pragma unroll 1
+      for (int dd = 0; dd < ndir; ++dd) {
+        const int d = dd == 0 ? dA : dB;
+        const int st = dd == 0 ? strideA : strideB;   // along the line
+        const int lst = dd == 0 ? strideB : strideA;  // between the lines
+        const LineOp<f32x2>& L = P.opx[d];
+        const bool act = valid && L.active;
+        const long long nb = act ? neighbour(P, gid, cc, d) : -1;
+        const bool first = ph == 0 && dd == 0;
+        const bool fin = lastph && dd == ndir - 1;
+        // upwind trace (cell 0 where there is no neighbour: every load address
+        // stays valid even if the compiler issues the guarded loads unconditionally)
+        const double* face = P.tin + (nb >= 0 ? nb : 0) * NC + L.nb_node * st;
+        int l = rot;
+        double upn = nb >= 0 ? __ldg(face + base + l * lst) : 0.0;
+#pragma unroll 1
+        for (int j = 0; j < nl; ++j) {
+          const int lb = base + l * lst;
+          const double upd = upn;
+          l = l + 1 < nl ? l + 1 : 0;
+          if (nb >= 0 && j + 1 < nl) upn = __ldg(face + base + l * lst);  // next line's trace
+          f32x2 u[N], acc[N];
+          if ((N % 2) == 0 && st == 1) {
+#pragma unroll
+            for (int q = 0; q < N; q += 2) {
+              const double2 w = *reinterpret_cast<const double2*>(su + lb + q);
+              u[q] = x2_from_double(w.x);
+              u[q + 1] = x2_from_double(w.y);
+            }
+          } else {
+#pragma unroll
+            for (int q = 0; q < N; ++q) u[q] = x2_from_double(su[lb + q * st]);
+          }
+          if (first) {
+#pragma unroll
+            for (int i = 0; i < N; ++i) acc[i] = f32x2{0.f, 0.f};
+          } else if ((N % 2) == 0 && st == 1) {
+#pragma unroll
+            for (int i = 0; i < N; i += 2) {
+              const float4 w = *reinterpret_cast<const float4*>(so + lb + i);
+              acc[i] = f32x2{w.x, w.y};
+              acc[i + 1] = f32x2{w.z, w.w};
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < N; ++i) acc[i] = so[lb + i * st];
+          }
+          if (act) {
+#pragma unroll
+            for (int i = 0; i < N; ++i)
+#pragma unroll
+              for (int q = 0; q < N; ++q) x2_mac(acc[i], L.M[i * N + q], u[q]);
+            const int in = L.in_node;
+            const double upv =
+                nb >= 0 ? upd : boundary_value<D, N, double>(P, cc, d, lb + in * st, su[lb + in * st]);
+            const f32x2 up = x2_from_double(upv);
+            if (in == 0) x2_mac(acc[0], L.cin, up);
+            else x2_mac(acc[N - 1], L.cin, up);
+          }
+          if (!fin) {
+            if ((N % 2) == 0 && st == 1) {
+#pragma unroll
+              for (int i = 0; i < N; i += 2) {
+                const f32x2 a0 = x2_norm(acc[i]), a1 = x2_norm(acc[i + 1]);
+                *reinterpret_cast<float4*>(so + lb + i) = make_float4(a0.hi, a0.lo, a1.hi, a1.lo);
+              }
+            } else {
+#pragma unroll
+              for (int i = 0; i < N; ++i) so[lb + i * st] = x2_norm(acc[i]);
+            }
+          } else if (valid) {
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+              const int node = lb + i * st;
+              const long long gi = g0 + node;
+              const double k = x2_to_double(acc[i]);
+              if constexpr (MODE == kApply) {
+                P.uout[gi] = k;
+              } else {
+                const double uv = MODE == kStageFirst ? su[node] : (uu ? uu[node] : P.uin[gi]);
+                P.uout[gi] = fma(P.fb, k, uv);
+                if constexpr (MODE != kStageLast) P.tout[gi] = fma(P.fa, k, uv);
+              }
+            }
+          }
+        }
+      }
+    }
+    if (!lastph) __syncthreads();
+  }
+}
+
 // stage modes mid/last also stage the RK solution of the block (two more
 // buffers) when five buffers of one cell fit in shared memory (not for the
 // FP64 6D shapes: their 32 KiB+ cell tiles would leave one CTA per SM)
@@ -457,7 +607,7 @@ struct EclStaging {
 // Persistent generic kernel: CTAs walk blocks of P.cpb cells with a stride of
 // the grid; the next block's input is staged by cp.async while the current
 // one is computed (two staging buffers + one accumulator tile).
-template <int D, int N, typename T, int MODE>
+template <int D, int N, typename T, int MODE, typename A = T>
 __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS, EclShape<D, N, T>::MINB)
     ecl_kernel(const __grid_constant__ EclParams<T> P) {
   using S = EclShape<D, N, T>;
@@ -494,7 +644,8 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS, EclShape<D, N, T>:
     cp_async_commit();
     cp_async_wait<1>();  // this thread's copies of block b are complete
     __syncthreads();     // ... and everybody's
-    ecl_block<D, N, T, MODE>(P, b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+    if constexpr (std::is_same_v<A, f32x2>) ecl_block_x2<D, N, MODE>(P, b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+    else ecl_block<D, N, T, MODE>(P, b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
     __syncthreads();     // cur and s_o are free for the next blocks
     odd = !odd;
   }
@@ -510,9 +661,9 @@ __host__ __device__ constexpr int ecl_default_cpb() {
   return cpb < 1 ? 1 : (cpb > EclShape<D, N, T>::CPB ? EclShape<D, N, T>::CPB : cpb);
 }
 
-// host launcher for one (D, N, T): P.cpb cells per CTA (1..CPB; 0 = default) and
-// ctas_per_sm CTAs per SM (0 = as many as fit), persistent grid
-template <int D, int N, typename T>
+// host launcher for one (D, N, T, arithmetic A): P.cpb cells per CTA (1..CPB;
+// 0 = default) and ctas_per_sm CTAs per SM (0 = as many as fit), persistent grid
+template <int D, int N, typename T, typename A = T>
 cudaError_t launch_ecl(const EclParams<T>& P0, int mode, cudaStream_t stream) {
   using S = EclShape<D, N, T>;
   if constexpr (!S::SUPPORTED) {
@@ -555,10 +706,10 @@ cudaError_t launch_ecl(const EclParams<T>& P0, int mode, cudaStream_t stream) {
       return cudaGetLastError();
     };
     switch (mode) {
-      case kApply: return go(ecl_kernel<D, N, T, kApply>);
-      case kStageFirst: return go(ecl_kernel<D, N, T, kStageFirst>);
-      case kStageMid: return go(ecl_kernel<D, N, T, kStageMid>);
-      case kStageLast: return go(ecl_kernel<D, N, T, kStageLast>);
+      case kApply: return go(ecl_kernel<D, N, T, kApply, A>);
+      case kStageFirst: return go(ecl_kernel<D, N, T, kStageFirst, A>);
+      case kStageMid: return go(ecl_kernel<D, N, T, kStageMid, A>);
+      case kStageLast: return go(ecl_kernel<D, N, T, kStageLast, A>);
       default: return cudaErrorInvalidValue;
     }
   }
@@ -571,6 +722,7 @@ struct EclLaunchers {
   size_t smem_f64, smem_f32;
   int threads_f64, threads_f32, cells_per_cta_f64, cells_per_cta_f32;
   bool ok_f64, ok_f32;
+  cudaError_t (*f64x)(const EclParams<double>&, int, cudaStream_t);  // FP64 storage, FP32x2 arithmetic
 };
 
 template <int D, int N>
@@ -578,7 +730,8 @@ EclLaunchers make_launchers() {
   using S64 = EclShape<D, N, double>;
   using S32 = EclShape<D, N, float>;
   return EclLaunchers{&launch_ecl<D, N, double>, &launch_ecl<D, N, float>, S64::SMEM, S32::SMEM,
-                      S64::THREADS, S32::THREADS, S64::CPB, S32::CPB, S64::SUPPORTED, S32::SUPPORTED};
+                      S64::THREADS, S32::THREADS, S64::CPB, S32::CPB, S64::SUPPORTED, S32::SUPPORTED,
+                      &launch_ecl<D, N, double, f32x2>};
 }
 
 // message of the last failure for hd_last_error() (hd_capi.cu)

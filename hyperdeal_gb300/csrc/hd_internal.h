@@ -42,6 +42,7 @@ struct hd_adv {
   double* d_table;     // factor table of product functions (sum_d cells_d * (k+1) doubles)
   int device;
   int variant;         // HD_KERNEL_AUTO / _GENERIC / _PIPELINED
+  int arith;           // HD_ARITH_NATIVE / _FP32X2 (FP64 storage)
   int gauss;           // 1: Gauss quadrature (non-collocation) path
   GaussTables gt;
   hd::GaussExtra<double> g64;

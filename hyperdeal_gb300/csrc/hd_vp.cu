@@ -53,7 +53,8 @@ __global__ void moment_partials(VpGeom g, const T* __restrict__ f, const double*
 #pragma unroll
     for (int k = 0; k < kMomChunk; ++k) {
       const long long gv = gv0 + k;
-      vals[k] = gv < g.ncv ? __ldg(f + (gxc + g.ncx * gv) * g.NC + node) : T(0);
+      const long long gvc = gv < g.ncv ? gv : g.ncv - 1;  // valid address even if loaded unconditionally
+      vals[k] = gv < g.ncv ? __ldg(f + (gxc + g.ncx * gvc) * g.NC + node) : T(0);
     }
     // FP32 storage: the chunk is summed pairwise in FP32 (the FP64 pipe is the
     // scarce resource here; the values carry FP32 precision anyway);

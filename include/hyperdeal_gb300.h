@@ -137,6 +137,17 @@ enum hd_kernel { HD_KERNEL_AUTO = 0, HD_KERNEL_GENERIC = 1, HD_KERNEL_PIPELINED 
 int hd_adv_set_kernel(hd_adv *op, int variant);
 int hd_adv_kernel(const hd_adv *op);
 
+/* Arithmetic of the FP64-storage form (no reference counterpart: the
+ * reference computes in double).  NATIVE runs the contractions in FP64;
+ * FP32X2 keeps FP64 storage, layout and stage update but runs the line
+ * contractions in double-word FP32 arithmetic (hi + lo float pairs, about 48
+ * significant bits) on the FP32 pipe, which GB300 issues at 64 times its FP64
+ * rate.  FP32X2 needs dtype HD_F64 and Gauss-Lobatto collocation (generic
+ * kernel); the default is NATIVE. */
+enum hd_arithmetic { HD_ARITH_NATIVE = 0, HD_ARITH_FP32X2 = 1 };
+int hd_adv_set_arithmetic(hd_adv *op, int arithmetic);
+int hd_adv_arithmetic(const hd_adv *op);
+
 /* Device-side error code of the pipelined kernel since the last call (0 = none;
  * 1/2 = a bounded wait on a copy / buffer slot timed out and the kernel
  * returned early).  Synchronises the device; clears the flag. */

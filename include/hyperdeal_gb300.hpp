@@ -152,6 +152,8 @@ class AdvectionOperation {
     double ms = 0.0;
     check(hd_adv_autotune(h_, src.data(), dst.data(), reps, &c, &p, &ms, stream_));
   }
+  // FP64 storage: contractions in FP64 (HD_ARITH_NATIVE) or double-word FP32 (HD_ARITH_FP32X2)
+  void set_arithmetic(int arithmetic) { check(hd_adv_set_arithmetic(h_, arithmetic)); }
   hd_adv* handle() const { return h_; }
   cudaStream_t stream() const { return stream_; }
   DeviceVector<Number> create_vector() const { return DeviceVector<Number>(n_dofs()); }
