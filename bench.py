@@ -502,10 +502,12 @@ def run_adv4d(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     res, sols = {}, {}
     clocks = None
-    for dtype in ("f32", "f64"):
+    for dtype in ("f32", "f64", "f64_fp32x2"):
         p = A.AdvectionParameters(2, 2, 3, [16, 16], [16, 16], [0.0] * 2, [1.0] * 2, [0.0] * 2, [1.0] * 2, vel,
-                                  dtype=dtype)
+                                  dtype=dtype[:3])
         op = A.AdvectionOperation(p)
+        if dtype == "f64_fp32x2":
+            op.set_arithmetic("fp32x2")
         sol = op.initialize_dof_vector()
         A.VectorTools.interpolate(op, f0, sol, 0.0)
         Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
@@ -537,6 +539,8 @@ def run_adv4d(args):
         sols[dtype] = sol.double()
         n = op.n_dofs
     l2 = float(torch.linalg.vector_norm(sols["f32"] - sols["f64"]) / torch.linalg.vector_norm(sols["f64"]))
+    res["f64_fp32x2"]["l2_rel_err_vs_f64"] = float(torch.linalg.vector_norm(sols["f64_fp32x2"] - sols["f64"])
+                                                   / torch.linalg.vector_norm(sols["f64"]))
     cpu = None
     if not args.no_cpu:
         from oracle import oracle as O
@@ -556,7 +560,7 @@ def run_adv4d(args):
                                   "(65,536 cells, 16,777,216 DoFs), periodic unit box, velocity (1.0, 0.7, 0.5, 0.3), "
                                   "f0 = prod sin(2 pi coord), fused rk45, CFL 0.2",
                       "l2_flush": "none: 67 MB per FP32 vector (3 vectors 201 MB > 129 MB L2)"},
-           "f32": res["f32"], "f64": res["f64"], "l2_rel_err_f32_vs_f64": l2,
+           "f32": res["f32"], "f64": res["f64"], "f64_fp32x2": res["f64_fp32x2"], "l2_rel_err_f32_vs_f64": l2,
            "roofline": {"bound": "hbm", "achieved": res["f32"]["hbm_gb_per_s"], "peak": peak, "unit": "GB/s",
                         "frac": round(res["f32"]["hbm_gb_per_s"] / peak, 4), "peak_source": peak_kind},
            "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": N_STAGES * args.steps}
@@ -703,22 +707,45 @@ def main():
         torch.cuda.synchronize()
         ms64 = e0.elapsed_time(e1) / args.steps_f64
         v64 = n * N_STAGES / (ms64 / 1e3) / 1e9
-        f64 = {"value": round(v64, 3), "ms_per_step": round(ms64, 3), "steps": args.steps_f64}
-        # same number of steps from the same initial data in both forms
+        f64 = {"value": round(v64, 3), "ms_per_step": round(ms64, 3), "steps": args.steps_f64,
+               "arithmetic": "native FP64"}
+        # the FP64-storage form with double-word FP32 contractions (hd_adv_set_arithmetic FP32X2)
+        op64.set_arithmetic("fp32x2")
+        for _ in range(args.warmup):
+            i64.perform_time_step(s64, t64, dt, op64)
+            t64 += dt
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps_f64):
+            i64.perform_time_step(s64, t64, dt, op64)
+            t64 += dt
+        e1.record(stream)
+        torch.cuda.synchronize()
+        msx = e0.elapsed_time(e1) / args.steps_f64
+        f64x = {"value": round(n * N_STAGES / (msx / 1e3) / 1e9, 3), "ms_per_step": round(msx, 3),
+                "steps": args.steps_f64, "arithmetic": "FP32x2 (double-word FP32) contractions, FP64 storage"}
+        # same number of steps from the same initial data in the three forms
         s32 = op.initialize_dof_vector()
         A.VectorTools.interpolate(op, f0, s32, 0.0)
         s64b = op64.initialize_dof_vector()
         A.VectorTools.interpolate(op64, f0, s64b, 0.0)
+        s64x = s64b.clone()
         nsteps = args.warmup + args.steps_f64
         tt = 0.0
         for _ in range(nsteps):
             integ.perform_time_step(s32, tt, dt, op)
+            op64.set_arithmetic("native")
             i64.perform_time_step(s64b, tt, dt, op64)
+            op64.set_arithmetic("fp32x2")
+            i64.perform_time_step(s64x, tt, dt, op64)
             tt += dt
         d = (s32.double() - s64b)
         l2 = float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(s64b))
         f64["l2_compared_after_steps"] = nsteps
-        del op64, s64, K64, T64, i64, s64b, d, s32
+        f64x["l2_rel_err_vs_f64"] = float(torch.linalg.vector_norm(s64x - s64b) / torch.linalg.vector_norm(s64b))
+        f64x["max_rel_err_vs_f64"] = float((s64x - s64b).abs().max() / s64b.abs().max())
+        f64["fp32x2"] = f64x
+        del op64, s64, K64, T64, i64, s64b, s64x, d, s32
         torch.cuda.empty_cache()
 
     # end to end through the public API with host buffers: every step copies a state from pinned

@@ -483,7 +483,8 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
       else { cc[d] = int(gv % P.cells[d]); gv /= P.cells[d]; }
     }
   }
-  const double* su = su_all + lc * CST;
+  // the staged input was converted to FP32x2 words in place (ecl_kernel)
+  const f32x2* sx = reinterpret_cast<const f32x2*>(su_all + lc * CST);
   f32x2* so = reinterpret_cast<f32x2*>(so_all + lc * CST);
   const double* uu = uu_all ? uu_all + lc * CST : nullptr;
   const long long g0 = gid * NC;
@@ -527,13 +528,13 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
           if ((N % 2) == 0 && st == 1) {
 #pragma unroll
             for (int q = 0; q < N; q += 2) {
-              const double2 w = *reinterpret_cast<const double2*>(su + lb + q);
-              u[q] = x2_from_double(w.x);
-              u[q + 1] = x2_from_double(w.y);
+              const float4 w = *reinterpret_cast<const float4*>(sx + lb + q);
+              u[q] = f32x2{w.x, w.y};
+              u[q + 1] = f32x2{w.z, w.w};
             }
           } else {
 #pragma unroll
-            for (int q = 0; q < N; ++q) u[q] = x2_from_double(su[lb + q * st]);
+            for (int q = 0; q < N; ++q) u[q] = sx[lb + q * st];
           }
           if (first) {
 #pragma unroll
@@ -556,7 +557,7 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
               for (int q = 0; q < N; ++q) x2_mac(acc[i], L.M[i * N + q], u[q]);
             const int in = L.in_node;
             const double upv =
-                nb >= 0 ? upd : boundary_value<D, N, double>(P, cc, d, lb + in * st, su[lb + in * st]);
+                nb >= 0 ? upd : boundary_value<D, N, double>(P, cc, d, lb + in * st, x2_to_double(sx[lb + in * st]));
             const f32x2 up = x2_from_double(upv);
             if (in == 0) x2_mac(acc[0], L.cin, up);
             else x2_mac(acc[N - 1], L.cin, up);
@@ -581,7 +582,8 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
               if constexpr (MODE == kApply) {
                 P.uout[gi] = k;
               } else {
-                const double uv = MODE == kStageFirst ? su[node] : (uu ? uu[node] : P.uin[gi]);
+                // exact U: the RK solution in FP64 (the first stage's is its input, read again from L2)
+                const double uv = uu ? uu[node] : P.uin[gi];
                 P.uout[gi] = fma(P.fb, k, uv);
                 if constexpr (MODE != kStageLast) P.tout[gi] = fma(P.fa, k, uv);
               }
@@ -606,9 +608,12 @@ struct EclStaging {
 
 // Persistent generic kernel: CTAs walk blocks of P.cpb cells with a stride of
 // the grid; the next block's input is staged by cp.async while the current
-// one is computed (two staging buffers + one accumulator tile).
+// one is computed (two staging buffers + one accumulator tile).  The FP32x2
+// kernels are capped at 128 registers (two CTAs of the largest shape per SM):
+// their issue-bound line loops need the warps.
 template <int D, int N, typename T, int MODE, typename A = T>
-__global__ void __launch_bounds__(EclShape<D, N, T>::THREADS, EclShape<D, N, T>::MINB)
+__global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
+                                  std::is_same_v<A, f32x2> ? 2 : EclShape<D, N, T>::MINB)
     ecl_kernel(const __grid_constant__ EclParams<T> P) {
   using S = EclShape<D, N, T>;
   constexpr int NC = S::NC, TPC = S::TPC;
@@ -644,6 +649,16 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS, EclShape<D, N, T>:
     cp_async_commit();
     cp_async_wait<1>();  // this thread's copies of block b are complete
     __syncthreads();     // ... and everybody's
+    if constexpr (std::is_same_v<A, f32x2>) {
+      // FP32x2: convert the staged input to double-word FP32 in place, once
+      // per value (the line loops read each value up to D times)
+      const int nv = cpb * EclTile<D, N, T>::CST;
+      for (int i = tid; i < nv; i += nthr) {
+        const double v = cur[i];
+        reinterpret_cast<f32x2*>(cur)[i] = x2_from_double(v);
+      }
+      __syncthreads();
+    }
     if constexpr (std::is_same_v<A, f32x2>) ecl_block_x2<D, N, MODE>(P, b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
     else ecl_block<D, N, T, MODE>(P, b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
     __syncthreads();     // cur and s_o are free for the next blocks
