@@ -389,6 +389,17 @@ def run_batch(args):
     clocks = sampler.stop()
     ms_graph = ms_graph2 / 2
     launches_per_step = N_STAGES * sum(1 if c["batched"] else c["members"] for c in classes)
+    # the same workload with the FP64 instances in FP32x2 arithmetic (FP64 storage)
+    for op in ops:
+        if op.dtype == torch.float64:
+            op.set_arithmetic("fp32x2")
+    batch_x = Bt.AdvectionBatch(ops)
+    batch_x.autotune(sols, Ks, reps=2)
+    batch_x.capture_graph(sols, Ks, Ts, times, dts)
+    ms_graph_x = timed(batch_x.replay_graph, max(1, args.steps // 2)) / 2
+    for op in ops:
+        if op.dtype == torch.float64:
+            op.set_arithmetic("native")
     peak, peak_kind = measured_peak_hbm()
 
     def line(ms):
@@ -403,7 +414,10 @@ def run_batch(args):
                                   "2..5, cells per dimension 4..12, unit random velocity, FP32 or FP64, periodic "
                                   "unit box, numpy default_rng(0)", "n_dofs_total": n_total,
                       "l2_flush": "inputs larger than L2 (%.1f GB resident)" % (bytes_step / 6 / 1e9)},
-           "graph_replay": line(ms_graph), "batched_autotuned": line(ms_tuned), "batched_default_tiles":
+           "graph_replay": line(ms_graph),
+           "graph_replay_f64_fp32x2": dict(line(ms_graph_x), note="FP64 instances with FP32x2 contractions "
+                                           "(hd_adv_set_arithmetic), FP64 storage"),
+           "batched_autotuned": line(ms_tuned), "batched_default_tiles":
            line(ms_default), "per_instance_launches": line(ms_single), "autotune_seconds": round(tune_s, 2),
            "classes": classes, "gpu_launches_per_step": launches_per_step,
            "roofline": {"bound": "hbm (FP32 classes) / FP64 pipe (FP64 classes)",

@@ -28,6 +28,7 @@ EXPORTED_SYMBOLS = (
     "hd_batch_create", "hd_batch_destroy", "hd_batch_n_classes", "hd_batch_class_info", "hd_batch_set_tile",
     "hd_batch_apply", "hd_batch_lsrk_step", "hd_batch_graph_capture", "hd_batch_graph_launch", "hd_batch_autotune",
     "hd_adv_autotune", "hd_vp_lsrk_step_fused", "hd_adv_set_arithmetic", "hd_adv_arithmetic",
+    "hd_batch_class_arithmetic",
 )
 HD_KERNEL_AUTO, HD_KERNEL_GENERIC, HD_KERNEL_PIPELINED = 0, 1, 2
 HD_ARITH_NATIVE, HD_ARITH_FP32X2 = 0, 1
@@ -143,6 +144,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.hd_batch_destroy.argtypes = [vp]
     L.hd_batch_n_classes.argtypes = [vp]
     L.hd_batch_class_info.argtypes = [vp, ctypes.c_int, ip, ip, ip, ip, ip, ip, ip]
+    L.hd_batch_class_arithmetic.argtypes = [vp, ctypes.c_int]
     L.hd_batch_set_tile.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.hd_batch_apply.argtypes = [vp, vpp, vpp, dp, vp]
     L.hd_batch_lsrk_step.argtypes = [vp, vpp, vpp, vpp, dp, dp, vp]

@@ -77,7 +77,9 @@ class AdvectionBatch:
         for c in range(int(self._L.hd_batch_n_classes(self._h))):
             v = [ctypes.c_int(0) for _ in range(7)]
             check(self._L.hd_batch_class_info(self._h, c, *[ctypes.byref(x) for x in v]))
+            ar = int(self._L.hd_batch_class_arithmetic(self._h, c))
             out.append({"dim": v[0].value, "degree": v[1].value, "dtype": _DTYPE[v[2].value],
+                        "arithmetic": "fp32x2" if ar == _lib.HD_ARITH_FP32X2 else "native",
                         "members": v[3].value, "batched": bool(v[4].value), "cells_per_cta": v[5].value,
                         "ctas_per_sm": v[6].value})
         return out
@@ -132,6 +134,12 @@ class AdvectionBatch:
             op._check_vec(v, name)
 
 
+def _tile_key(c: dict) -> str:
+    # "<dim>-<degree>-<dtype>", dtype "f64x" for FP64 storage in FP32x2 arithmetic
+    dt = "f64x" if c.get("arithmetic") == "fp32x2" else c["dtype"]
+    return "%d-%d-%s" % (c["dim"], c["degree"], dt)
+
+
 def save_tile_table(batch: AdvectionBatch, path: str) -> None:
     """Write the batch's per-class tiles ({"<dim>-<degree>-<dtype>": [cells_per_cta, ctas_per_sm]})."""
     table = {}
@@ -139,7 +147,7 @@ def save_tile_table(batch: AdvectionBatch, path: str) -> None:
         table = json.load(open(path))
     for c in batch.classes:
         if c["batched"]:
-            table["%d-%d-%s" % (c["dim"], c["degree"], c["dtype"])] = [c["cells_per_cta"], c["ctas_per_sm"]]
+            table[_tile_key(c)] = [c["cells_per_cta"], c["ctas_per_sm"]]
     with open(path, "w") as f:
         json.dump(table, f, indent=1, sort_keys=True)
 
@@ -149,7 +157,7 @@ def load_tile_table(batch: AdvectionBatch, path: str) -> int:
     table = json.load(open(path))
     n = 0
     for i, c in enumerate(batch.classes):
-        key = "%d-%d-%s" % (c["dim"], c["degree"], c["dtype"])
+        key = _tile_key(c)
         if c["batched"] and key in table:
             batch.set_tile(i, *table[key])
             n += 1

@@ -47,7 +47,7 @@ __global__ void advance_time_kernel(EclParams<T>* slots, int n_slots, int n, con
 namespace {
 
 struct BatchClass {
-  int D, N, dtype, gauss;
+  int D, N, dtype, gauss, arith;
   std::vector<int> members;  // instance indices
   bool batched;              // one launch per stage for the whole class
   hd::BatchLaunchers L;
@@ -180,7 +180,7 @@ int launch_slot(hd_batch* b, BatchClass& c, int slot, const std::vector<StageArg
   const int mode = args[0].mode;
   cudaError_t e;
   if (c.dtype == HD_F64)
-    e = c.L.f64(hd::BatchLaunch<double>{(hd::EclParams<double>*)c.d_slots + size_t(slot) * n, c.d_prefix, n, c.cpb,
+    e = (c.arith == HD_ARITH_FP32X2 ? c.L.f64x : c.L.f64)(hd::BatchLaunch<double>{(hd::EclParams<double>*)c.d_slots + size_t(slot) * n, c.d_prefix, n, c.cpb,
                                         c.per_sm},
                 mode, s);
   else
@@ -232,7 +232,7 @@ int hd_batch_create(hd_adv* const* ops, int n, const hd_lsrk* rk, hd_batch** out
   for (int i = 0; i < n; ++i) {
     const hd_adv* op = ops[i];
     auto it = std::find_if(b->classes.begin(), b->classes.end(), [&](const BatchClass& c) {
-      return c.D == op->D && c.N == op->N && c.dtype == op->dtype && c.gauss == op->gauss;
+      return c.D == op->D && c.N == op->N && c.dtype == op->dtype && c.gauss == op->gauss && c.arith == op->arith;
     });
     if (it == b->classes.end()) {
       BatchClass c;
@@ -240,6 +240,7 @@ int hd_batch_create(hd_adv* const* ops, int n, const hd_lsrk* rk, hd_batch** out
       c.N = op->N;
       c.dtype = op->dtype;
       c.gauss = op->gauss;
+      c.arith = op->arith;
       c.L = hd::batch_launchers(op->D, op->N);
       c.batched = c.L.ok && !op->gauss;  // the batch kernel is the collocation operator
       c.cpb = 0;
@@ -288,6 +289,11 @@ int hd_batch_class_info(const hd_batch* b, int c, int* D, int* degree, int* dtyp
   if (cells_per_cta) *cells_per_cta = k.batched ? (k.cpb > 0 ? k.cpb : maxc) : 0;
   if (ctas_per_sm) *ctas_per_sm = k.per_sm;
   return HD_OK;
+}
+
+int hd_batch_class_arithmetic(const hd_batch* b, int c) {
+  if (!b || c < 0 || c >= int(b->classes.size())) return -1;
+  return b->classes[c].arith;
 }
 
 int hd_batch_set_tile(hd_batch* b, int c, int cells_per_cta, int ctas_per_sm) {

@@ -5,7 +5,8 @@
 // computed with its own instance's parameters (mesh, line operators, stage
 // factors, vectors), and the next block -- of whichever instance -- is staged
 // by cp.async while the current one is computed, as in the single-instance
-// generic kernel (hd_ecl.cuh).
+// generic kernel (hd_ecl.cuh).  FP64 instances switched to FP32x2 arithmetic
+// (hd_adv_set_arithmetic) form their own class with the FP32x2 block.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -34,6 +35,7 @@ struct BatchLaunchers {
   int max_cpb_f64, max_cpb_f32;
   int def_cpb_f64, def_cpb_f32;  // default tiles (ecl_default_cpb)
   bool ok;
+  cudaError_t (*f64x)(const BatchLaunch<double>&, int mode, cudaStream_t);  // FP64 storage, FP32x2 arithmetic
 };
 
 // classes with a batch kernel: D in {4, 5}, N in {3..6} (degree 2..5);
@@ -42,8 +44,9 @@ BatchLaunchers batch_launchers(int D, int N);
 BatchLaunchers batch_launchers_d4(int N);
 BatchLaunchers batch_launchers_d5(int N);
 
-template <int D, int N, typename T, int MODE>
-__global__ void __launch_bounds__(EclShape<D, N, T>::THREADS, EclShape<D, N, T>::MINB)
+template <int D, int N, typename T, int MODE, typename A = T>
+__global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
+                                  std::is_same_v<A, f32x2> ? 2 : EclShape<D, N, T>::MINB)
     ecl_batch_kernel(const EclParams<T>* __restrict__ params, const long long* __restrict__ prefix, int n, int cpb) {
   using S = EclShape<D, N, T>;
   constexpr int NC = S::NC, TPC = S::TPC;
@@ -100,7 +103,18 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS, EclShape<D, N, T>:
     cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
-    ecl_block<D, N, T, MODE>(params[inst], (b - s_prefix[inst]) * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+    if constexpr (std::is_same_v<A, f32x2>) {
+      // FP32x2: the staged input converted to double-word FP32 in place (as in ecl_kernel)
+      const int nv = cpb * EclTile<D, N, T>::CST;
+      for (int i = tid; i < nv; i += nthr) {
+        const double v = cur[i];
+        reinterpret_cast<f32x2*>(cur)[i] = x2_from_double(v);
+      }
+      __syncthreads();
+      ecl_block_x2<D, N, MODE>(params[inst], (b - s_prefix[inst]) * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+    } else {
+      ecl_block<D, N, T, MODE>(params[inst], (b - s_prefix[inst]) * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+    }
     __syncthreads();
     odd = !odd;
     inst = ninst;
@@ -108,7 +122,7 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS, EclShape<D, N, T>:
   cp_async_wait<0>();
 }
 
-template <int D, int N, typename T>
+template <int D, int N, typename T, typename A = T>
 cudaError_t launch_batch(const BatchLaunch<T>& L, int mode, cudaStream_t stream) {
   using S = EclShape<D, N, T>;
   if constexpr (!S::SUPPORTED) {
@@ -149,10 +163,10 @@ cudaError_t launch_batch(const BatchLaunch<T>& L, int mode, cudaStream_t stream)
       return cudaGetLastError();
     };
     switch (mode) {
-      case kApply: return go(ecl_batch_kernel<D, N, T, kApply>);
-      case kStageFirst: return go(ecl_batch_kernel<D, N, T, kStageFirst>);
-      case kStageMid: return go(ecl_batch_kernel<D, N, T, kStageMid>);
-      case kStageLast: return go(ecl_batch_kernel<D, N, T, kStageLast>);
+      case kApply: return go(ecl_batch_kernel<D, N, T, kApply, A>);
+      case kStageFirst: return go(ecl_batch_kernel<D, N, T, kStageFirst, A>);
+      case kStageMid: return go(ecl_batch_kernel<D, N, T, kStageMid, A>);
+      case kStageLast: return go(ecl_batch_kernel<D, N, T, kStageLast, A>);
       default: return cudaErrorInvalidValue;
     }
   }
@@ -172,7 +186,8 @@ BatchLaunchers make_batch_launchers() {
   constexpr int m64 = batch_max_cpb<D, N, double>(), m32 = batch_max_cpb<D, N, float>();
   constexpr int d64 = ecl_default_cpb<D, N, double>(), d32 = ecl_default_cpb<D, N, float>();
   return BatchLaunchers{&launch_batch<D, N, double>, &launch_batch<D, N, float>, m64, m32, d64 < m64 ? d64 : m64,
-                        d32 < m32 ? d32 : m32, EclShape<D, N, double>::SUPPORTED && EclShape<D, N, float>::SUPPORTED};
+                        d32 < m32 ? d32 : m32, EclShape<D, N, double>::SUPPORTED && EclShape<D, N, float>::SUPPORTED,
+                        &launch_batch<D, N, double, f32x2>};
 }
 
 }  // namespace hd

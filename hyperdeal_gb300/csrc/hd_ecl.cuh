@@ -79,16 +79,28 @@ struct EclParams {
 
 enum EclMode { kApply = 0, kStageFirst = 1, kStageMid = 2, kStageLast = 3 };
 
+// (explicitly rounded operations here and in the boundary values below: the
+// result must not depend on how the surrounding kernel lets the compiler fuse
+// multiplies and adds, so that every kernel evaluating the same boundary data
+// gets the same bits)
 __device__ __forceinline__ double eval_function(const DevFunction& f, const double* x, int D, double t) {
   if (f.kind == 0) return 0.0;
   if (f.kind == 1) return f.amp;
   double r = f.amp;
   for (int d = 0; d < D; ++d) {
-    const double arg = f.omega[d] * (x[d] - f.speed[d] * t) + f.phase[d];
-    r *= f.cosine[d] ? cos(arg) : sin(arg);
+    const double arg = __fma_rn(f.omega[d], __fma_rn(-f.speed[d], t, x[d]), f.phase[d]);
+    r = __dmul_rn(r, f.cosine[d] ? cos(arg) : sin(arg));
   }
   return r;
 }
+
+// coordinate lo + (c + xi) h of a node (xi: reference coordinate in [0, 1])
+__device__ __forceinline__ double node_coord(double lo, int c, double xi, double h) {
+  return __fma_rn(__dadd_rn(double(c), xi), h, lo);
+}
+
+// exterior value of an inhomogeneous Dirichlet face: u+ = -u- + 2 g
+__device__ __forceinline__ double dirichlet_exterior(double um, double g) { return __fma_rn(2.0, g, -um); }
 
 // threads per cell and cells per CTA
 template <int D, int N, typename T>
@@ -175,10 +187,10 @@ __device__ __forceinline__ T boundary_value(const EclParams<T>& P, const int* cc
   for (int e = 0; e < D; ++e) {
     const int ie = t % N;
     t /= N;
-    x[e] = (e == d) ? P.lo[e] + (cc[e] + (P.op[d].step > 0 ? 1 : 0)) * P.h[e]
-                    : P.lo[e] + (cc[e] + P.gl[ie]) * P.h[e];
+    x[e] = (e == d) ? node_coord(P.lo[e], cc[e], P.op[d].step > 0 ? 1.0 : 0.0, P.h[e])
+                    : node_coord(P.lo[e], cc[e], P.gl[ie], P.h[e]);
   }
-  return T(-double(um) + 2.0 * eval_function(P.bc, x, D, P.time));
+  return T(dirichlet_exterior(double(um), eval_function(P.bc, x, D, P.time)));
 }
 
 // ---- asynchronous global -> shared copies (cp.async; the copies of a group

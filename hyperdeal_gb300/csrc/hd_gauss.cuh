@@ -203,9 +203,10 @@ __device__ __forceinline__ void gauss_block(const EclParams<T>& P, const GaussEx
           for (int f = 0; f < D; ++f) {
             const int id = node % N;
             node /= N;
-            x[f] = (f == d) ? P.lo[f] + (cc[f] + (L.step > 0 ? 1 : 0)) * P.h[f] : P.lo[f] + (cc[f] + G.gq[id]) * P.h[f];
+            x[f] = (f == d) ? node_coord(P.lo[f], cc[f], L.step > 0 ? 1.0 : 0.0, P.h[f])
+                            : node_coord(P.lo[f], cc[f], G.gq[id], P.h[f]);
           }
-          up = T(-double(um) + 2.0 * eval_function(P.bc, x, D, P.time));
+          up = T(dirichlet_exterior(double(um), eval_function(P.bc, x, D, P.time)));
         }
       }
 #pragma unroll

@@ -235,9 +235,10 @@ int hd_lsrk_coefficients(const hd_lsrk *rk, double *ai, double *bi, double *ci);
  * grouped by class (dim_x + dim_v, degree, dtype); a class with a batch
  * kernel (dim_x + dim_v in {4, 5}, degree 2..5) runs as ONE persistent launch
  * per RK stage over all its instances, other classes launch per instance.
- * The scheme is fixed at creation; the handle keeps pointers to the
- * operators (they must outlive it).  Results equal the per-instance
- * hd_lsrk_step / hd_adv_apply. */
+ * The scheme and the classes (dimension, degree, storage type and, for the
+ * batched classes, the arithmetic set by hd_adv_set_arithmetic) are fixed at
+ * creation; FP64 operators in FP32x2 arithmetic form their own classes.  The handle keeps pointers to the operators (they must outlive
+ * it).  Results equal the per-instance hd_lsrk_step / hd_adv_apply. */
 typedef struct hd_batch hd_batch;
 
 int hd_batch_create(hd_adv *const *ops, int n_ops, const hd_lsrk *rk, hd_batch **out);
@@ -245,6 +246,8 @@ int hd_batch_destroy(hd_batch *b);
 int hd_batch_n_classes(const hd_batch *b);
 int hd_batch_class_info(const hd_batch *b, int cls, int *dim, int *degree, int *dtype, int *n_members, int *batched,
                         int *cells_per_cta, int *ctas_per_sm);
+/* arithmetic of class cls (HD_ARITH_NATIVE / HD_ARITH_FP32X2), -1 on a bad class */
+int hd_batch_class_arithmetic(const hd_batch *b, int cls);
 /* tile of class cls (-1: all classes); 0 = default */
 int hd_batch_set_tile(hd_batch *b, int cls, int cells_per_cta, int ctas_per_sm);
 /* dst[i] = A_i src[i] at time[i] (time may be NULL: 0) */

@@ -179,3 +179,47 @@ def test_single_operator_autotune_keeps_results():
         assert tile["cells_per_cta"] >= 1 and tile["ms_per_apply"] > 0
         op.apply(dst, u, 0.0)
         assert torch.equal(dst, ref)
+
+
+def test_fp32x2_instances_equal_single_operators():
+    """FP64 operators switched to FP32x2 arithmetic form their own batch class
+    (beside the native FP64 ones of the same shape) and equal their own
+    single-operator FP32x2 path bit for bit, apply and fused steps."""
+    specs = [(2, 2, 3, 3, 3, "f64", False), (2, 2, 3, 2, 4, "f64", False), (2, 3, 2, 2, 3, "f64", True),
+             (2, 2, 3, 3, 2, "f64", False)]
+    ops, us, probs = [], [], []
+    for i, s in enumerate(specs):
+        op, u, prob = _make(s, 300 + i)
+        if i < 3:
+            op.set_arithmetic("fp32x2")
+        ops.append(op)
+        us.append(u)
+        probs.append(prob)
+    batch = B.AdvectionBatch(ops, "rk45")
+    cls = batch.classes
+    x2 = [c for c in cls if c["arithmetic"] == "fp32x2"]
+    nat = [c for c in cls if c["arithmetic"] == "native"]
+    assert sum(c["members"] for c in x2) == 3 and all(c["batched"] for c in x2)
+    assert len(nat) == 1 and nat[0]["members"] == 1 and (nat[0]["dim"], nat[0]["degree"]) == (4, 3)
+    dst = [op.initialize_dof_vector() for op in ops]
+    batch.apply(dst, us, [0.2] * len(ops))
+    for op, u, d, prob in zip(ops, us, dst, probs):
+        ref = op.initialize_dof_vector()
+        op.apply(ref, u, 0.2)
+        assert torch.equal(d, ref)
+        o = O.apply(prob, u.cpu().numpy(), 0.2)
+        assert np.abs(d.cpu().numpy() - o).max() <= 1e-12 * np.abs(o).max()
+    sols = [u.clone() for u in us]
+    Ks = [op.initialize_dof_vector() for op in ops]
+    Ts = [op.initialize_dof_vector() for op in ops]
+    refs = [u.clone() for u in us]
+    integ = [A.LowStorageRungeKuttaIntegrator(op.initialize_dof_vector(), op.initialize_dof_vector(), "rk45")
+             for op in ops]
+    times, dts = [0.0] * len(ops), [0.01] * len(ops)
+    for step in range(2):
+        batch.perform_time_step(sols, Ks, Ts, times, dts)
+        for i, op in enumerate(ops):
+            integ[i].perform_time_step(refs[i], times[i], dts[i], op)
+        times = [t + d for t, d in zip(times, dts)]
+    for s, r in zip(sols, refs):
+        assert torch.equal(s, r)
