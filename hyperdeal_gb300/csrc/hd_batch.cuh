@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
   __shared__ long long s_prefix[kBatchMaxInstances + 1];
   for (int i = threadIdx.x; i <= n; i += blockDim.x) s_prefix[i] = prefix[i];
   __syncthreads();
-  constexpr bool SU = EclStaging<D, N, T, MODE>::STAGE_U;
+  constexpr bool SU = EclStaging<D, N, T, MODE, A>::STAGE_U;
   const long long bufe = ecl_buffer_elems<D, N, T>(cpb);
   T* const s_in0 = reinterpret_cast<T*>(smem_raw);
   T* const s_in1 = s_in0 + bufe;
@@ -131,8 +131,8 @@ cudaError_t launch_batch(const BatchLaunch<T>& L, int mode, cudaStream_t stream)
     if (L.n < 1 || L.n > kBatchMaxInstances) return cudaErrorInvalidValue;
     if (mode < kApply || mode > kStageLast) return cudaErrorInvalidValue;
     int cpb = (L.cpb < 1 || L.cpb > S::CPB) ? ecl_default_cpb<D, N, T>() : L.cpb;
-    const int nbuf = mode == kStageMid ? EclStaging<D, N, T, kStageMid>::NBUF
-                     : mode == kStageLast ? EclStaging<D, N, T, kStageLast>::NBUF : 3;
+    const int nbuf = mode == kStageMid ? EclStaging<D, N, T, kStageMid, A>::NBUF
+                     : mode == kStageLast ? EclStaging<D, N, T, kStageLast, A>::NBUF : 3;
     // (the static prefix table takes 2 KiB beside the dynamic tiles); the
     // block offsets were made for this cpb, so it must fit as it is
     if (size_t(nbuf * ecl_buffer_elems<D, N, T>(cpb)) * sizeof(T) > 218 * 1024) return cudaErrorInvalidValue;

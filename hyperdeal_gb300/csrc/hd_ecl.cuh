@@ -611,9 +611,12 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
 // stage modes mid/last also stage the RK solution of the block (two more
 // buffers) when five buffers of one cell fit in shared memory (not for the
 // FP64 6D shapes: their 32 KiB+ cell tiles would leave one CTA per SM)
-template <int D, int N, typename T, int MODE>
+template <int D, int N, typename T, int MODE, typename A = T>
 struct EclStaging {
+  // (not for FP32x2 arithmetic either: its issue-bound kernels gain more from
+  // the CTAs that the two extra buffers would cost than from staging U)
   static constexpr bool STAGE_U = (MODE == kStageMid || MODE == kStageLast) && !(sizeof(T) == 8 && D == 6) &&
+                                  !std::is_same_v<A, f32x2> &&
                                   size_t(5) * EclShape<D, N, T>::NC * sizeof(T) + 64 <= 220 * 1024;
   static constexpr int NBUF = STAGE_U ? 5 : 3;
 };
@@ -631,7 +634,7 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
   constexpr int NC = S::NC, TPC = S::TPC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int cpb = P.cpb;
-  constexpr bool SU = EclStaging<D, N, T, MODE>::STAGE_U;
+  constexpr bool SU = EclStaging<D, N, T, MODE, A>::STAGE_U;
   const long long bufe = ecl_buffer_elems<D, N, T>(cpb);
   T* const s_in0 = reinterpret_cast<T*>(smem_raw);
   T* const s_in1 = s_in0 + bufe;
@@ -699,8 +702,8 @@ cudaError_t launch_ecl(const EclParams<T>& P0, int mode, cudaStream_t stream) {
     EclParams<T> P = P0;
     if (P.cpb < 1 || P.cpb > S::CPB) P.cpb = ecl_default_cpb<D, N, T>();
     if (mode < kApply || mode > kStageLast) return cudaErrorInvalidValue;
-    const int nbuf = mode == kStageMid ? EclStaging<D, N, T, kStageMid>::NBUF
-                     : mode == kStageLast ? EclStaging<D, N, T, kStageLast>::NBUF : 3;
+    const int nbuf = mode == kStageMid ? EclStaging<D, N, T, kStageMid, A>::NBUF
+                     : mode == kStageLast ? EclStaging<D, N, T, kStageLast, A>::NBUF : 3;
     // the staged tiles of the largest shape may not fit five times: shrink the tile
     while (P.cpb > 1 && size_t(nbuf * ecl_buffer_elems<D, N, T>(P.cpb)) * sizeof(T) > 220 * 1024) --P.cpb;
     const int threads = S::TPC * P.cpb;
