@@ -210,9 +210,11 @@ def run_vp(args):
     f0 = V.perturbed_maxwellian(VP_DIM_X, eps=0.01, k=0.5, perturbed_dims=(0, 1))
 
     def make(guess, dtype, tol, rhs_rel):
+        # "learned5": the learned guess with its Adam steps every 5th solve (once per rk45 step)
         p = V.VlasovPoissonParameters(VP_DIM_X, DEGREE, [VP_CELLS_X] * 2, [VP_CELLS_V] * 2, [0.0] * 2,
-                                      [two_pi] * 2, [-6.0] * 2, [6.0] * 2, dtype=dtype, cg_tol=tol, guess=guess,
-                                      cg_rhs_relative=rhs_rel)
+                                      [two_pi] * 2, [-6.0] * 2, [6.0] * 2, dtype=dtype, cg_tol=tol,
+                                      guess="learned" if guess == "learned5" else guess,
+                                      cg_rhs_relative=rhs_rel, learn_every=5 if guess == "learned5" else 0)
         return V.VlasovPoissonOperation(p)
 
     stream = torch.cuda.current_stream()
@@ -220,11 +222,13 @@ def run_vp(args):
     runs = {}
     clocks = None
     selected = [r.strip() for r in args.vp_runs.split(",")]
-    for dtype in ("f64", "f32"):
-        for guess in ("previous", "zero", "learned"):
+    for dtype in ("f64", "f64x", "f32"):  # f64x: FP64 storage, FP32x2 advection contractions
+        for guess in ("previous", "zero", "learned", "learned5"):
             if "%s/%s" % (dtype, guess) not in selected:
                 continue
-            op = make(guess, dtype, args.vp_tol, True)
+            op = make(guess, dtype[:3], args.vp_tol, True)
+            if dtype == "f64x":
+                op.set_arithmetic("fp32x2")
             sol = op.initialize_dof_vector()
             op.interpolate(f0, sol)
             Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
@@ -273,8 +277,10 @@ def run_vp(args):
             O.lsrk_step_op("rk45", fo, s * dt, dt, st.operator)
         cpu_s = (time.perf_counter() - c0) / args.vp_oracle_steps
         e_ref = np.array(st.diagnostics(fo)[:VP_DIM_X])
-        for dtype in ("f64", "f32"):
-            op = make("learned", dtype, args.vp_tol, True)
+        for dtype in ("f64", "f64x", "f32"):
+            op = make("learned", dtype[:3], args.vp_tol, True)
+            if dtype == "f64x":
+                op.set_arithmetic("fp32x2")
             sol = op.initialize_dof_vector()
             op.interpolate(f0, sol)
             Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
@@ -597,7 +603,8 @@ def main():
                     choices=["advection6d", "adv2d", "adv4d", "vp2x2v", "batch64"])
     ap.add_argument("--vp-tol", type=float, default=1e-10, help="CG: ||r|| <= tol ||rhs|| (vp2x2v)")
     ap.add_argument("--vp-oracle-steps", type=int, default=2, help="steps compared with the FP64 oracle (vp2x2v)")
-    ap.add_argument("--vp-runs", default="f64/previous,f64/zero,f64/learned,f32/previous,f32/zero,f32/learned",
+    ap.add_argument("--vp-runs", default="f64/previous,f64/zero,f64/learned,f64/learned5,f64x/previous,f64x/learned,"
+                                         "f32/previous,f32/zero,f32/learned",
                     help="dtype/guess combinations timed (vp2x2v)")
     args = ap.parse_args()
     if args.workload == "vp2x2v":

@@ -28,7 +28,7 @@ EXPORTED_SYMBOLS = (
     "hd_batch_create", "hd_batch_destroy", "hd_batch_n_classes", "hd_batch_class_info", "hd_batch_set_tile",
     "hd_batch_apply", "hd_batch_lsrk_step", "hd_batch_graph_capture", "hd_batch_graph_launch", "hd_batch_autotune",
     "hd_adv_autotune", "hd_vp_lsrk_step_fused", "hd_adv_set_arithmetic", "hd_adv_arithmetic",
-    "hd_batch_class_arithmetic",
+    "hd_batch_class_arithmetic", "hd_vp_set_arithmetic",
 )
 HD_KERNEL_AUTO, HD_KERNEL_GENERIC, HD_KERNEL_PIPELINED = 0, 1, 2
 HD_ARITH_NATIVE, HD_ARITH_FP32X2 = 0, 1
@@ -136,6 +136,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.hd_vp_fields.argtypes = [vp, vp, vp, vp, vp]
     L.hd_vp_cg_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int), llp, llp, dp, llp]
     L.hd_vp_set_guess.argtypes = [vp, ctypes.c_int]
+    L.hd_vp_set_arithmetic.argtypes = [vp, ctypes.c_int]
     L.hd_vp_learn_loss_grad.argtypes = [ctypes.c_longlong, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp,
                                         vp]
     vpp = ctypes.POINTER(vp)

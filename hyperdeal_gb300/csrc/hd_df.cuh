@@ -108,34 +108,6 @@ __device__ __forceinline__ double x2_to_double(const f32x2& a) {
   return __dadd_rn(x2_float_to_double(a.hi), x2_float_to_double(a.lo));
 }
 
-// ---- the kernels' arithmetic interface: A is the arithmetic type, T the
-// storage type (A == T: native arithmetic; A = f32x2 with T = double)
-template <typename A, typename T>
-__device__ __forceinline__ A ar_load(T x) {
-  if constexpr (std::is_same_v<A, T>) return x;
-  else return x2_from_double(x);
-}
-template <typename T>
-__device__ __forceinline__ T ar_store(float a) { return a; }
-template <typename T>
-__device__ __forceinline__ T ar_store(double a) { return a; }
-template <typename T>
-__device__ __forceinline__ T ar_store(const f32x2& a) { return x2_to_double(a); }
-
-template <typename A>
-__device__ __forceinline__ A ar_zero() {
-  if constexpr (std::is_same_v<A, f32x2>) return f32x2{0.f, 0.f};
-  else return A(0);
-}
-
-__device__ __forceinline__ void ar_mac(float& acc, float c, float u) { acc = fmaf(c, u, acc); }
-__device__ __forceinline__ void ar_mac(double& acc, double c, double u) { acc = fma(c, u, acc); }
-__device__ __forceinline__ void ar_mac(f32x2& acc, const f32x2& c, const f32x2& u) { x2_mac(acc, c, u); }
-
-__device__ __forceinline__ float ar_norm(float a) { return a; }
-__device__ __forceinline__ double ar_norm(double a) { return a; }
-__device__ __forceinline__ f32x2 ar_norm(const f32x2& a) { return x2_norm(a); }
-
 // host: exact split of a double coefficient into hi + lo floats
 inline f32x2 x2_split_host(double v) {
   f32x2 r;

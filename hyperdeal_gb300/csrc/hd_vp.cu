@@ -551,6 +551,7 @@ struct hd_vp {
   hd_vp_desc desc;
   hd::VpGeom g;
   int dtype;
+  int arith;          // HD_ARITH_NATIVE / HD_ARITH_FP32X2 of the FP64 advection
   double* d_wv;       // v-node weights (NCv)
   double* d_partial;  // moment partials (nchunks * nx)
   int nchunks;
@@ -749,7 +750,7 @@ int solve_poisson(hd_vp* v, cudaStream_t s) {
   if (rc) return rc;
   // the solver's own (rho - rho_prev, phi - phi_prev) pair trains the learned guess
   hd::diff_kernel<<<nb, 256, 0, s>>>(nx, v->d_phi, v->d_phi_prev, v->d_dy);
-  const int every = v->desc.learn_every > 0 ? v->desc.learn_every : 5;
+  const int every = v->desc.learn_every > 0 ? v->desc.learn_every : 1;
   rc = vcuda(hd::vp_model_observe(v->model, v->d_dx, v->d_dy, s, (v->observed++ % every) == 0),
              "learned guess update");
   if (!rc) rc = vcuda(cudaMemcpyAsync(v->d_rho_prev, v->d_rho, sizeof(double) * nx, cudaMemcpyDeviceToDevice, s),
@@ -770,7 +771,7 @@ int vp_advect(hd_vp* v, int mode, const void* src, const void* uin, void* dst, v
   } else {
     hd::VpAdvParams<double> P{(const double*)src, (double*)dst, (const double*)uin, (double*)tout, fb, fa,
                               (const double*)v->d_xs, (const double*)v->d_es, v->g};
-    e = hd::launch_vp_advection(P, mode, s);
+    e = hd::launch_vp_advection(P, mode, s, v->arith == HD_ARITH_FP32X2);
   }
   return vcuda(e, "vp advection");
 }
@@ -795,6 +796,7 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
   std::memset(v, 0, sizeof(*v));
   v->desc = d;
   v->dtype = d.dtype;
+  v->arith = HD_ARITH_NATIVE;
   v->guess = d.guess;
   hd::VpGeom& g = v->g;
   g.dx = d.dim_x;
@@ -1079,6 +1081,16 @@ int hd_vp_cg_stats(const hd_vp* v, int* last_iterations, long long* total_iterat
   if (total_iterations) *total_iterations = st.total_iters;
   if (solves) *solves = st.solves;
   if (last_residual) *last_residual = st.last_res;
+  return HD_OK;
+}
+
+int hd_vp_set_arithmetic(hd_vp* v, int arithmetic) {
+  if (!v) return vfail(HD_ERR_INVALID, "hd_vp_set_arithmetic: null handle");
+  if (arithmetic != HD_ARITH_NATIVE && arithmetic != HD_ARITH_FP32X2)
+    return vfail(HD_ERR_INVALID, "unknown arithmetic");
+  if (arithmetic == HD_ARITH_FP32X2 && (v->dtype != HD_F64 || v->g.dx > 2))
+    return vfail(HD_ERR_UNSUPPORTED, "FP32x2 arithmetic needs FP64 storage and dim_x = dim_v <= 2");
+  v->arith = arithmetic;
   return HD_OK;
 }
 

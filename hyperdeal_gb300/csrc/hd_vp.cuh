@@ -54,6 +54,7 @@ struct VpAdvParams {
 };
 
 cudaError_t launch_vp_advection(const VpAdvParams<float>& P, int mode, cudaStream_t s);
-cudaError_t launch_vp_advection(const VpAdvParams<double>& P, int mode, cudaStream_t s);
+// x2: FP32x2 arithmetic (hd_df.cuh) for FP64 storage; 1x1v and 2x2v shapes
+cudaError_t launch_vp_advection(const VpAdvParams<double>& P, int mode, cudaStream_t s, bool x2 = false);
 
 }  // namespace hd

@@ -235,12 +235,153 @@ __device__ __forceinline__ void vp_block(const VpAdvParams<T>& P, const VpLine<T
   }
 }
 
-template <int D, int N, typename T, int MODE>
-__global__ void __launch_bounds__(EclShape<D, N, T>::THREADS, EclShape<D, N, T>::MINB)
-    vp_adv_kernel(const __grid_constant__ VpAdvParams<T> P, const __grid_constant__ VpLine<T> Lk, int cpb) {
+// The block in FP32x2 arithmetic on FP64 storage (hd_df.cuh), line by line as
+// ecl_block_x2 in hd_ecl.cuh: the staged input was converted to double-word
+// words in place; per line  t_i = sum_q G_iq u_q  (double-word), acc_i += s t_i
+// with the line's scale s, then the upwind face terms; the stage update is
+// done in FP64 on the rounded result.
+template <int D, int N, int MODE>
+__device__ __forceinline__ void vp_block_x2(const VpAdvParams<double>& P, const VpLine<f32x2>& Lk, long long cell0,
+                                            int lc, int tl, const double* su_all, double* so_all) {
+  using S = EclShape<D, N, double>;
+  constexpr int NC = S::NC, TPC = S::TPC, DX = D / 2;
+  constexpr int CST = EclTile<D, N, double>::CST;
+  const VpGeom& g = P.g;
+  const long long gid = cell0 + lc;
+  const bool valid = gid < g.n_cells;
+  int cc[D];
+  long long nbL[D], nbR[D];
+  long long gx = 0;
+  {
+    const long long gg = valid ? gid : 0;
+    gx = gg % g.ncx;
+    long long a = gx, b = gg / g.ncx;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      if (d < DX) { cc[d] = int(a % g.cells[d]); a /= g.cells[d]; }
+      else { cc[d] = int(b % g.cells[d]); b /= g.cells[d]; }
+      const long long cs = g.cstride[d];
+      nbL[d] = cc[d] > 0 ? gg - cs : gg + (long long)(g.cells[d] - 1) * cs;
+      nbR[d] = cc[d] + 1 < g.cells[d] ? gg + cs : gg - (long long)(g.cells[d] - 1) * cs;
+    }
+  }
+  const f32x2* sx = reinterpret_cast<const f32x2*>(su_all + lc * CST);
+  f32x2* so = reinterpret_cast<f32x2*>(so_all + lc * CST);
+  const long long g0 = gid * NC;
+  auto line_scale = [&](int d, int bnode) -> double {
+    if (d < DX) {
+      const int e = DX + d;
+      int ie = bnode;
+      for (int k = 0; k < e; ++k) ie /= N;
+      return __ldg(P.xs + (d * g.cells[e] + cc[e]) * N + ie % N);
+    }
+    return __ldg(P.es + (gx * g.NCx + (bnode % ipow(N, DX))) * DX + (d - DX));
+  };
+
+#pragma unroll 1
+  for (int ph = 0; ph < S::NPH; ++ph) {
+    const int dA = 2 * ph;
+    const int dB = (2 * ph + 1 < D) ? 2 * ph + 1 : -1;
+    int strideA = 1;
+    for (int e = 0; e < dA; ++e) strideA *= N;
+    const int strideB = strideA * N;
+    const int nitems = dB >= 0 ? ipow(N, D - 2) : ipow(N, D - 1);
+    const int ndir = dB >= 0 ? 2 : 1;
+    const int nl = dB >= 0 ? N : 1;
+    const int rot = nl > 1 ? tl % N : 0;
+    const bool lastph = ph == S::NPH - 1;
+    for (int item = tl; item < nitems; item += TPC) {
+      const int base = item_base<D, N>(item, dA, dB);
+#pragma unroll 1
+      for (int dd = 0; dd < ndir; ++dd) {
+        const int d = dd == 0 ? dA : dB;
+        const int st = dd == 0 ? strideA : strideB;   // along the line
+        const int lst = dd == 0 ? strideB : strideA;  // between the lines
+        const bool first = ph == 0 && dd == 0;
+        const bool fin = lastph && dd == ndir - 1;
+        int l = rot;
+#pragma unroll 1
+        for (int j = 0; j < nl; ++j) {
+          const int lb = base + l * lst;
+          l = l + 1 < nl ? l + 1 : 0;
+          const double sc = valid ? line_scale(d, lb) : 0.0;
+          // upwind trace (the neighbour cells are valid cells even for an invalid gid)
+          const double up = __ldg(P.src + (sc > 0.0 ? nbL[d] * NC + lb + (N - 1) * st : nbR[d] * NC + lb));
+          f32x2 u[N], acc[N];
+          if ((N % 2) == 0 && st == 1) {
+#pragma unroll
+            for (int q = 0; q < N; q += 2) {
+              const float4 w = *reinterpret_cast<const float4*>(sx + lb + q);
+              u[q] = f32x2{w.x, w.y};
+              u[q + 1] = f32x2{w.z, w.w};
+            }
+          } else {
+#pragma unroll
+            for (int q = 0; q < N; ++q) u[q] = sx[lb + q * st];
+          }
+          if (first) {
+#pragma unroll
+            for (int i = 0; i < N; ++i) acc[i] = f32x2{0.f, 0.f};
+          } else {
+#pragma unroll
+            for (int i = 0; i < N; ++i) acc[i] = so[lb + i * st];
+          }
+          if (sc != 0.0) {
+            const f32x2 s2 = x2_from_double(sc);
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+              f32x2 t{0.f, 0.f};
+#pragma unroll
+              for (int q = 0; q < N; ++q) x2_mac(t, Lk.G[i * N + q], u[q]);
+              x2_mac(acc[i], s2, x2_norm(t));
+            }
+            // upwind face: (s / w_k)(u+ - u-) at the inflow node
+            f32x2 c0{0.f, 0.f}, ck{0.f, 0.f};
+            x2_mac(c0, s2, Lk.winv0);
+            x2_mac(ck, s2, Lk.winvk);
+            c0 = x2_norm(c0);
+            ck = x2_norm(ck);
+            const f32x2 nck{-ck.hi, -ck.lo};
+            const f32x2 upx = x2_from_double(up);
+            if (sc > 0.0) {
+              x2_mac(acc[N - 1], nck, u[N - 1]);
+              x2_mac(acc[0], c0, upx);
+            } else {
+              x2_mac(acc[0], c0, u[0]);
+              x2_mac(acc[N - 1], nck, upx);
+            }
+          }
+          if (!fin) {
+#pragma unroll
+            for (int i = 0; i < N; ++i) so[lb + i * st] = x2_norm(acc[i]);
+          } else if (valid) {
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+              const long long gi = g0 + lb + i * st;
+              const double k = x2_to_double(acc[i]);
+              if constexpr (MODE == kApply) {
+                P.dst[gi] = k;
+              } else {
+                const double uv = P.uin[gi];  // exact U in FP64 (kStageFirst: the stage input)
+                P.dst[gi] = fma(P.fb, k, uv);
+                if constexpr (MODE != kStageLast) P.tout[gi] = fma(P.fa, k, uv);
+              }
+            }
+          }
+        }
+      }
+    }
+    if (!lastph) __syncthreads();
+  }
+}
+
+template <int D, int N, typename T, int MODE, typename A = T>
+__global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
+                                  std::is_same_v<A, f32x2> ? 2 : EclShape<D, N, T>::MINB)
+    vp_adv_kernel(const __grid_constant__ VpAdvParams<T> P, const __grid_constant__ VpLine<A> Lk, int cpb) {
   using S = EclShape<D, N, T>;
   constexpr int NC = S::NC, TPC = S::TPC;
-  constexpr bool SU = EclStaging<D, N, T, MODE>::STAGE_U;
+  constexpr bool SU = EclStaging<D, N, T, MODE, A>::STAGE_U;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const long long bufe = ecl_buffer_elems<D, N, T>(cpb);
   T* const s_in0 = reinterpret_cast<T*>(smem_raw);
@@ -272,64 +413,93 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS, EclShape<D, N, T>:
     cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
-    vp_block<D, N, T, MODE>(P, Lk, b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+    if constexpr (std::is_same_v<A, f32x2>) {
+      // FP32x2: the staged input converted to double-word FP32 in place, once per value
+      const int nv = cpb * EclTile<D, N, T>::CST;
+      for (int i = tid; i < nv; i += nthr) {
+        const double v = cur[i];
+        reinterpret_cast<f32x2*>(cur)[i] = x2_from_double(v);
+      }
+      __syncthreads();
+      vp_block_x2<D, N, MODE>(P, Lk, b * cpb, lc, tl, cur, s_o);
+    } else {
+      vp_block<D, N, T, MODE>(P, Lk, b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+    }
     __syncthreads();
     odd = !odd;
   }
   cp_async_wait<0>();
 }
 
+template <int D, int N, typename T, typename A>
+static cudaError_t launch_vp_kernel(const VpAdvParams<T>& P, const VpLine<A>& Lk, int mode, cudaStream_t s) {
+  using S = EclShape<D, N, T>;
+  const int nbuf = mode == kStageMid ? EclStaging<D, N, T, kStageMid, A>::NBUF
+                   : mode == kStageLast ? EclStaging<D, N, T, kStageLast, A>::NBUF : 3;
+  // measured on GB300: FP32 is fastest with the largest tile, FP64 with the default one
+  int cpb = sizeof(T) == 4 ? S::CPB : ecl_default_cpb<D, N, T>();
+  while (cpb > 1 && size_t(nbuf * ecl_buffer_elems<D, N, T>(cpb)) * sizeof(T) > 220 * 1024) --cpb;
+  const int threads = S::TPC * cpb;
+  const size_t smem = size_t(nbuf * ecl_buffer_elems<D, N, T>(cpb)) * sizeof(T);
+  static bool attr_done[4] = {false, false, false, false};
+  static int sms = 0;
+  auto go = [&](auto kern) -> cudaError_t {
+    if (!attr_done[mode]) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+      if (e != cudaSuccess) return e;
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      attr_done[mode] = true;
+    }
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    const long long nblk = (P.g.n_cells + cpb - 1) / cpb;
+    const long long want = (long long)sms * per_sm;
+    kern<<<unsigned(nblk < want ? nblk : want), threads, smem, s>>>(P, Lk, cpb);
+    return cudaGetLastError();
+  };
+  switch (mode) {
+    case kApply: return go(vp_adv_kernel<D, N, T, kApply, A>);
+    case kStageFirst: return go(vp_adv_kernel<D, N, T, kStageFirst, A>);
+    case kStageMid: return go(vp_adv_kernel<D, N, T, kStageMid, A>);
+    default: return go(vp_adv_kernel<D, N, T, kStageLast, A>);
+  }
+}
+
+// x2: FP64 storage with FP32x2 arithmetic (built for the 1x1v and 2x2v shapes)
 template <int D, int N, typename T>
-static cudaError_t launch_vp_dn(const VpAdvParams<T>& P, int mode, cudaStream_t s) {
+static cudaError_t launch_vp_dn(const VpAdvParams<T>& P, int mode, cudaStream_t s, bool x2) {
   using S = EclShape<D, N, T>;
   if constexpr (!S::SUPPORTED) {
     return cudaErrorNotSupported;
   } else {
     if (mode < kApply || mode > kStageLast) return cudaErrorInvalidValue;
+    if (x2) {
+      if constexpr (sizeof(T) == 8 && D <= 4) {
+        VpLine<f32x2> Lx;
+        for (int i = 0; i < N * N; ++i) Lx.G[i] = x2_split_host(P.g.G[i]);
+        Lx.winv0 = x2_split_host(1.0 / P.g.glw[0]);
+        Lx.winvk = x2_split_host(1.0 / P.g.glw[N - 1]);
+        return launch_vp_kernel<D, N, T, f32x2>(P, Lx, mode, s);
+      } else {
+        return cudaErrorNotSupported;
+      }
+    }
     VpLine<T> Lk;
     for (int i = 0; i < N * N; ++i) Lk.G[i] = T(P.g.G[i]);
     Lk.winv0 = T(1.0 / P.g.glw[0]);
     Lk.winvk = T(1.0 / P.g.glw[N - 1]);
-    const int nbuf = mode == kStageMid ? EclStaging<D, N, T, kStageMid>::NBUF
-                     : mode == kStageLast ? EclStaging<D, N, T, kStageLast>::NBUF : 3;
-    // measured on GB300: FP32 is fastest with the largest tile, FP64 with the default one
-    int cpb = sizeof(T) == 4 ? S::CPB : ecl_default_cpb<D, N, T>();
-    while (cpb > 1 && size_t(nbuf * ecl_buffer_elems<D, N, T>(cpb)) * sizeof(T) > 220 * 1024) --cpb;
-    const int threads = S::TPC * cpb;
-    const size_t smem = size_t(nbuf * ecl_buffer_elems<D, N, T>(cpb)) * sizeof(T);
-    static bool attr_done[4] = {false, false, false, false};
-    static int sms = 0;
-    auto go = [&](auto kern) -> cudaError_t {
-      if (!attr_done[mode]) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        if (e != cudaSuccess) return e;
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        attr_done[mode] = true;
-      }
-      int per_sm = 0;
-      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
-      if (e != cudaSuccess) return e;
-      if (per_sm < 1) per_sm = 1;
-      const long long nblk = (P.g.n_cells + cpb - 1) / cpb;
-      const long long want = (long long)sms * per_sm;
-      kern<<<unsigned(nblk < want ? nblk : want), threads, smem, s>>>(P, Lk, cpb);
-      return cudaGetLastError();
-    };
-    switch (mode) {
-      case kApply: return go(vp_adv_kernel<D, N, T, kApply>);
-      case kStageFirst: return go(vp_adv_kernel<D, N, T, kStageFirst>);
-      case kStageMid: return go(vp_adv_kernel<D, N, T, kStageMid>);
-      default: return go(vp_adv_kernel<D, N, T, kStageLast>);
-    }
+    return launch_vp_kernel<D, N, T, T>(P, Lk, mode, s);
   }
 }
 
 template <typename T>
-static cudaError_t launch_vp_any(const VpAdvParams<T>& P, int mode, cudaStream_t s) {
+static cudaError_t launch_vp_any(const VpAdvParams<T>& P, int mode, cudaStream_t s, bool x2) {
 #define HD_VP_CASE(DD, NN) \
-  if (P.g.D == DD && P.g.N == NN) return launch_vp_dn<DD, NN, T>(P, mode, s);
+  if (P.g.D == DD && P.g.N == NN) return launch_vp_dn<DD, NN, T>(P, mode, s, x2);
   HD_VP_CASE(2, 2) HD_VP_CASE(2, 3) HD_VP_CASE(2, 4) HD_VP_CASE(2, 5) HD_VP_CASE(2, 6)
   HD_VP_CASE(4, 2) HD_VP_CASE(4, 3) HD_VP_CASE(4, 4) HD_VP_CASE(4, 5) HD_VP_CASE(4, 6)
   HD_VP_CASE(6, 2) HD_VP_CASE(6, 3) HD_VP_CASE(6, 4)
@@ -338,10 +508,10 @@ static cudaError_t launch_vp_any(const VpAdvParams<T>& P, int mode, cudaStream_t
 }
 
 cudaError_t launch_vp_advection(const VpAdvParams<float>& P, int mode, cudaStream_t s) {
-  return launch_vp_any(P, mode, s);
+  return launch_vp_any(P, mode, s, false);
 }
-cudaError_t launch_vp_advection(const VpAdvParams<double>& P, int mode, cudaStream_t s) {
-  return launch_vp_any(P, mode, s);
+cudaError_t launch_vp_advection(const VpAdvParams<double>& P, int mode, cudaStream_t s, bool x2) {
+  return launch_vp_any(P, mode, s, x2);
 }
 
 }  // namespace hd

@@ -51,7 +51,7 @@ class VlasovPoissonParameters:
     learn_rank: int = 0
     learn_history: int = 0
     cg_rhs_relative: bool = False  # False: ||r|| <= cg_tol ||r_0|| as deal.II's ReductionControl
-    learn_every: int = 0  # Adam steps every n-th solve (0: 5)
+    learn_every: int = 0  # Adam steps every n-th solve (0: every solve)
 
     def c(self) -> _lib.hd_vp_desc:
         d = _lib.hd_vp_desc()
@@ -185,6 +185,12 @@ class VlasovPoissonOperation:
                                      ctypes.byref(res), ctypes.byref(picked)))
         return {"last_iterations": it.value, "total_iterations": tot.value, "solves": solves.value,
                 "last_residual": res.value, "learned_picked": picked.value}
+
+    def set_arithmetic(self, arithmetic: str) -> None:
+        """'native' (FP64 advection contractions) or 'fp32x2' (double-word FP32
+        contractions on FP64 storage; the Poisson solve stays FP64)."""
+        v = {"native": _lib.HD_ARITH_NATIVE, "fp32x2": _lib.HD_ARITH_FP32X2}[arithmetic]
+        check(self._L.hd_vp_set_arithmetic(self._h, v))
 
     def set_guess(self, guess: str) -> None:
         check(self._L.hd_vp_set_guess(self._h, _GUESS[guess]))

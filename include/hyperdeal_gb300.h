@@ -303,7 +303,7 @@ typedef struct hd_vp_desc {
                            iterations                                         */
   int learn_every;      /* the learned guess stores every solve's pair and
                            takes its Adam steps every learn_every-th solve
-                           (0: 5, once per rk45 step)                         */
+                           (0: 1, every solve)                                */
 } hd_vp_desc;
 
 typedef struct hd_vp hd_vp;
@@ -336,6 +336,10 @@ int hd_vp_fields(hd_vp *vp, double *rho, double *phi, double *E, void *stream);
 int hd_vp_cg_stats(const hd_vp *vp, int *last_iterations, long long *total_iterations, long long *solves,
                    double *last_residual, long long *learned_picked);
 int hd_vp_set_guess(hd_vp *vp, int guess);
+/* arithmetic of the FP64-storage phase-space advection (hd_adv_set_arithmetic):
+ * HD_ARITH_NATIVE (default) or HD_ARITH_FP32X2 (dim_x = dim_v <= 2); the
+ * moments, the Poisson solve, the field and the stage update stay FP64 */
+int hd_vp_set_arithmetic(hd_vp *vp, int arithmetic);
 /* loss = 1/(2B) sum_b ||W2 W1 x_b - y_b||^2 and its gradients with the learned
  * guess's own training kernels (device pointers, row-major W1: r x n,
  * W2: n x r, X, Y: B x n) -- exposed to check them against a CPU reference */

@@ -195,6 +195,8 @@ class VlasovPoissonOperation {
     return out;
   }
   long long n_dofs() const { return hd_vp_n_dofs(h_); }
+  // FP64 storage: advection contractions in FP64 (HD_ARITH_NATIVE) or double-word FP32 (HD_ARITH_FP32X2)
+  void set_arithmetic(int arithmetic) { check(hd_vp_set_arithmetic(h_, arithmetic)); }
   hd_vp* handle() const { return h_; }
   cudaStream_t stream() const { return stream_; }
   DeviceVector<Number> create_vector() const { return DeviceVector<Number>(n_dofs()); }

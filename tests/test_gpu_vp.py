@@ -214,3 +214,72 @@ def test_fused_step_equals_unfused(dtype):
             op.perform_time_step(integ, f, s * 1e-3, 1e-3)
         out[fused] = f.double().cpu().numpy()
     assert _rel(out[True], out[False]) <= (1e-12 if dtype == "f64" else 2e-6)
+
+
+@pytest.mark.parametrize("dim_x,degree,cx,cv", CASES[:3])
+def test_fp32x2_apply_matches_oracle(dim_x, degree, cx, cv):
+    """FP64 storage with double-word FP32 advection contractions (hd_vp_set_arithmetic): the
+    operator against the oracle at the FP64 bar of test_apply_matches_oracle, and against the
+    native FP64 operator to 1e-12 (the field is solved identically in FP64 in both)."""
+    op, prob = _setup(dim_x, degree, cx, cv)
+    rng = np.random.default_rng(7 + dim_x * 10 + degree)
+    fo = O.interpolate(prob, O.vp_initial_function(dim_x, dim_x, eps=0.2))
+    fo = fo * (1.0 + 0.05 * rng.standard_normal(fo.size))
+    src = torch.tensor(fo, device="cuda")
+    nat = op.initialize_dof_vector()
+    op.apply(nat, src, 0.0)
+    op.set_arithmetic("fp32x2")
+    x2 = op.initialize_dof_vector()
+    op.apply(x2, src, 0.0)
+    st = O.VPState(prob, 1e-12)
+    ref = np.zeros_like(fo)
+    st.operator(fo, ref, 0.0)
+    assert _rel(x2.cpu().numpy(), ref) <= 1e-9
+    assert _rel(x2.cpu().numpy(), nat.cpu().numpy()) <= 1e-12
+
+
+def test_fp32x2_steps_equal_native():
+    """Four fused rk45 steps of the 2x2v problem in FP32x2 and in native FP64 arithmetic: the
+    distributions and the field energies agree to 1e-12; FP32 storage is refused."""
+    dim_x, degree, cx, cv = 2, 3, 4, 6
+    out, energy = {}, {}
+    for ar in ("native", "fp32x2"):
+        op, _ = _setup(dim_x, degree, cx, cv, guess="zero")
+        op.set_arithmetic(ar)
+        f = op.initialize_dof_vector()
+        op.interpolate(V.perturbed_maxwellian(dim_x, eps=0.05, perturbed_dims=(0, 1)), f)
+        _run_steps(op, f, 4, 1e-2)
+        out[ar] = f.cpu().numpy()
+        energy[ar] = op.diagnostics(f)
+    assert _rel(out["fp32x2"], out["native"]) <= 1e-12
+    assert _rel(energy["fp32x2"], energy["native"]) <= 1e-12
+    op32, _ = _setup(dim_x, degree, cx, cv, dtype="f32")
+    with pytest.raises(Exception):
+        op32.set_arithmetic("fp32x2")
+
+
+def test_learned_guess_saves_iterations():
+    """What the trained network gains over the method without it, on the 2x2v benchmark problem
+    (16^2 x-cells, 32^2 v-cells, k = 3): at a fixed accuracy (||r|| <= 1e-10 ||rhs||), once the
+    model has seen a few solves, CG from the learned guess needs fewer iterations per solve than
+    from the previous potential (the reference's start)."""
+    per_solve = {}
+    for guess in ("previous", "learned"):
+        params = V.VlasovPoissonParameters(2, 3, [16, 16], [32, 32], [0.0] * 2, [4 * math.pi] * 2, [-6.0] * 2,
+                                           [6.0] * 2, dtype="f64", cg_tol=1e-10, guess=guess, cg_rhs_relative=True)
+        op = V.VlasovPoissonOperation(params)
+        f = op.initialize_dof_vector()
+        op.interpolate(V.perturbed_maxwellian(2, eps=0.01, k=0.5, perturbed_dims=(0, 1)), f)
+        Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
+        integ = V.LowStorageRungeKuttaIntegrator(Ki, Ti, "rk45")
+        dt = V.time_step_rule(1.0, 0.05, min(4 * math.pi / 16, 12.0 / 32 / 6.0), 3, 0.0, 1.0)
+        for s in range(3):
+            op.perform_time_step(integ, f, s * dt, dt)
+        st0 = op.cg_stats()
+        for s in range(3, 13):
+            op.perform_time_step(integ, f, s * dt, dt)
+        st1 = op.cg_stats()
+        per_solve[guess] = (st1["total_iterations"] - st0["total_iterations"]) / (st1["solves"] - st0["solves"])
+        if guess == "learned":
+            assert st1["learned_picked"] - st0["learned_picked"] > 0
+    assert per_solve["learned"] < per_solve["previous"], per_solve
