@@ -7,10 +7,11 @@
 // Prints the diagnostics lines of the reference ("Time, norm, error" at every
 // DiagnosticsTick) so its output can be compared with the reference's .out
 // files.  Gauss-Lobatto collocation (DoCollocation = true) or, with the
-// `gauss` argument, Gauss quadrature.
+// `gauss` argument, Gauss quadrature.  Storage f64 (FP64 arithmetic), f64x
+// (FP64 storage, double-word FP32 contractions) or f32.
 //
 // usage: advection_hyperrectangle dim_x dim_v degree subdivisions periodic(0|1)
-//                                 final_time rk_type [f64|f32] [time_step cfl tick] [gauss]
+//                                 final_time rk_type [f64|f64x|f32] [time_step cfl tick] [gauss]
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -23,7 +24,7 @@ using namespace hyperdeal_gb300;
 
 template <typename Number>
 int run(int dim_x, int dim_v, int degree, int subdivisions, bool periodic, double final_time, const std::string& rk,
-        double time_step, double cfl, double tick, bool gauss) {
+        double time_step, double cfl, double tick, bool gauss, bool fp32x2) {
   const int dim = dim_x + dim_v;
   // ExactSolution: sin(2 pi (x0 - a0 t)) prod_{d>=1} cos(2 pi (x_d - a_d t)), a = (1, 0.15, -0.05, 0, ...),
   // domain [-1, 1]^dim, Dirichlet data = the exact solution (hyperrectangle.h:29-66, :220-235)
@@ -49,6 +50,7 @@ int run(int dim_x, int dim_v, int degree, int subdivisions, bool periodic, doubl
   desc.quadrature = gauss ? HD_QUAD_GAUSS : HD_QUAD_GAUSS_LOBATTO;
 
   AdvectionOperation<Number> op(desc);
+  if (fp32x2) op.set_arithmetic(HD_ARITH_FP32X2);
   DeviceVector<Number> solution = op.create_vector(), Ki = op.create_vector(), Ti = op.create_vector();
   VectorTools::interpolate(op, exact, solution, 0.0);
   LowStorageRungeKuttaIntegrator<Number> integrator(Ki, Ti, rk);
@@ -73,7 +75,8 @@ int run(int dim_x, int dim_v, int degree, int subdivisions, bool periodic, doubl
 int main(int argc, char** argv) {
   if (argc < 8) {
     std::fprintf(stderr,
-                 "usage: %s dim_x dim_v degree subdivisions periodic final_time rk [f64|f32] [time_step cfl tick]\n",
+                 "usage: %s dim_x dim_v degree subdivisions periodic final_time rk [f64|f64x|f32] "
+                 "[time_step cfl tick] [gauss]\n",
                  argv[0]);
     return 2;
   }
@@ -89,8 +92,9 @@ int main(int argc, char** argv) {
   const bool gauss = argc > 12 && std::string(argv[12]) == "gauss";
   try {
     if (dtype == "f32")
-      return run<float>(dim_x, dim_v, degree, sub, periodic, final_time, rk, time_step, cfl, tick, gauss);
-    return run<double>(dim_x, dim_v, degree, sub, periodic, final_time, rk, time_step, cfl, tick, gauss);
+      return run<float>(dim_x, dim_v, degree, sub, periodic, final_time, rk, time_step, cfl, tick, gauss, false);
+    return run<double>(dim_x, dim_v, degree, sub, periodic, final_time, rk, time_step, cfl, tick, gauss,
+                       dtype == "f64x");
   } catch (const std::exception& e) {
     std::fprintf(stderr, "error: %s\n", e.what());
     return 1;

@@ -39,6 +39,15 @@ def test_cpp_application_reproduces_reference_golden(name, args):
         assert abs(t - rt) <= 0.5e-3 * max(abs(rt), 1e-3) + 1e-12
         assert abs(n - rn) <= max(1e-5, 1e-8 * abs(rn)) and abs(n - rn) / rn < 1e-9
         assert abs(e - re_) <= max(1e-5, 1e-8 * abs(re_))
+    # FP64 storage with FP32x2 contractions meets the same golden bar and prints the FP64 run's norms
+    # (to the printed 11 digits, one unit of the last one)
+    rx = subprocess.run([exe] + args + ["f64x"], capture_output=True, text=True, timeout=600)
+    assert rx.returncode == 0, rx.stderr
+    rows_x = _rows(rx.stdout)
+    assert len(rows_x) == len(ref)
+    for (t, n, e), (tx, nx, ex), (rt, rn, re_) in zip(rows, rows_x, ref):
+        assert abs(nx - rn) <= max(1e-5, 1e-8 * abs(rn)) and abs(ex - re_) <= max(1e-5, 1e-8 * abs(re_))
+        assert abs(nx - n) <= 2e-10 * abs(n)
     # the FP32-storage form of the same run stays within 1e-5 of the FP64 norms
     r32 = subprocess.run([exe] + args + ["f32"], capture_output=True, text=True, timeout=600)
     assert r32.returncode == 0, r32.stderr
