@@ -517,13 +517,14 @@ def run_adv4d(args):
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     vel = [1.0, 0.7, 0.5, 0.3]
+    k4 = args.adv4d_degree  # 3: the BASELINE configuration; other degrees for the compute-bound check
     f0 = A.Function(2, 1.0, omega=[2 * math.pi] * 4, speed=[0.0] * 4)
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     res, sols = {}, {}
     clocks = None
     for dtype in ("f32", "f64", "f64_fp32x2"):
-        p = A.AdvectionParameters(2, 2, 3, [16, 16], [16, 16], [0.0] * 2, [1.0] * 2, [0.0] * 2, [1.0] * 2, vel,
+        p = A.AdvectionParameters(2, 2, k4, [16, 16], [16, 16], [0.0] * 2, [1.0] * 2, [0.0] * 2, [1.0] * 2, vel,
                                   dtype=dtype[:3])
         op = A.AdvectionOperation(p)
         if dtype == "f64_fp32x2":
@@ -532,7 +533,7 @@ def run_adv4d(args):
         A.VectorTools.interpolate(op, f0, sol, 0.0)
         Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
         integ = A.LowStorageRungeKuttaIntegrator(Ki, Ti, "rk45")
-        dt = CFL * op.critical_time_step() / DEGREE ** 1.5
+        dt = CFL * op.critical_time_step() / k4 ** 1.5
         t = 0.0
         for _ in range(args.warmup):
             integ.perform_time_step(sol, t, dt, op)
@@ -564,7 +565,7 @@ def run_adv4d(args):
     cpu = None
     if not args.no_cpu:
         from oracle import oracle as O
-        prob = O.Problem(2, 2, 3, [16] * 4, [0.0] * 4, [1.0] * 4, vel)
+        prob = O.Problem(2, 2, k4, [16] * 4, [0.0] * 4, [1.0] * 4, vel)
         u = O.interpolate(prob, O.make_func(2, 1.0, omega=[2 * math.pi] * 4, speed=[0.0] * 4))
         c0 = time.perf_counter()
         O.lsrk_step(prob, "rk45", u, 0.0, 1e-4)
@@ -572,14 +573,15 @@ def run_adv4d(args):
         cpu = {"value": round(n * N_STAGES / cpu_s / 1e9, 4), "unit": "GDoF/s", "cores": os.cpu_count(),
                "kind": "port", "sample": "one rk45 step of the full 16^2 x 16^2 mesh by the oracle (FP64, OpenMP)"}
     peak, peak_kind = measured_peak_hbm()
-    out = {"metric": "advection GDoF/s (4D k=3, 16^2 x 16^2) FP32 and FP64 fused rk45", "value": res["f32"]["gdof_per_s"],
+    out = {"metric": "advection GDoF/s (4D k=%d, 16^2 x 16^2) FP32 and FP64 fused rk45" % k4,
+           "value": res["f32"]["gdof_per_s"],
            "unit": "GDoF/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": res["f32"]["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32", "data": "synthetic",
-           "config": {"workload": "4D (2x+2v) upwind DG advection, k=3 Gauss-Lobatto collocation, 16^2 x 16^2 cells "
-                                  "(65,536 cells, 16,777,216 DoFs), periodic unit box, velocity (1.0, 0.7, 0.5, 0.3), "
-                                  "f0 = prod sin(2 pi coord), fused rk45, CFL 0.2",
-                      "l2_flush": "none: 67 MB per FP32 vector (3 vectors 201 MB > 129 MB L2)"},
+           "config": {"workload": "4D (2x+2v) upwind DG advection, k=%d Gauss-Lobatto collocation, 16^2 x 16^2 cells "
+                                  "(65,536 cells, %d DoFs), periodic unit box, velocity (1.0, 0.7, 0.5, 0.3), "
+                                  "f0 = prod sin(2 pi coord), fused rk45, CFL 0.2" % (k4, n),
+                      "l2_flush": "none: %d MB per FP32 vector (3 vectors > 129 MB L2)" % (4 * n // 10 ** 6)},
            "f32": res["f32"], "f64": res["f64"], "f64_fp32x2": res["f64_fp32x2"], "l2_rel_err_f32_vs_f64": l2,
            "roofline": {"bound": "hbm", "achieved": res["f32"]["hbm_gb_per_s"], "peak": peak, "unit": "GB/s",
                         "frac": round(res["f32"]["hbm_gb_per_s"] / peak, 4), "peak_source": peak_kind},
@@ -601,6 +603,7 @@ def main():
                     help="x-cells per direction (8 = the benchmark workload; smaller only for profiling)")
     ap.add_argument("--workload", default="advection6d",
                     choices=["advection6d", "adv2d", "adv4d", "vp2x2v", "batch64"])
+    ap.add_argument("--adv4d-degree", type=int, default=3, help="degree of the adv4d workload (default 3)")
     ap.add_argument("--vp-tol", type=float, default=1e-10, help="CG: ||r|| <= tol ||rhs|| (vp2x2v)")
     ap.add_argument("--vp-oracle-steps", type=int, default=2, help="steps compared with the FP64 oracle (vp2x2v)")
     ap.add_argument("--vp-runs", default="f64/previous,f64/zero,f64/learned,f64/learned5,f64x/previous,f64x/learned,"
