@@ -123,3 +123,25 @@ def test_fp32x2_needs_f64_collocation():
     with pytest.raises(Exception):
         op32.set_arithmetic("fp32x2")
     assert op32.arithmetic == "native"
+
+
+def test_tiles_and_autotune_keep_results():
+    """The FP32x2 kernel's result does not depend on its tile: every tile of a 5D k=2 mesh and
+    the autotuned one give the same bits as the default tile."""
+    op, prob = make_x2(3, 2, 2, [3, 2, 2, 3, 2], [0.9, -0.4, 0.6, 0.2, -0.7])
+    u = torch.randn(prob.n_dofs, dtype=torch.float64, device="cuda")
+    ref = op.initialize_dof_vector()
+    op.apply(ref, u, 0.0)
+    max_cpb, _ = op.tile_limits()
+    for cpb in sorted({1, 2, max_cpb // 2, max_cpb} - {0}):
+        op.set_tile(cpb, 0)
+        d = op.initialize_dof_vector()
+        op.apply(d, u, 0.0)
+        assert torch.equal(d, ref), cpb
+    op.set_tile(0, 0)
+    scratch = op.initialize_dof_vector()
+    tuned = op.autotune(u, scratch, reps=1)
+    assert tuned["cells_per_cta"] >= 1
+    d = op.initialize_dof_vector()
+    op.apply(d, u, 0.0)
+    assert torch.equal(d, ref)
