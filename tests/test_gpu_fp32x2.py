@@ -58,7 +58,7 @@ def test_apply_dirichlet_and_skew(skew):
 
 def test_smooth_data_and_zero_values():
     """Smooth data (the contractions cancel) with exact zeros and tiny values
-    mixed in (the split's zero and FP64-conversion branches)."""
+    mixed in (the split's zero and FP32-precision ranges below 2^-103)."""
     op, prob = make_x2(2, 2, 4, [3, 3, 2, 2], [0.9, -0.6, 0.3, 0.2])
     f = O.make_func(2, 1.0, omega=[2 * math.pi] * 4, speed=[0.0] * 4)
     u = O.interpolate(prob, f)
