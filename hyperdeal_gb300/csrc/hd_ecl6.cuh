@@ -99,6 +99,23 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
+// the same with an L2 cache-policy hint (createpolicy)
+__device__ __forceinline__ void tma_load_2d_hint(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar,
+                                                 uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%2, "
+      "%3}], [%4], %5;" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(policy)
+      : "memory");
+}
+
+// L2 policy "evict first" for data read or written once per stage
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
   asm volatile(
       "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
@@ -200,6 +217,7 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
     if (tid == E6_CTHREADS) {
       int issued = 0;
       bool ok = true;
+      const uint64_t pol_u = l2_evict_first_policy();
       uint32_t bytes = 16384u + (READ_U ? 16384u : 0u);
 #pragma unroll
       for (int d = 2; d < 6; ++d) bytes += P.p.op[d].active ? 4096u : 0u;
@@ -218,7 +236,9 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
         float* st = s_stage + s * E6_STAGE_FLOATS;
         mbar_arrive_expect_tx(&full[s], bytes);
         tma_load_2d(st, &maps.tcell, 0, int(gid * 128), &full[s]);
-        if (READ_U) tma_load_2d(st + 4096, &maps.ucell, 0, int(gid * 128), &full[s]);
+        // U is read once per stage: evict it first, so that L2 keeps the stage
+        // input T, whose faces the neighbours read again later
+        if (READ_U) tma_load_2d_hint(st + 4096, &maps.ucell, 0, int(gid * 128), &full[s], pol_u);
         if (P.p.op[2].active)
           tma_load_3d(st + 8192, &maps.tx2, 0, P.p.op[2].nb_node, int((gid + R.nb[2]) * 64), &full[s]);
         if (P.p.op[3].active)
@@ -482,16 +502,17 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const float4 kv = *reinterpret_cast<const float4*>(so + vo + 1024 * j);
+          // results are streamed out (read again only in the next stage): evict-first stores
           if constexpr (MODE == kApply) {
-            go[256 * j] = kv;
+            __stcs(go + 256 * j, kv);
           } else {
             const float4 u = uv[j];
-            go[256 * j] = make_float4(fmaf(P.p.fb, kv.x, u.x), fmaf(P.p.fb, kv.y, u.y), fmaf(P.p.fb, kv.z, u.z),
-                                      fmaf(P.p.fb, kv.w, u.w));
+            __stcs(go + 256 * j, make_float4(fmaf(P.p.fb, kv.x, u.x), fmaf(P.p.fb, kv.y, u.y),
+                                             fmaf(P.p.fb, kv.z, u.z), fmaf(P.p.fb, kv.w, u.w)));
             if constexpr (MODE != kStageLast) {
               float4* gt = reinterpret_cast<float4*>(P.p.tout + gid * NC + vnode);
-              gt[256 * j] = make_float4(fmaf(P.p.fa, kv.x, u.x), fmaf(P.p.fa, kv.y, u.y), fmaf(P.p.fa, kv.z, u.z),
-                                        fmaf(P.p.fa, kv.w, u.w));
+              __stcs(gt + 256 * j, make_float4(fmaf(P.p.fa, kv.x, u.x), fmaf(P.p.fa, kv.y, u.y),
+                                               fmaf(P.p.fa, kv.z, u.z), fmaf(P.p.fa, kv.w, u.w)));
             }
           }
         }
