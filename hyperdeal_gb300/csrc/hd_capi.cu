@@ -394,7 +394,7 @@ int launch(hd_adv* op, int mode, const void* tin, const void* uin, void* uout, v
     hd::EclParams<float> P = op->p32;
     P.tin = (const float*)tin; P.uin = (const float*)uin; P.uout = (float*)uout; P.tout = (float*)tout;
     P.fb = float(fb); P.fa = float(fa); P.time = time;
-    e = hd::launch_ecl6(P, op->d_err, mode, s);
+    e = hd::launch_ecl6(P, op->d_err, op->d_err + 1, mode, s);
   } else if (op->dtype == HD_F64) {
     hd::EclParams<double> P = op->p64;
     P.tin = (const double*)tin; P.uin = (const double*)uin; P.uout = (double*)uout; P.tout = (double*)tout;
@@ -552,6 +552,7 @@ int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
     }
     cudaError_t e = cudaGetDevice(&op->device);
     if (e != cudaSuccess) { delete op; return cuda_fail(e, "cudaGetDevice"); }
+    // norm partials (2 * kNormBlocks), result (2), error flag + row ticket of the pipelined kernel (1)
     e = cudaMalloc(&op->d_partials, sizeof(double) * (2 * hd::kNormBlocks + 3));
     if (e != cudaSuccess) { delete op; return cuda_fail(e, "cudaMalloc (norm scratch)"); }
     op->d_err = reinterpret_cast<int*>(op->d_partials + 2 * hd::kNormBlocks + 2);

@@ -768,9 +768,10 @@ EclLaunchers make_launchers() {
 void set_last_error(const char* msg);
 
 // pipelined 6D degree-3 FP32 kernel (hd_ecl6.cu): eligible for fully periodic
-// 3x+3v meshes; err receives a device error code on a bounded-wait time-out
+// 3x+3v meshes; err receives a device error code on a bounded-wait time-out;
+// ticket is a device int the launch uses as its row counter
 bool ecl6_eligible(const EclParams<float>& P);
-cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int mode, cudaStream_t stream);
+cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int* ticket, int mode, cudaStream_t stream);
 
 // defined in hd_ecl_d{2..6}.cu
 EclLaunchers ecl_launchers_d2(int N);

@@ -77,12 +77,13 @@ bool ecl6_eligible(const EclParams<float>& P) {
   return true;
 }
 
-cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int mode, cudaStream_t stream) {
+cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int* ticket, int mode, cudaStream_t stream) {
   Ecl6Params E;
   E.p = P;
   E.row_len = P.cells[0];
   E.n_rows = int(P.n_cells / P.cells[0]);
   E.err = err;
+  E.ticket = ticket;
   Ecl6Maps maps;
   cudaError_t e = encode_ecl6_maps(P.tin, P.uin, P.n_cells * 4096LL, &maps);
   if (e != cudaSuccess) return e;
@@ -98,6 +99,9 @@ cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int mode, cudaStrea
       if (ee != cudaSuccess) return ee;
       attr_done[mode] = true;
     }
+    // the row tickets start at 0 for every launch (stream-ordered, also inside a captured graph)
+    cudaError_t ee = cudaMemsetAsync(ticket, 0, sizeof(int), stream);
+    if (ee != cudaSuccess) return ee;
     kern<<<grid, E6_THREADS, E6_SMEM, stream>>>(E, maps);
     return cudaGetLastError();
   };

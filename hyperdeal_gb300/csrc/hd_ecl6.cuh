@@ -2,7 +2,9 @@
 // degree-3 (4 nodes per direction), FP32-storage case, all faces periodic.
 //
 // Structure (one CTA per SM slot, 8 compute warps + 1 producer warp):
-//   * Work item = one x0-row of cells (consecutive cell ids).  A CTA walks the
+//   * Work item = one x0-row of cells (consecutive cell ids), claimed from a
+//     global ticket counter (one row ahead), so the rows in flight form a
+//     contiguous window.  A CTA walks the
 //     row in the upwind order of direction x0, so the x0 face trace a cell
 //     needs is the previous cell's face, which the thread owning that plane
 //     still holds in registers ("carry"); only a row's first cell reads it
@@ -150,6 +152,7 @@ struct Ecl6Params {
   int n_rows;          // x0-rows of cells
   int row_len;         // cells per row (cells in x0)
   int* err;            // device error flag
+  int* ticket;         // next unclaimed row (zeroed before every launch)
 };
 
 // first cell id of row r and the upwind-neighbour offsets (in cells) of the
@@ -197,6 +200,11 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
   uint64_t* full = bars;               // [E6_STAGES]: TMA bytes landed
   uint64_t* empty = bars + E6_STAGES;  // [E6_STAGES]: all 8 compute warps done with the slot
   volatile int* s_abort = reinterpret_cast<volatile int*>(bars + 2 * E6_STAGES);
+  // rows claimed by this CTA: s_rows[q % 4] = row of the CTA's q-th row (-1: none);
+  // s_cont[it & 1]: whether the compute warps continue after cell it (one decision
+  // for all of them, taken by thread 0 before a barrier)
+  volatile int* s_rows = reinterpret_cast<volatile int*>(bars + 2 * E6_STAGES) + 2;
+  volatile int* s_cont = s_rows + 4;
 
   const int tid = threadIdx.x;
   if (tid == 0) {
@@ -209,8 +217,10 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
   }
   __syncthreads();
 
-  const int n_my_rows = P.n_rows > (int)blockIdx.x ? (P.n_rows - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-  const int n_cells_cta = n_my_rows * P.row_len;
+  // Rows are claimed dynamically from a global ticket counter, one row ahead,
+  // so that the rows in flight across the grid stay a contiguous window of the
+  // row order (their upwind x1 / x2 / v0 neighbours are then read while still
+  // in L2), whatever the CTAs' relative speed.
 
   if (tid >= E6_CTHREADS) {
     // ------------------------------------------------------------------ producer
@@ -221,9 +231,17 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
       uint32_t bytes = 16384u + (READ_U ? 16384u : 0u);
 #pragma unroll
       for (int d = 2; d < 6; ++d) bytes += P.p.op[d].active ? 4096u : 0u;
-      int r = (int)blockIdx.x, k = 0;
-      E6Row R = e6_row(P, r < P.n_rows ? r : 0);
-      for (int it = 0; it < n_cells_cta; ++it) {
+      auto take = [&]() -> int {
+        const int t = atomicAdd(P.ticket, 1);
+        return t < P.n_rows ? t : -1;
+      };
+      int q = 0, k = 0;
+      int r = take();
+      s_rows[0] = r;
+      s_rows[1] = r >= 0 ? take() : -1;
+      E6Row R = e6_row(P, r >= 0 ? r : 0);
+      if (r < 0) mbar_arrive(&full[0]);  // no row for this CTA: release the compute warps
+      for (int it = 0; r >= 0; ++it) {
         const int s = it % E6_STAGES;
         if (it >= E6_STAGES && !mbar_wait(&empty[s], ((it / E6_STAGES) - 1) & 1)) {
           atomicExch(P.err, E6_ERR_TIMEOUT_EMPTY);
@@ -232,6 +250,12 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
           break;
         }
         if (*s_abort) { ok = false; break; }
+        if (k == 0 && q > 0) {
+          r = s_rows[q % 4];
+          if (r < 0) break;  // the compute warps stop at the end of row q - 1 by themselves
+          s_rows[(q + 1) % 4] = take();
+          R = e6_row(P, r);
+        }
         const long long gid = e6_cell(P, R.first, k);
         float* st = s_stage + s * E6_STAGE_FLOATS;
         mbar_arrive_expect_tx(&full[s], bytes);
@@ -250,8 +274,7 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
         ++issued;
         if (++k == P.row_len) {
           k = 0;
-          r += (int)gridDim.x;
-          if (r < P.n_rows) R = e6_row(P, r);
+          ++q;
         }
       }
       // on an abort, wait (bounded) for the copies still in flight before leaving
@@ -298,14 +321,22 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
       px1 = __ldg(reinterpret_cast<const float4*>(P.p.tin + (g + nb1) * NC + 16 * tid + 4 * L[1].nb_node));
   };
 
-  int r = (int)blockIdx.x, k = 0;
-  E6Row R = e6_row(P, r < P.n_rows ? r : 0);
-  if (n_cells_cta > 0) fetch_x1(e6_cell(P, R.first, 0), R.nb[1]);
-  for (int it = 0; it < n_cells_cta; ++it) {
+  // the first cell (or the producer's "no row" signal) decides whether there is work
+  if (lane == 0 && !mbar_wait(&full[0], 0)) {
+    *s_abort = 1;
+    atomicExch(P.err, E6_ERR_TIMEOUT_FULL);
+  }
+  __syncwarp();
+  if (tid == 0) s_cont[0] = (!*s_abort && s_rows[0] >= 0) ? 1 : 0;
+  bar_compute();
+  if (!s_cont[0]) return;
+  int q = 0, k = 0;
+  E6Row R = e6_row(P, s_rows[0]);
+  fetch_x1(e6_cell(P, R.first, 0), R.nb[1]);
+  for (int it = 0;; ++it) {
     const int s = it % E6_STAGES;
     const long long gid = e6_cell(P, R.first, k);
     const float* st = s_stage + s * E6_STAGE_FLOATS;
-    const bool has_next = it + 1 < n_cells_cta;
     const bool new_row = k + 1 == P.row_len;
 
     // row start: x0 face of the upwind neighbour of the row's first cell (periodic wrap)
@@ -323,6 +354,10 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
       atomicExch(P.err, E6_ERR_TIMEOUT_FULL);
     }
     __syncwarp();
+    // the CTA's next row was claimed before this row's first cell was issued
+    // (s_rows is read after that cell's barrier); -1: no next row
+    const int next_row = new_row ? s_rows[(q + 1) % 4] : -1;
+    const bool has_next = !new_row || next_row >= 0;
 
     // ---------------- phase 0: directions x0 (a) and x1 (b); plane = nodes 16*tid + a + 4b
     {
@@ -377,7 +412,7 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
     // x1 face of the next cell of this CTA
     if (has_next) {
       if (new_row) {
-        const E6Row Rn = e6_row(P, r + (int)gridDim.x);
+        const E6Row Rn = e6_row(P, next_row);
         fetch_x1(e6_cell(P, Rn.first, 0), Rn.nb[1]);
       } else {
         fetch_x1(e6_cell(P, R.first, k + 1), R.nb[1]);
@@ -518,12 +553,15 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
         }
       }
     }
-    // the accumulator tile is rewritten by the next cell's phase 0
+    // the accumulator tile is rewritten by the next cell's phase 0; whether
+    // to continue is decided once (thread 0) for all compute warps
+    if (tid == 0) s_cont[(it + 1) & 1] = (!*s_abort && has_next) ? 1 : 0;
     bar_compute();
+    if (!s_cont[(it + 1) & 1]) break;
     if (new_row) {
       k = 0;
-      r += (int)gridDim.x;
-      if (r < P.n_rows) R = e6_row(P, r);
+      ++q;
+      R = e6_row(P, next_row);
     } else {
       ++k;
     }
