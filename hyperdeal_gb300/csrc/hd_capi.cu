@@ -394,7 +394,8 @@ int launch(hd_adv* op, int mode, const void* tin, const void* uin, void* uout, v
     hd::EclParams<float> P = op->p32;
     P.tin = (const float*)tin; P.uin = (const float*)uin; P.uout = (float*)uout; P.tout = (float*)tout;
     P.fb = float(fb); P.fa = float(fa); P.time = time;
-    e = hd::launch_ecl6(P, op->d_err, op->d_err + 1, mode, s);
+    int* ticket = op->d_tickets + (op->ticket_slot++ % hd::kTicketSlots);
+    e = hd::launch_ecl6(P, op->d_err, ticket, mode, s);
   } else if (op->dtype == HD_F64) {
     hd::EclParams<double> P = op->p64;
     P.tin = (const double*)tin; P.uin = (const double*)uin; P.uout = (double*)uout; P.tout = (double*)tout;
@@ -552,10 +553,13 @@ int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
     }
     cudaError_t e = cudaGetDevice(&op->device);
     if (e != cudaSuccess) { delete op; return cuda_fail(e, "cudaGetDevice"); }
-    // norm partials (2 * kNormBlocks), result (2), error flag + row ticket of the pipelined kernel (1)
-    e = cudaMalloc(&op->d_partials, sizeof(double) * (2 * hd::kNormBlocks + 3));
+    // norm partials (2 * kNormBlocks), result (2), error flag of the pipelined kernel (1),
+    // the pipelined kernel's row counters (kTicketSlots ints)
+    e = cudaMalloc(&op->d_partials, sizeof(double) * (2 * hd::kNormBlocks + 3 + hd::kTicketSlots / 2));
     if (e != cudaSuccess) { delete op; return cuda_fail(e, "cudaMalloc (norm scratch)"); }
     op->d_err = reinterpret_cast<int*>(op->d_partials + 2 * hd::kNormBlocks + 2);
+    op->d_tickets = reinterpret_cast<int*>(op->d_partials + 2 * hd::kNormBlocks + 3);
+    op->ticket_slot = 0;
     e = cudaMemset(op->d_err, 0, sizeof(int));
     if (e != cudaSuccess) { cudaFree(op->d_partials); delete op; return cuda_fail(e, "cudaMemset (error flag)"); }
     op->variant = HD_KERNEL_AUTO;

@@ -39,6 +39,9 @@ struct hd_adv {
   hd::VecGeom geom;
   double* d_partials;  // norm reduction scratch (2*kNormBlocks + 2 doubles) + error flag
   int* d_err;          // device error flag of the pipelined kernel (inside d_partials)
+  int* d_tickets;      // kTicketSlots row counters of the pipelined kernel (inside d_partials)
+  unsigned ticket_slot;  // next counter: consecutive launches use different ones, so that
+                         // launches of one operator on different streams may overlap
   double* d_table;     // factor table of product functions (sum_d cells_d * (k+1) doubles)
   int device;
   int variant;         // HD_KERNEL_AUTO / _GENERIC / _PIPELINED
@@ -57,6 +60,7 @@ struct hd_lsrk {
 };
 
 namespace hd {
+constexpr int kTicketSlots = 64;
 // one stage launch of an operator (the kernel hd_adv_kernel reports)
 int adv_launch(hd_adv* op, int mode, const void* tin, const void* uin, void* uout, void* tout, double fb, double fa,
                double time, cudaStream_t s);

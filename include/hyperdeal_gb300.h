@@ -14,7 +14,10 @@
  *     stream).  All work of one call is enqueued on that stream; calls return
  *     without synchronising unless documented otherwise.
  *   - A handle is not thread-safe (as the reference operator, whose
- *     evaluators are members, is not re-entrant).
+ *     evaluators are members, is not re-entrant).  Calls on one handle from
+ *     one thread may target different streams and overlap on the device (up
+ *     to 64 launches of the pipelined kernel in flight at once: each launch
+ *     takes its own row counter from a ring of 64).
  *
  * DoF numbering (identical to the reference's, 1 rank, NRefinements = 0):
  *   cell gid = gid_x + n_cells_x * gid_v, gid_x / gid_v lexicographic over

@@ -289,3 +289,35 @@ def test_pipelined_kernel_selection_rules():
         op.set_kernel("pipelined")
     op64, _ = make(3, 3, 3, [2] * 6, [1.0] * 6, dtype="f64")
     assert op64.kernel == "generic"
+
+
+def test_pipelined_launches_on_two_streams_overlap():
+    """The pipelined kernel hands out rows from a per-launch counter (a ring of them per
+    operator): steps of two independent states launched on two streams of one operator,
+    overlapping on the device, give the bits of the same steps run one after the other."""
+    op, prob = make(3, 3, 3, [4, 3, 4, 2, 3, 4], [1.0, 0.8, 0.6, 0.4, 0.3, 0.2], dtype="f32")
+    assert op.kernel == "pipelined"
+    g = torch.Generator(device="cuda").manual_seed(5)
+    states = [torch.randn(prob.n_dofs, device="cuda", generator=g) for _ in range(2)]
+    # reference: one after the other on the current stream
+    refs = []
+    for u in states:
+        sol = u.clone()
+        integ = A.LowStorageRungeKuttaIntegrator(op.initialize_dof_vector(), op.initialize_dof_vector(), "rk45")
+        for s in range(3):
+            integ.perform_time_step(sol, s * 1e-3, 1e-3, op)
+        refs.append(sol.clone())
+    # the same steps interleaved on two streams
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    sols = [u.clone() for u in states]
+    integs = [A.LowStorageRungeKuttaIntegrator(op.initialize_dof_vector(), op.initialize_dof_vector(), "rk45")
+              for _ in states]
+    torch.cuda.synchronize()
+    for s in range(3):
+        for j in range(2):
+            with torch.cuda.stream(streams[j]):
+                integs[j].perform_time_step(sols[j], s * 1e-3, 1e-3, op)
+    torch.cuda.synchronize()
+    assert op.device_status() == 0
+    for sol, ref in zip(sols, refs):
+        assert torch.equal(sol, ref)
