@@ -532,6 +532,7 @@ def run_adv4d(args):
         sol = op.initialize_dof_vector()
         A.VectorTools.interpolate(op, f0, sol, 0.0)
         Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
+        tuned = None if args.adv4d_default_tile else op.autotune(sol, Ki, reps=2)  # outside the timed region
         integ = A.LowStorageRungeKuttaIntegrator(Ki, Ti, "rk45")
         dt = CFL * op.critical_time_step() / k4 ** 1.5
         t = 0.0
@@ -556,7 +557,7 @@ def run_adv4d(args):
         S = 4 if dtype == "f32" else 8
         res[dtype] = {"ms_per_step": round(ms, 4), "gdof_per_s": round(op.n_dofs * N_STAGES / (ms / 1e3) / 1e9, 2),
                       "hbm_gb_per_s": round(18 * S * op.n_dofs / (ms / 1e3) / 1e9, 1),
-                      "tile": op.tile_limits()}
+                      "tile": op.tile_limits(), "autotuned": tuned}
         sols[dtype] = sol.double()
         n = op.n_dofs
     l2 = float(torch.linalg.vector_norm(sols["f32"] - sols["f64"]) / torch.linalg.vector_norm(sols["f64"]))
@@ -604,6 +605,8 @@ def main():
     ap.add_argument("--workload", default="advection6d",
                     choices=["advection6d", "adv2d", "adv4d", "vp2x2v", "batch64"])
     ap.add_argument("--adv4d-degree", type=int, default=3, help="degree of the adv4d workload (default 3)")
+    ap.add_argument("--adv4d-default-tile", action="store_true",
+                    help="adv4d: keep the default tile instead of picking it with hd_adv_autotune")
     ap.add_argument("--vp-tol", type=float, default=1e-10, help="CG: ||r|| <= tol ||rhs|| (vp2x2v)")
     ap.add_argument("--vp-oracle-steps", type=int, default=2, help="steps compared with the FP64 oracle (vp2x2v)")
     ap.add_argument("--vp-runs", default="f64/previous,f64/zero,f64/learned,f64/learned5,f64x/previous,f64x/learned,"
