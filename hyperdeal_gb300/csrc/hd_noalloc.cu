@@ -31,6 +31,7 @@
 
 #include "../../include/hyperdeal_gb300.h"
 #include "hd_ecl.cuh"
+#include "hd_rules.h"
 
 namespace {
 
@@ -115,6 +116,10 @@ __global__ void noalloc_finish(double* __restrict__ scratch, int nblocks) {
   }
 }
 
+constexpr const char* kTooLarge =
+    "hd_norm_and_error_noalloc: more than 134,217,728 DoFs (its static scratch holds 16384 block partials); "
+    "use hd_norm_and_error";
+
 int noalloc_fail(int code, const char* msg) {
   hd::set_last_error(msg);
   return code;
@@ -140,49 +145,6 @@ int scratch_address(double** out) {
   return HD_OK;
 }
 
-// Gauss-Lobatto rule on [0,1] (end points + roots of P_{n-1}', Newton)
-void gauss_lobatto(int n, double* x, double* w) {
-  const int m = n - 1;
-  auto legendre = [](int nn, double z, double* p, double* dp) {
-    double p0 = 1.0, p1 = z;
-    for (int k = 2; k <= nn; ++k) {
-      const double pk = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
-      p0 = p1;
-      p1 = pk;
-    }
-    *p = nn == 0 ? 1.0 : p1;
-    *dp = nn == 0 ? 0.0 : nn * (p0 - z * p1) / (1.0 - z * z);
-  };
-  x[0] = 0.0;
-  x[n - 1] = 1.0;
-  for (int i = 1; i < m; ++i) {
-    double z = -std::cos(M_PI * i / m);
-    for (int it = 0; it < 100; ++it) {
-      double p, dp;
-      legendre(m, z, &p, &dp);
-      const double dz = dp / ((2.0 * z * dp - m * (m + 1.0) * p) / (1.0 - z * z));
-      z -= dz;
-      if (std::fabs(dz) < 1e-17) break;
-    }
-    x[i] = 0.5 * (1.0 + z);
-  }
-  for (int i = 0; i < n; ++i) {
-    double p = 1.0, dp;
-    if (i == 0) p = (m % 2) ? -1.0 : 1.0;
-    else if (i < n - 1) legendre(m, 2.0 * x[i] - 1.0, &p, &dp);
-    w[i] = 1.0 / (m * (m + 1.0) * p * p);
-  }
-  for (int i = 0; i < n / 2; ++i) {
-    const double xs = 0.5 * (x[i] + (1.0 - x[n - 1 - i]));
-    const double ws = 0.5 * (w[i] + w[n - 1 - i]);
-    x[i] = xs;
-    x[n - 1 - i] = 1.0 - xs;
-    w[i] = ws;
-    w[n - 1 - i] = ws;
-  }
-  if (n % 2) x[n / 2] = 0.5;
-}
-
 }  // namespace
 
 extern "C" int hd_norm_and_error_noalloc(const hd_adv_desc* desc, const hd_function* f, double time,
@@ -194,6 +156,8 @@ extern "C" int hd_norm_and_error_noalloc(const hd_adv_desc* desc, const hd_funct
     return noalloc_fail(HD_ERR_INVALID, "hd_norm_and_error_noalloc: unsupported descriptor");
   if (d.quadrature != HD_QUAD_GAUSS_LOBATTO)
     return noalloc_fail(HD_ERR_UNSUPPORTED, "hd_norm_and_error_noalloc: Gauss-Lobatto collocation only");
+  if (f->kind < 0 || f->kind > 2)
+    return noalloc_fail(HD_ERR_INVALID, "hd_norm_and_error_noalloc: unknown function kind");
   Geom g;
   std::memset(&g, 0, sizeof(g));
   g.D = d.dim_x + d.dim_v;
@@ -211,15 +175,15 @@ extern "C" int hd_norm_and_error_noalloc(const hd_adv_desc* desc, const hd_funct
     g.cells[i] = c;
     g.lo[i] = lo;
     g.h[i] = (hi - lo) / c;
-    ncells = ncells > kNoAllocMaxDofs ? ncells : ncells * c;  // saturates above the limit
+    // ncells <= 2^27 and c < 2^31 before the product, so it cannot overflow
+    ncells *= c;
+    if (ncells > kNoAllocMaxDofs) return noalloc_fail(HD_ERR_INVALID, kTooLarge);
     if (isx) g.ncx *= c;
   }
+  // ncells <= 2^27 and NC <= 6^6, so this product fits comfortably in 64 bits
   g.n = ncells * g.NC;
-  if (ncells > kNoAllocMaxDofs || g.n > kNoAllocMaxDofs)
-    return noalloc_fail(HD_ERR_INVALID,
-                        "hd_norm_and_error_noalloc: more than 134,217,728 DoFs (its static scratch holds "
-                        "16384 block partials); use hd_norm_and_error");
-  gauss_lobatto(g.N, g.gl, g.glw);
+  if (g.n > kNoAllocMaxDofs) return noalloc_fail(HD_ERR_INVALID, kTooLarge);
+  hd::rules::gauss_lobatto(g.N, g.gl, g.glw);
   hd::DevFunction df;
   std::memset(&df, 0, sizeof(df));
   df.kind = f->kind;

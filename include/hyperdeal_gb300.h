@@ -184,8 +184,10 @@ int hd_norm_and_error(hd_adv *op, const hd_function *f, double time, const void 
  * it takes the descriptor instead of a handle (hd_adv_create allocates) and
  * calls no cudaMalloc / cudaFree; its scratch is a fixed 256 KiB array in
  * device global memory inside the library, held by every GPU that loads the
- * library until exit.  Limit: at most 134,217,728 DoFs (larger meshes get
- * HD_ERR_INVALID; use hd_norm_and_error).  All calls share the scratch, so
+ * library until exit.  Limits: at most 134,217,728 DoFs (larger meshes get
+ * HD_ERR_INVALID; use hd_norm_and_error); Gauss-Lobatto collocation
+ * descriptors only (HD_QUAD_GAUSS gets HD_ERR_UNSUPPORTED); function kinds
+ * 0..2 (others get HD_ERR_INVALID).  All calls share the scratch, so
  * calls whose kernels overlap on the GPU race: serialise them.  The first call
  * on a device looks up the scratch address for that device (make it before
  * any stream capture).  Synchronises `stream`; result is host memory. */

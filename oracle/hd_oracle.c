@@ -701,6 +701,36 @@ int hdo_velocity_moment(const hdo_problem *p, const double *src, double *rho) {
   return 0;
 }
 
+/* numerics/vector_tools.h:317-400 (coordinate_space_integration): the
+ * x-space counterpart of the velocity moment, one v-DoF at a time: the raw
+ * DoF values times the x-space JxW of the Gauss-Lobatto points (quad_no_x = 2
+ * in the reference's tests), summed over every x-cell */
+int hdo_coordinate_moment(const hdo_problem *p, const double *src, double *out) {
+  ctx_t c;
+  if (make_ctx(p, &c)) return -1;
+  int nx = 1, nv = 1;
+  for (int d = 0; d < c.dx; ++d) nx *= c.n;
+  for (int d = c.dx; d < c.D; ++d) nv *= c.n;
+  double jx = 1.0;
+  for (int d = 0; d < c.dx; ++d) jx *= c.h[d];
+#pragma omp parallel for schedule(static)
+  for (long long gv = 0; gv < c.ncv; ++gv)
+    for (int iv = 0; iv < nv; ++iv) {
+      double acc = 0.0;
+      for (long long gx = 0; gx < c.ncx; ++gx) {
+        const double *u = src + (gx + c.ncx * gv) * c.NC;
+        for (int ix = 0; ix < nx; ++ix) {
+          double w = jx;
+          int t = ix;
+          for (int d = 0; d < c.dx; ++d) { w *= c.glw[t % c.n]; t /= c.n; }
+          acc += u[ix + nx * iv] * w;
+        }
+      }
+      out[gv * nv + iv] = acc;
+    }
+  return 0;
+}
+
 /* x-space view of a phase-space context */
 typedef struct {
   int dx, n, NCx;

@@ -130,6 +130,11 @@ double hdo_critical_time_step(const hdo_problem *p);
  * removal): rho[x_dof] = sum over v-cells and v-nodes of f * JxW_v        */
 int hdo_velocity_moment(const hdo_problem *p, const double *src, double *rho);
 
+/* coordinate-moment of f over x for every v-DoF: out[v_dof] = sum over
+ * x-cells and x-nodes of f * JxW_x at the Gauss-Lobatto points
+ * (numerics/vector_tools.h:317-400, coordinate_space_integration) */
+int hdo_coordinate_moment(const hdo_problem *p, const double *src, double *out);
+
 /* SIPG Laplacian on the x-mesh (src mean removed first), its right-hand
  * side from rho, CG (phi: initial guess in, solution out), the potential
  * gradient at the x-quadrature points, one full Vlasov-Poisson operator

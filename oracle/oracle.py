@@ -158,6 +158,7 @@ def lib():
         L.hdo_gauss.argtypes = [ctypes.c_int, dp, dp]
         L.hdo_lsrk_coefficients.argtypes = [ctypes.c_char_p, dp, dp]
         L.hdo_velocity_moment.argtypes = [P, dp, dp]
+        L.hdo_coordinate_moment.argtypes = [P, dp, dp]
         L.hdo_n_dofs.argtypes = [P]
         L.hdo_n_dofs.restype = ctypes.c_longlong
         L.hdo_poisson_apply.argtypes = [P, dp, dp]
@@ -270,6 +271,35 @@ def velocity_moment(p: Problem, src: np.ndarray) -> np.ndarray:
     cp = p.c()
     _check(lib().hdo_velocity_moment(ctypes.byref(cp), _ptr(src), _ptr(rho)), "velocity_moment")
     return rho
+
+
+def coordinate_moment(p: Problem, src: np.ndarray) -> np.ndarray:
+    """The integral over x of f at every v-DoF (vector_tools.h:317-400)."""
+    nv = int(np.prod(p.cells[p.dim_x:])) * (p.degree + 1) ** p.dim_v
+    out = np.zeros(nv)
+    cp = p.c()
+    _check(lib().hdo_coordinate_moment(ctypes.byref(cp), _ptr(src), _ptr(out)), "coordinate_moment")
+    return out
+
+
+def node_coordinates(p: Problem) -> np.ndarray:
+    """Coordinates (n_dofs x dim) of the Gauss-Lobatto support points in the DoF order: cell gid =
+    gid_x + n_cells_x gid_v with lexicographic x- and v-cells, nodes lexicographic inside a cell
+    (matrix_free.templates.h:535-563, shape_info.h:141-160)."""
+    n = p.degree + 1
+    D = p.dim
+    xi, _ = gauss_lobatto(n)
+    cells = [int(c) for c in p.cells]
+    h = [(p.hi[d] - p.lo[d]) / cells[d] for d in range(D)]
+    # cell coordinates: x-cells (first direction fastest), then v-cells
+    cell_axes = np.meshgrid(*[np.arange(c) for c in reversed(cells)], indexing="ij")
+    cc = [a.reshape(-1) for a in reversed(cell_axes)]  # cc[d][gid]
+    node_axes = np.meshgrid(*[np.arange(n)] * D, indexing="ij")
+    nn = [a.reshape(-1) for a in reversed(node_axes)]  # nn[d][node]
+    out = np.empty((len(cc[0]) * n ** D, D))
+    for d in range(D):
+        out[:, d] = (p.lo[d] + (cc[d][:, None] + xi[nn[d]][None, :]) * h[d]).reshape(-1)
+    return out
 
 
 def gauss_lobatto(n: int):

@@ -12,6 +12,14 @@ Sources (paths relative to the reference root):
   tests/time_discretization/time_integrators_01.output  -- stage counts
   tests/time_discretization/time_integrators_02.mpirun=1.output -- rk45 KAT
   tests/vector_tools/vector_tools_01.mpirun=1.output   -- interpolate + L2
+  tests/vector_tools/vector_tools_02.mpirun=1.output   -- ordered dumps of the
+      v-integrated x-vector and the x-integrated v-vector, 1+1D k=3, 2..5
+      refinements of [0,1], functions 0, 1, sin(pi x) cos(pi v)
+  tests/vector_tools/vector_tools_03.mpirun=1.output   -- the same for 2+2D k=3,
+      3 refinements of [-1,1], max(0, 0.5 - |p|)
+  tests/matrix_free/fefaceevalutation_02.mpirun=1.output -- the face-trace
+      property (trace of f = x_dir equals the face-point coordinate) and the
+      (dim_x, dim_v, dir, loop, face) combinations it passed for
 The fixture holds numbers and run parameters only.
 """
 import glob
@@ -76,6 +84,35 @@ def main(root):
         vals = re.findall(NUM, line.split("::", 1)[1]) if "::" in line else []
         if len(vals) == 2:
             vt01.append([float(v) for v in vals])
+    # ordered vector dumps ("Vector data:" followed by one line of values)
+    def vector_dumps(path):
+        lines = open(path).read().splitlines()
+        out = []
+        for i, line in enumerate(lines):
+            if line.strip() == "Vector data:":
+                out.append([float(v) for v in lines[i + 1].split()])
+        return out
+
+    vt02_all = vector_dumps(os.path.join(root, "tests", "vector_tools", "vector_tools_02.mpirun=1.output"))
+    # vector_tools_02.cc:99-129, :139-146: for refs 2..5, for f in (0, 1, sin(pi x) cos(pi v)): vec_x, vec_v
+    vt02 = []
+    k = 0
+    for refs in range(2, 6):
+        for fname in ("zero", "one", "sin_cos"):
+            vt02.append({"refinements": refs, "function": fname, "vec_x": vt02_all[k], "vec_v": vt02_all[k + 1]})
+            k += 2
+    assert k == len(vt02_all)
+    vt03_all = vector_dumps(os.path.join(root, "tests", "vector_tools", "vector_tools_03.mpirun=1.output"))
+    assert len(vt03_all) == 2
+    vt03 = {"dim_x": 2, "dim_v": 2, "degree": 3, "refinements": 3, "lo": -1.0, "hi": 1.0,
+            "function": "max(0, 0.5 - |p|)", "vec_x": vt03_all[0], "vec_v": vt03_all[1]}
+    ff02 = []
+    for line in open(os.path.join(root, "tests", "matrix_free", "fefaceevalutation_02.mpirun=1.output")):
+        m = re.match(r"DEAL:0:dim_x=(\d):(\d):dir=(\d):(FCL|ECL):dir=(\d+)::(.*)$", line.strip())
+        if m:
+            ff02.append([int(m.group(1)), int(m.group(2)), int(m.group(3)), m.group(4), int(m.group(5)),
+                         "succeeded" in m.group(6)])
+
     vp = []
     vp_dir = os.path.join(root, "examples", "vlasov_poisson", "tests")
     for jpath in sorted(glob.glob(os.path.join(vp_dir, "*.json"))):
@@ -103,6 +140,10 @@ def main(root):
         "time_integrators_01_stages": ti01,
         "time_integrators_02_rk45_values": ti02,
         "vector_tools_01_rows": vt01,
+        "vector_tools_02": vt02,
+        "vector_tools_03": vt03,
+        "fefaceevalutation_02": {"columns": "dim_x, dim_v, dir (of f = x_dir), loop, face, succeeded",
+                                 "rows": ff02},
     }
     with open(os.path.join(here, "reference_goldens.json"), "w") as f:
         json.dump(out, f, indent=1)
@@ -110,4 +151,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_goldens.py <root of the hyper.deal tree>")
+    main(sys.argv[1])

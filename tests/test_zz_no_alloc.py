@@ -65,3 +65,42 @@ def test_noalloc_rejects_meshes_above_its_scratch():
     rc = L.hd_norm_and_error_noalloc(ctypes.byref(desc), ctypes.byref(fc), 0.0, ctypes.c_void_p(256), out, None)
     assert rc == _lib.HD_ERR_INVALID
     assert "134,217,728" in _lib.last_error()
+
+
+def test_noalloc_at_its_size_limit():
+    """134,217,728 DoFs exactly (3x+3v, k=3, 32,768 cells): 16,384 block partials, the whole scratch."""
+    params, f = _case(3, 3, [8, 8, 8, 8, 8, 2], "f32")
+    op = A.AdvectionOperation(params)
+    assert op.n_dofs == 134217728
+    v = op.initialize_dof_vector()
+    A.VectorTools.interpolate(op, f, v, 0.0)
+    ref = A.VectorTools.norm_and_error(op, f, v, 0.1)
+    L = _lib.load()
+    desc, fc = params.c(), f.c()
+    out = (ctypes.c_double * 2)(-1.0, -1.0)
+    rc = L.hd_norm_and_error_noalloc(ctypes.byref(desc), ctypes.byref(fc), 0.1, ctypes.c_void_p(v.data_ptr()), out,
+                                     ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0, _lib.last_error()
+    assert abs(out[0] - ref[0]) <= REL_TOL * abs(ref[0])
+    assert abs(out[1] - ref[1]) <= 1e-9 * abs(ref[0])  # the error is FP32 round-off: compare on the norm's scale
+    del op, v
+    torch.cuda.empty_cache()
+
+
+def test_noalloc_rejects_gauss_descriptors_and_unknown_functions():
+    """Both are refused on the host, before any device work."""
+    L = _lib.load()
+    out = (ctypes.c_double * 2)()
+    params, f = _case(2, 2, [2, 2, 2, 2], "f64")
+    desc = params.c()
+    desc.quadrature = 1  # HD_QUAD_GAUSS
+    fc = f.c()
+    rc = L.hd_norm_and_error_noalloc(ctypes.byref(desc), ctypes.byref(fc), 0.0, ctypes.c_void_p(256), out, None)
+    assert rc == _lib.HD_ERR_UNSUPPORTED
+    assert "Gauss-Lobatto" in _lib.last_error()
+    desc = params.c()
+    fc = f.c()
+    fc.kind = 7
+    rc = L.hd_norm_and_error_noalloc(ctypes.byref(desc), ctypes.byref(fc), 0.0, ctypes.c_void_p(256), out, None)
+    assert rc == _lib.HD_ERR_INVALID
+    assert "kind" in _lib.last_error()
