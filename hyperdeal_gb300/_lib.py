@@ -29,10 +29,13 @@ EXPORTED_SYMBOLS = (
     "hd_batch_apply", "hd_batch_lsrk_step", "hd_batch_graph_capture", "hd_batch_graph_launch", "hd_batch_autotune",
     "hd_adv_autotune", "hd_vp_lsrk_step_fused", "hd_adv_set_arithmetic", "hd_adv_arithmetic",
     "hd_batch_class_arithmetic", "hd_vp_set_arithmetic",
+    "hd_part_layout_get", "hd_adv_create_part", "hd_adv_part_layout", "hd_adv_pack_faces", "hd_adv_apply_cells",
+    "hd_lsrk_stage", "hd_lsrk_stage_input",
 )
 HD_KERNEL_AUTO, HD_KERNEL_GENERIC, HD_KERNEL_PIPELINED = 0, 1, 2
 HD_ARITH_NATIVE, HD_ARITH_FP32X2 = 0, 1
 HD_VP_GUESS_ZERO, HD_VP_GUESS_PREVIOUS, HD_VP_GUESS_LEARNED = 0, 1, 2
+HD_CELLS_ALL, HD_CELLS_INTERIOR, HD_CELLS_BOUNDARY = 0, 1, 2
 
 
 class HdError(RuntimeError):
@@ -66,6 +69,17 @@ class hd_vp_desc(ctypes.Structure):
                 ("cg_tol", ctypes.c_double), ("cg_max_iter", ctypes.c_int), ("guess", ctypes.c_int),
                 ("learn_rank", ctypes.c_int), ("learn_history", ctypes.c_int), ("cg_rhs_relative", ctypes.c_int),
                 ("learn_every", ctypes.c_int)]
+
+
+class hd_part_layout(ctypes.Structure):
+    _fields_ = [("first_cell", ctypes.c_longlong), ("n_cells", ctypes.c_longlong),
+                ("layer_cells", ctypes.c_longlong), ("face_values", ctypes.c_longlong),
+                ("ghost_values", ctypes.c_longlong), ("recv_from", ctypes.c_int), ("send_to", ctypes.c_int),
+                ("send_first_cell", ctypes.c_longlong), ("send_slab", ctypes.c_int),
+                ("boundary_first", ctypes.c_longlong), ("boundary_cells", ctypes.c_longlong)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 
 _lib = None
@@ -152,6 +166,14 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.hd_batch_graph_capture.argtypes = [vp, vpp, vpp, vpp, dp, dp]
     L.hd_batch_graph_launch.argtypes = [vp, vp]
     L.hd_batch_autotune.argtypes = [vp, vpp, vpp, ctypes.c_int, vp]
+    L.hd_part_layout_get.argtypes = [ctypes.POINTER(hd_adv_desc), ctypes.c_int, ctypes.c_int,
+                                     ctypes.POINTER(hd_part_layout)]
+    L.hd_adv_create_part.argtypes = [ctypes.POINTER(hd_adv_desc), ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
+    L.hd_adv_part_layout.argtypes = [vp, ctypes.POINTER(hd_part_layout)]
+    L.hd_adv_pack_faces.argtypes = [vp, vp, vp, vp]
+    L.hd_adv_apply_cells.argtypes = [vp, vp, vp, ctypes.c_double, ctypes.c_int, vp]
+    L.hd_lsrk_stage.argtypes = [vp, vp, ctypes.c_int, vpp, ctypes.c_double, ctypes.c_double, ctypes.c_int, vp]
+    L.hd_lsrk_stage_input.argtypes = [vp, ctypes.c_int]
     _lib = L
     return L
 

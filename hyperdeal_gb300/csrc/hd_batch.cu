@@ -227,6 +227,10 @@ int hd_batch_create(hd_adv* const* ops, int n, const hd_lsrk* rk, hd_batch** out
   b->graph_ready = false;
   for (int i = 0; i < n; ++i) {
     if (!ops[i]) { batch_free(b); return bfail(HD_ERR_INVALID, "hd_batch_create: null operator"); }
+    if (ops[i]->n_parts > 1) {
+      batch_free(b);
+      return bfail(HD_ERR_UNSUPPORTED, "hd_batch_create: parts of a partitioned operator are not batched");
+    }
     b->ops.push_back(ops[i]);
   }
   for (int i = 0; i < n; ++i) {

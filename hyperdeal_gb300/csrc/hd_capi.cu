@@ -256,6 +256,11 @@ void fill_params(const hd_adv* op, hd::EclParams<T>* P) {
     }
   }
   if (op->D < hd::kMaxDim) P->cstride[op->D] = st;
+  P->gid0 = op->part.first_cell;
+  P->c_lo = 0;
+  P->c_hi = op->n_cells;
+  P->layer = op->part.layer_cells;
+  P->ghost = nullptr;
   for (int i = 0; i < op->N; ++i) P->gl[i] = op->gl[i];
   P->bc_inhom = op->desc.bc_kind == HD_BC_FUNCTION;
   P->bc = to_dev(op->desc.bc);
@@ -279,9 +284,37 @@ int selected_kernel(const hd_adv* op) {
   return pipelined_ok ? HD_KERNEL_PIPELINED : HD_KERNEL_GENERIC;
 }
 
+// local cells [lo, hi) of a cell subset (enum hd_cells); the boundary cells of
+// a part are one layer at one end of its range, so both subsets are ranges
+void cell_range(const hd_adv* op, int which, long long* lo, long long* hi) {
+  const hd_part_layout& L = op->part;
+  *lo = 0;
+  *hi = op->n_cells;
+  if (which == HD_CELLS_BOUNDARY) {
+    *lo = L.boundary_first;
+    *hi = L.boundary_first + L.boundary_cells;
+  } else if (which == HD_CELLS_INTERIOR && L.boundary_cells > 0) {
+    if (L.boundary_first == 0) *lo = L.boundary_cells;
+    else *hi = L.boundary_first;
+  }
+}
+
+template <typename T>
+void set_launch(const hd_adv* op, hd::EclParams<T>* P, const void* tin, const void* uin, void* uout, void* tout,
+                double fb, double fa, double time, long long c_lo, long long c_hi) {
+  P->tin = (const T*)tin; P->uin = (const T*)uin; P->uout = (T*)uout; P->tout = (T*)tout;
+  P->fb = T(fb); P->fa = T(fa); P->time = time;
+  P->c_lo = c_lo; P->c_hi = c_hi;
+  // the ghost region follows the part's cells in the operator input
+  P->ghost = op->part.ghost_values > 0 ? (const T*)tin + op->n_dofs : nullptr;
+}
+
 int launch(hd_adv* op, int mode, const void* tin, const void* uin, void* uout, void* tout, double fb,
-           double fa, double time, cudaStream_t s) {
+           double fa, double time, cudaStream_t s, int which = HD_CELLS_ALL) {
   cudaError_t e;
+  long long c_lo = 0, c_hi = 0;
+  cell_range(op, which, &c_lo, &c_hi);
+  if (c_hi <= c_lo) return HD_OK;  // an empty subset: nothing to launch
   if (op->gauss) {
     if (op->dtype == HD_F64) {
       hd::EclParams<double> P = op->p64;
@@ -296,19 +329,16 @@ int launch(hd_adv* op, int mode, const void* tin, const void* uin, void* uout, v
     }
   } else if (selected_kernel(op) == HD_KERNEL_PIPELINED) {
     hd::EclParams<float> P = op->p32;
-    P.tin = (const float*)tin; P.uin = (const float*)uin; P.uout = (float*)uout; P.tout = (float*)tout;
-    P.fb = float(fb); P.fa = float(fa); P.time = time;
+    set_launch(op, &P, tin, uin, uout, tout, fb, fa, time, c_lo, c_hi);
     int* ticket = op->d_tickets + (op->ticket_slot++ % hd::kTicketSlots);
     e = hd::launch_ecl6(P, op->d_err, ticket, mode, s);
   } else if (op->dtype == HD_F64) {
     hd::EclParams<double> P = op->p64;
-    P.tin = (const double*)tin; P.uin = (const double*)uin; P.uout = (double*)uout; P.tout = (double*)tout;
-    P.fb = fb; P.fa = fa; P.time = time;
+    set_launch(op, &P, tin, uin, uout, tout, fb, fa, time, c_lo, c_hi);
     e = (op->arith == HD_ARITH_FP32X2 ? op->launchers.f64x : op->launchers.f64)(P, mode, s);
   } else {
     hd::EclParams<float> P = op->p32;
-    P.tin = (const float*)tin; P.uin = (const float*)uin; P.uout = (float*)uout; P.tout = (float*)tout;
-    P.fb = float(fb); P.fa = float(fa); P.time = time;
+    set_launch(op, &P, tin, uin, uout, tout, fb, fa, time, c_lo, c_hi);
     e = op->launchers.f32(P, mode, s);
   }
   if (e != cudaSuccess) return cuda_fail(e, "ECL kernel launch");
@@ -316,6 +346,53 @@ int launch(hd_adv* op, int mode, const void* tin, const void* uin, void* uout, v
 }
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// Part `part` of n_parts v-slabs: whole layers of the last direction (D-1).
+// `last` is the line operator of that direction: only its upwind side is read,
+// so a part receives the faces of one layer of its upwind part and sends one
+// layer to its downwind part (with wraps on a periodic direction).
+int compute_layout(int D, int N, const int* cells, const LineOpD& last, int periodic_last, int n_parts, int part,
+                   hd_part_layout* L) {
+  const int lc = cells[D - 1];
+  if (n_parts < 1 || n_parts > lc || part < 0 || part >= n_parts)
+    return fail(HD_ERR_INVALID, "partition: need 1 <= n_parts <= %d (cells in the last direction), 0 <= part < "
+                                "n_parts (got %d, %d)", lc, n_parts, part);
+  long long ncells = 1;
+  for (int d = 0; d < D; ++d) ncells *= cells[d];
+  const long long layer = ncells / lc;
+  const long long l0 = (long long)part * lc / n_parts, l1 = (long long)(part + 1) * lc / n_parts;
+  std::memset(L, 0, sizeof(*L));
+  L->first_cell = l0 * layer;
+  L->n_cells = (l1 - l0) * layer;
+  L->layer_cells = layer;
+  L->face_values = hd::ipow(N, D - 1);
+  L->recv_from = -1;
+  L->send_to = -1;
+  if (n_parts > 1 && last.active) {
+    int up, down;
+    if (last.step < 0) {  // upwind neighbour at the lower layer
+      up = part - 1;
+      down = part + 1;
+      L->boundary_first = 0;
+      L->send_first_cell = L->n_cells - layer;
+    } else {
+      up = part + 1;
+      down = part - 1;
+      L->boundary_first = L->n_cells - layer;
+      L->send_first_cell = 0;
+    }
+    if (up < 0 || up >= n_parts) up = periodic_last ? (up + n_parts) % n_parts : -1;
+    if (down < 0 || down >= n_parts) down = periodic_last ? (down + n_parts) % n_parts : -1;
+    L->recv_from = up;
+    L->send_to = down;
+    L->send_slab = last.nb_node;
+    if (up >= 0) {
+      L->ghost_values = layer * L->face_values;
+      L->boundary_cells = layer;
+    }
+  }
+  return HD_OK;
+}
 
 }  // namespace
 
@@ -339,10 +416,11 @@ int hd_last_error(char* buf, size_t len) {
 
 const char* hd_version(void) { return "hyperdeal_gb300 0.1 (sm_103a)"; }
 
-int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
+static int create_impl(const hd_adv_desc* desc, int n_parts, int part, bool layout_only, hd_adv** out,
+                       hd_part_layout* layout_out) {
   try {
-    if (!desc || !out) return fail(HD_ERR_INVALID, "hd_adv_create: null argument");
-    *out = nullptr;
+    if (!desc || (!out && !layout_out)) return fail(HD_ERR_INVALID, "hd_adv_create: null argument");
+    if (out) *out = nullptr;
     const hd_adv_desc& d = *desc;
     if (d.dim_x < 1 || d.dim_x > 3 || d.dim_v < 1 || d.dim_v > 3)
       return fail(HD_ERR_INVALID, "dim_x and dim_v must be in 1..3 (got %d, %d)", d.dim_x, d.dim_v);
@@ -357,6 +435,8 @@ int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
     if (d.bc_kind != HD_BC_HOMOGENEOUS && d.bc_kind != HD_BC_FUNCTION)
       return fail(HD_ERR_INVALID, "unknown bc_kind %d", d.bc_kind);
     if (!std::isfinite(d.skew)) return fail(HD_ERR_INVALID, "skew factor is not finite");
+    if (n_parts > 1 && d.quadrature != HD_QUAD_GAUSS_LOBATTO)
+      return fail(HD_ERR_UNSUPPORTED, "partitioned operators use Gauss-Lobatto collocation");
     hd_adv* op = new (std::nothrow) hd_adv;
     if (!op) return fail(HD_ERR_ALLOC, "out of host memory");
     std::memset(op, 0, sizeof(*op));
@@ -387,7 +467,6 @@ int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
       op->n_cells *= c;
       if (isx) op->ncx *= c;
     }
-    op->n_dofs = op->n_cells * op->NC;
     gauss_lobatto(op->N, op->gl, op->glw);
     lagrange_derivative_matrix(op->N, op->gl, op->Dm);
     op->gauss = d.quadrature == HD_QUAD_GAUSS;
@@ -436,6 +515,20 @@ int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
           return fail(HD_ERR_UNSUPPORTED, "direction %d: flux is not one-sided upwind", i);
         }
     }
+    {
+      const int rc = compute_layout(op->D, op->N, op->cells, op->ops[op->D - 1], op->periodic[op->D - 1], n_parts,
+                                    part, &op->part);
+      if (rc) { delete op; return rc; }
+      op->n_parts = n_parts;
+      op->part_index = part;
+      op->n_cells = op->part.n_cells;  // the cells of this part (all of them for n_parts = 1)
+      op->n_dofs = op->n_cells * op->NC;
+    }
+    if (layout_only) {
+      *layout_out = op->part;
+      delete op;
+      return HD_OK;
+    }
     op->launchers = get_launchers(op->D, op->N);
     const bool ok = d.dtype == HD_F64 ? op->launchers.ok_f64 : op->launchers.ok_f32;
     if (!op->launchers.f64 || !ok) {
@@ -448,6 +541,7 @@ int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
     hd::VecGeom& g = op->geom;
     std::memset(&g, 0, sizeof(g));
     g.D = op->D; g.dim_x = d.dim_x; g.N = op->N; g.NC = op->NC; g.ncx = op->ncx; g.n_dofs = op->n_dofs;
+    g.gid0 = op->part.first_cell;
     for (int i = 0; i < op->D; ++i) { g.cells[i] = op->cells[i]; g.lo[i] = op->lo[i]; g.h[i] = op->h[i]; }
     for (int i = 0; i < op->N; ++i) { g.gl[i] = op->gl[i]; g.glw[i] = op->glw[i]; }
     g.gauss = op->gauss;
@@ -479,6 +573,51 @@ int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
   } catch (...) {
     return fail(HD_ERR_INVALID, "hd_adv_create: unexpected exception");
   }
+}
+
+int hd_adv_create(const hd_adv_desc* desc, hd_adv** out) {
+  if (!out) return fail(HD_ERR_INVALID, "hd_adv_create: null argument");
+  return create_impl(desc, 1, 0, false, out, nullptr);
+}
+
+int hd_adv_create_part(const hd_adv_desc* desc, int n_parts, int part, hd_adv** out) {
+  if (!out) return fail(HD_ERR_INVALID, "hd_adv_create_part: null argument");
+  return create_impl(desc, n_parts, part, false, out, nullptr);
+}
+
+int hd_part_layout_get(const hd_adv_desc* desc, int n_parts, int part, hd_part_layout* out) {
+  if (!out) return fail(HD_ERR_INVALID, "hd_part_layout_get: null argument");
+  return create_impl(desc, n_parts, part, true, nullptr, out);
+}
+
+int hd_adv_part_layout(const hd_adv* op, hd_part_layout* out) {
+  if (!op || !out) return fail(HD_ERR_INVALID, "hd_adv_part_layout: null argument");
+  *out = op->part;
+  return HD_OK;
+}
+
+int hd_adv_pack_faces(hd_adv* op, const void* vec, void* sendbuf, void* stream) {
+  if (!op || !vec || !sendbuf) return fail(HD_ERR_INVALID, "hd_adv_pack_faces: null argument");
+  const hd_part_layout& L = op->part;
+  if (L.send_to < 0) return HD_OK;  // nobody reads this part's faces
+  const int sz = op->dtype == HD_F64 ? 8 : 4;
+  const char* src = (const char*)vec + (L.send_first_cell * op->NC + (long long)L.send_slab * L.face_values) * sz;
+  cudaError_t e = hd::launch_pack_faces(src, op->NC * sz, L.face_values * sz, L.layer_cells, sendbuf,
+                                        (cudaStream_t)stream);
+  return e == cudaSuccess ? HD_OK : cuda_fail(e, "face pack kernel");
+}
+
+int hd_adv_apply_cells(hd_adv* op, void* dst, const void* src, double time, int cells, void* stream) {
+  if (!op || !dst || !src) return fail(HD_ERR_INVALID, "hd_adv_apply: null argument");
+  if (cells != HD_CELLS_ALL && cells != HD_CELLS_INTERIOR && cells != HD_CELLS_BOUNDARY)
+    return fail(HD_ERR_INVALID, "hd_adv_apply_cells: unknown cell subset %d", cells);
+  if (!aligned16(dst) || !aligned16(src)) return fail(HD_ERR_INVALID, "hd_adv_apply: vectors must be 16-byte aligned");
+  const size_t sz = op->dtype == HD_F64 ? 8 : 4;
+  const size_t bytes = size_t(op->n_dofs + op->part.ghost_values) * sz;
+  const char* a = (const char*)src;
+  const char* b = (const char*)dst;
+  if (a < b + bytes && b < a + bytes) return fail(HD_ERR_INVALID, "hd_adv_apply: dst and src overlap");
+  return launch(op, hd::kApply, src, src, dst, nullptr, 0.0, 0.0, time, (cudaStream_t)stream, cells);
 }
 
 int hd_adv_destroy(hd_adv* op) {
@@ -600,13 +739,7 @@ double hd_adv_critical_time_step(const hd_adv* op) {
 }
 
 int hd_adv_apply(hd_adv* op, void* dst, const void* src, double time, void* stream) {
-  if (!op || !dst || !src) return fail(HD_ERR_INVALID, "hd_adv_apply: null argument");
-  if (!aligned16(dst) || !aligned16(src)) return fail(HD_ERR_INVALID, "hd_adv_apply: vectors must be 16-byte aligned");
-  const size_t bytes = size_t(op->n_dofs) * (op->dtype == HD_F64 ? 8 : 4);
-  const char* a = (const char*)src;
-  const char* b = (const char*)dst;
-  if (a < b + bytes && b < a + bytes) return fail(HD_ERR_INVALID, "hd_adv_apply: dst and src overlap");
-  return launch(op, hd::kApply, src, src, dst, nullptr, 0.0, 0.0, time, (cudaStream_t)stream);
+  return hd_adv_apply_cells(op, dst, src, time, HD_CELLS_ALL, stream);
 }
 
 int hd_interpolate(hd_adv* op, const hd_function* f, double time, void* dst, void* stream) {
@@ -699,39 +832,50 @@ int hd_lsrk_coefficients(const hd_lsrk* rk, double* ai, double* bi, double* ci) 
   return HD_OK;
 }
 
+// Buffer rotation of the fused step (X0 = sol, X1 = Ki, X2 = Ti as passed):
+// X0 holds U and the first stage input; the new solution accumulates in X1;
+// the stage inputs alternate between X0 (even stages) and X2 (odd stages),
+// each stage writing the next input into the other one.
+int hd_lsrk_stage_input(const hd_lsrk* rk, int stage) {
+  if (!rk || stage < 0 || stage >= rk->ns) return -1;
+  return (stage % 2) ? 2 : 0;
+}
+
+int hd_lsrk_stage(hd_adv* op, const hd_lsrk* rk, int stage, void* const* X, double time, double dt, int cells,
+                  void* stream) {
+  if (!op || !rk || !X || !X[0] || !X[1] || !X[2]) return fail(HD_ERR_INVALID, "hd_lsrk_stage: null argument");
+  if (stage < 0 || stage >= rk->ns) return fail(HD_ERR_INVALID, "hd_lsrk_stage: stage %d of %d", stage, rk->ns);
+  if (cells != HD_CELLS_ALL && cells != HD_CELLS_INTERIOR && cells != HD_CELLS_BOUNDARY)
+    return fail(HD_ERR_INVALID, "hd_lsrk_stage: unknown cell subset %d", cells);
+  if (X[0] == X[1] || X[0] == X[2] || X[1] == X[2]) return fail(HD_ERR_INVALID, "hd_lsrk_stage: vectors must differ");
+  if (!aligned16(X[0]) || !aligned16(X[1]) || !aligned16(X[2]))
+    return fail(HD_ERR_INVALID, "hd_lsrk_stage: vectors must be 16-byte aligned");
+  const bool last = stage == rk->ns - 1;
+  const double fb = rk->bi[stage] * dt;
+  const double fa = last ? 0.0 : rk->ai[stage] * dt;
+  const double t_s = time + rk->ci[stage] * dt;
+  int mode = stage == 0 ? hd::kStageFirst : (last ? hd::kStageLast : hd::kStageMid);
+  if (stage == 0 && last) mode = hd::kStageFirst;  // single-stage schemes are not built
+  void* t_in = X[hd_lsrk_stage_input(rk, stage)];
+  void* t_out = last ? nullptr : X[(stage % 2) ? 0 : 2];
+  return launch(op, mode, t_in, stage == 0 ? t_in : X[1], X[1], t_out, fb, fa, t_s, (cudaStream_t)stream, cells);
+}
+
 int hd_lsrk_step(hd_adv* op, const hd_lsrk* rk, void** sol, void** Ki, void** Ti, double time, double dt,
                  void* stream) {
   if (!op || !rk || !sol || !Ki || !Ti || !*sol || !*Ki || !*Ti)
     return fail(HD_ERR_INVALID, "hd_lsrk_step: null argument");
-  if (*sol == *Ki || *sol == *Ti || *Ki == *Ti) return fail(HD_ERR_INVALID, "hd_lsrk_step: vectors must differ");
-  if (!aligned16(*sol) || !aligned16(*Ki) || !aligned16(*Ti))
-    return fail(HD_ERR_INVALID, "hd_lsrk_step: vectors must be 16-byte aligned");
-  cudaStream_t s = (cudaStream_t)stream;
-  // buffer rotation: X0 holds U and T_1; the new solution accumulates in X1;
-  // the stage inputs alternate between X2 and X0
-  void* X0 = *sol;
-  void* X1 = *Ki;
-  void* X2 = *Ti;
-  void* t_in = X0;
-  void* t_free = X2;
+  if (op->part.ghost_values > 0)
+    return fail(HD_ERR_UNSUPPORTED, "hd_lsrk_step: a part with ghost faces steps with hd_lsrk_stage and an "
+                                    "exchange of the stage input's faces before every stage");
+  void* X[3] = {*sol, *Ki, *Ti};
   for (int st = 0; st < rk->ns; ++st) {
-    const double fb = rk->bi[st] * dt;
-    const bool last = st == rk->ns - 1;
-    const double fa = last ? 0.0 : rk->ai[st] * dt;
-    const double t_s = time + rk->ci[st] * dt;
-    int mode = st == 0 ? hd::kStageFirst : (last ? hd::kStageLast : hd::kStageMid);
-    if (st == 0 && last) mode = hd::kStageFirst;  // single-stage schemes are not built
-    const int rc = launch(op, mode, t_in, st == 0 ? t_in : X1, X1, last ? nullptr : t_free, fb, fa, t_s, s);
+    const int rc = hd_lsrk_stage(op, rk, st, X, time, dt, HD_CELLS_ALL, stream);
     if (rc) return rc;
-    if (!last) {
-      void* next = t_free;
-      t_free = (st == 0) ? X0 : t_in;
-      t_in = next;
-    }
   }
-  *sol = X1;
-  *Ki = X0;
-  *Ti = X2;
+  *sol = X[1];
+  *Ki = X[0];
+  *Ti = X[2];
   return HD_OK;
 }
 
@@ -747,6 +891,8 @@ int hd_lsrk_stage_update(int dtype, long long n, double factor_bi, double factor
 int hd_lsrk_step_unfused(hd_adv* op, const hd_lsrk* rk, void* sol, void* Ki, void* Ti, double time, double dt,
                          void* stream) {
   if (!op || !rk || !sol || !Ki || !Ti) return fail(HD_ERR_INVALID, "hd_lsrk_step_unfused: null argument");
+  if (op->part.ghost_values > 0)
+    return fail(HD_ERR_UNSUPPORTED, "hd_lsrk_step_unfused: a part with ghost faces needs an exchange per stage");
   cudaStream_t s = (cudaStream_t)stream;
   const size_t bytes = size_t(op->n_dofs) * (op->dtype == HD_F64 ? 8 : 4);
   // first stage with only_Ti_is_ghosted = true: Ti = sol (time_integrators.templates.h:142-148)

@@ -75,6 +75,16 @@ struct EclParams {
   double gl[kMaxN];  // Gauss-Lobatto nodes on [0,1]
   int cpb;           // generic kernel tile: cells per CTA (0 = the shape's maximum)
   int ctas_per_sm;   //   and CTAs per SM of the persistent grid (0 = occupancy limit)
+  // Partitioned operators (hd_adv_create_part): the vectors hold the cells
+  // [gid0, gid0 + n_cells) of the global mesh -- whole layers of the last
+  // direction -- and cells/cstride above describe the global mesh.  A launch
+  // processes the local cells [c_lo, c_hi).  The upwind faces of cells owned
+  // by another part (only across the last direction) are read from `ghost`:
+  // one face of NC/N values per cell of a layer, in the cells' in-layer order
+  // (layer = cells per layer).  Unpartitioned: gid0 = 0, c_lo = 0,
+  // c_hi = n_cells, ghost = nullptr.
+  long long gid0, c_lo, c_hi, layer;
+  const T* ghost;
 };
 
 enum EclMode { kApply = 0, kStageFirst = 1, kStageMid = 2, kStageLast = 3 };
@@ -177,6 +187,31 @@ __device__ __forceinline__ long long neighbour(const EclParams<T>& P, long long 
   return gid + step * P.cstride[d] - (long long)step * P.cells[d] * P.cstride[d];
 }
 
+// Source of the upwind trace of neighbour nb (global id; -1: none): returns
+// the base pointer and sets *off so that base[*off + node] is the trace value
+// at node `node` of the neighbour's nb_node slab (node numbered inside the
+// neighbour's cell).  A neighbour in this part's vector is read in place; a
+// neighbour owned by another part -- only across the last direction, whose
+// layers the parts split, so its slab nb_node is the contiguous node range
+// [nb_node NC/N, (nb_node + 1) NC/N) -- is read from the ghost region, where
+// its face is the NC/N values of that range in order.  Every index formed for
+// a node of the slab lies inside the buffer it addresses.
+template <int NC, int N, typename T>
+__device__ __forceinline__ const T* trace_src(const EclParams<T>& P, long long nb, int nb_node, long long* off) {
+  const long long l = nb - P.gid0;
+  if (nb < 0) {
+    *off = 0;
+    return P.tin;
+  }
+  if (l >= 0 && l < P.n_cells) {
+    *off = l * NC;
+    return P.tin;
+  }
+  constexpr int NF = NC / N;
+  *off = (nb % P.layer) * NF - (long long)nb_node * NF;
+  return P.ghost;
+}
+
 // exterior value on a boundary (inflow) face: u+ = -u- (+ 2 g(x, t))
 template <int D, int N, typename T>
 __device__ __forceinline__ T boundary_value(const EclParams<T>& P, const int* cc, int d, int node, T um) {
@@ -262,13 +297,15 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
                                           T* so_all, const T* uu_all) {
   using S = EclShape<D, N, T>;
   constexpr int NC = S::NC, TPC = S::TPC;
-  const long long gid = cell0 + lc;
-  const bool valid = gid < P.n_cells;
+  const long long gid = cell0 + lc;  // local cell
+  const bool valid = gid < P.c_hi;
+  // global id (of a valid cell also for the idle threads of a partial block)
+  const long long gg = P.gid0 + (valid ? gid : P.c_lo);
 
   // ---- cell coordinates
   int cc[D];
   {
-    long long g = valid ? gid : 0;
+    long long g = gg;
     long long gx = g % (P.cstride[P.dim_x]), gv = g / (P.cstride[P.dim_x]);
 #pragma unroll
     for (int d = 0; d < D; ++d) {
@@ -290,11 +327,14 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
     const bool last = (ph == S::NPH - 1);
     const bool actA = valid && P.op[dA].active;
     const bool actB = dB >= 0 && valid && P.op[dB].active;
-    const long long nbA = actA ? neighbour(P, gid, cc, dA) : -1;
-    const long long nbB = actB ? neighbour(P, gid, cc, dB) : -1;
-    // face-load cells: the neighbour, or cell 0 where there is none, so that
-    // every load address is valid even if the compiler issues it unconditionally
-    const long long fA = nbA >= 0 ? nbA : 0, fB = nbB >= 0 ? nbB : 0;
+    const long long nbA = actA ? neighbour(P, gg, cc, dA) : -1;
+    const long long nbB = actB ? neighbour(P, gg, cc, dB) : -1;
+    // trace sources: the neighbour (here or in the ghost region), or cell 0
+    // where there is none, so that every load address is valid even if the
+    // compiler issues the guarded loads unconditionally
+    long long oA = 0, oB = 0;
+    const T* const sA = trace_src<NC, N>(P, nbA, P.op[dA].nb_node, &oA);
+    const T* const sB = dB >= 0 ? trace_src<NC, N>(P, nbB, P.op[dB].nb_node, &oB) : P.tin;
 
     for (int item = tl; item < nitems; item += TPC) {
       const int base = item_base<D, N>(item, dA, dB);
@@ -305,10 +345,10 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
         T upA[N], upB[N];
 #pragma unroll
         for (int b = 0; b < N; ++b)
-          upA[b] = nbA >= 0 ? __ldg(P.tin + fA * NC + base + LA.nb_node * strideA + b * strideB) : T(0);
+          upA[b] = nbA >= 0 ? __ldg(sA + (oA + base + LA.nb_node * strideA + b * strideB)) : T(0);
 #pragma unroll
         for (int a = 0; a < N; ++a)
-          upB[a] = nbB >= 0 ? __ldg(P.tin + fB * NC + base + a * strideA + LB.nb_node * strideB) : T(0);
+          upB[a] = nbB >= 0 ? __ldg(sB + (oB + base + a * strideA + LB.nb_node * strideB)) : T(0);
         T uu[N][N], acc[N][N];  // [a][b]: node base + a*strideA + b*strideB
         // phase 0: the plane of directions 0, 1 is N*N contiguous values; when
         // that is a whole number of 16-byte words it is read as such (far
@@ -418,7 +458,7 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
       } else {
         // single-direction phase (odd D): lines along dA
         const LineOp<T>& LA = P.op[dA];
-        const T upf = nbA >= 0 ? __ldg(P.tin + fA * NC + base + LA.nb_node * strideA) : T(0);
+        const T upf = nbA >= 0 ? __ldg(sA + (oA + base + LA.nb_node * strideA)) : T(0);
         T uu[N], acc[N];
 #pragma unroll
         for (int a = 0; a < N; ++a) {
@@ -483,11 +523,12 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
   using S = EclShape<D, N, double>;
   constexpr int NC = S::NC, TPC = S::TPC;
   constexpr int CST = EclTile<D, N, double>::CST;
-  const long long gid = cell0 + lc;
-  const bool valid = gid < P.n_cells;
+  const long long gid = cell0 + lc;  // local cell
+  const bool valid = gid < P.c_hi;
+  const long long gg = P.gid0 + (valid ? gid : P.c_lo);  // global id
   int cc[D];
   {
-    long long g = valid ? gid : 0;
+    long long g = gg;
     long long gx = g % (P.cstride[P.dim_x]), gv = g / (P.cstride[P.dim_x]);
 #pragma unroll
     for (int d = 0; d < D; ++d) {
@@ -522,12 +563,15 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
         const int lst = dd == 0 ? strideB : strideA;  // between the lines
         const LineOp<f32x2>& L = P.opx[d];
         const bool act = valid && L.active;
-        const long long nb = act ? neighbour(P, gid, cc, d) : -1;
+        const long long nb = act ? neighbour(P, gg, cc, d) : -1;
         const bool first = ph == 0 && dd == 0;
         const bool fin = lastph && dd == ndir - 1;
-        // upwind trace (cell 0 where there is no neighbour: every load address
-        // stays valid even if the compiler issues the guarded loads unconditionally)
-        const double* face = P.tin + (nb >= 0 ? nb : 0) * NC + L.nb_node * st;
+        // upwind trace (here or in the ghost region; cell 0 where there is no
+        // neighbour: every load address stays valid even if the compiler issues
+        // the guarded loads unconditionally)
+        long long fo = 0;
+        const double* const fs = trace_src<NC, N>(P, nb, L.nb_node, &fo);
+        const double* face = fs + (fo + L.nb_node * st);
         int l = rot;
         double upn = nb >= 0 ? __ldg(face + base + l * lst) : 0.0;
 #pragma unroll 1
@@ -643,10 +687,10 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
   T* const s_u1 = s_in0 + 4 * bufe;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lc = tid / TPC, tl = tid % TPC;
-  const long long nblk = (P.n_cells + cpb - 1) / cpb;
+  const long long nblk = (P.c_hi - P.c_lo + cpb - 1) / cpb;
   auto stage = [&](T* dst, T* dstu, long long blk) {
-    const long long c0 = blk * cpb;
-    const long long ncell = (P.n_cells - c0) < cpb ? (P.n_cells - c0) : cpb;
+    const long long c0 = P.c_lo + blk * cpb;
+    const long long ncell = (P.c_hi - c0) < cpb ? (P.c_hi - c0) : cpb;
     stage_cells<D, N, T>(dst, P.tin + c0 * NC, ncell, tid, nthr);
     if constexpr (SU) stage_cells<D, N, T>(dstu, P.uin + c0 * NC, ncell, tid, nthr);
   };
@@ -674,8 +718,10 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
       }
       __syncthreads();
     }
-    if constexpr (std::is_same_v<A, f32x2>) ecl_block_x2<D, N, MODE>(P, b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
-    else ecl_block<D, N, T, MODE>(P, b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+    if constexpr (std::is_same_v<A, f32x2>)
+      ecl_block_x2<D, N, MODE>(P, P.c_lo + b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+    else
+      ecl_block<D, N, T, MODE>(P, P.c_lo + b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
     __syncthreads();     // cur and s_o are free for the next blocks
     odd = !odd;
   }
@@ -729,7 +775,8 @@ cudaError_t launch_ecl(const EclParams<T>& P0, int mode, cudaStream_t stream) {
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
       }
-      const long long nblk = (P.n_cells + P.cpb - 1) / P.cpb;
+      const long long nblk = (P.c_hi - P.c_lo + P.cpb - 1) / P.cpb;
+      if (nblk <= 0) return cudaSuccess;  // an empty cell range launches nothing
       const long long want = (long long)sms * per_sm;
       const unsigned grid = unsigned(nblk < want ? nblk : want);
       kern<<<grid, threads, smem, stream>>>(P);

@@ -81,9 +81,16 @@ cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int* ticket, int mo
   Ecl6Params E;
   E.p = P;
   E.row_len = P.cells[0];
-  E.n_rows = int(P.n_cells / P.cells[0]);
+  // parts hold whole layers of v2, so every boundary below falls on a row
+  E.row_lo = int(P.c_lo / P.cells[0]);
+  E.row_hi = int(P.c_hi / P.cells[0]);
+  E.row0 = int(P.gid0 / P.cells[0]);
+  E.lay0 = int(P.gid0 / P.layer);
+  E.lay1 = int((P.gid0 + P.n_cells) / P.layer);
   E.err = err;
   E.ticket = ticket;
+  const int n_rows = E.row_hi - E.row_lo;
+  if (n_rows <= 0) return cudaSuccess;  // an empty cell range launches nothing
   Ecl6Maps maps;
   cudaError_t e = encode_ecl6_maps(P.tin, P.uin, P.n_cells * 4096LL, &maps);
   if (e != cudaSuccess) return e;
@@ -92,7 +99,7 @@ cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int* ticket, int mo
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int grid = 2 * sms;
-  if (grid > E.n_rows) grid = E.n_rows;
+  if (grid > n_rows) grid = n_rows;
   auto go = [&](auto kern) -> cudaError_t {
     if (!attr_done[mode]) {
       cudaError_t ee = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, E6_SMEM);

@@ -148,25 +148,30 @@ __device__ __forceinline__ int swz_o(int i) {
 }
 
 struct Ecl6Params {
-  EclParams<float> p;  // operator, mesh, vectors, stage factors
-  int n_rows;          // x0-rows of cells
+  EclParams<float> p;  // operator, mesh, vectors, stage factors, part (gid0, ghost, layer)
+  int row_lo, row_hi;  // the launch's x0-rows of cells (local rows [row_lo, row_hi))
   int row_len;         // cells per row (cells in x0)
+  int row0;            // global row index of local row 0 (parts hold whole layers)
+  int lay0, lay1;      // this part's layers [lay0, lay1) of direction v2
   int* err;            // device error flag
   int* ticket;         // next unclaimed row (zeroed before every launch)
 };
 
-// first cell id of row r and the upwind-neighbour offsets (in cells) of the
-// row's cells in directions 1..5 (inside a row only x0 varies)
+// first (local) cell id of row r and the upwind-neighbour offsets (in cells)
+// of the row's cells in directions 1..5 (inside a row only x0 varies); ghost5:
+// the v2 neighbour belongs to another part (its face is in the ghost region)
 struct E6Row {
   long long first;
   int nb[6];
+  int ghost5;
 };
 
 __device__ __forceinline__ E6Row e6_row(const Ecl6Params& P, int r) {
   E6Row R;
   R.first = (long long)r * P.row_len;
   R.nb[0] = 0;
-  int rem = r;
+  R.ghost5 = 0;
+  int rem = P.row0 + r;  // global row: coordinates of the global mesh
 #pragma unroll
   for (int d = 1; d < 6; ++d) {
     const int nc = P.p.cells[d];
@@ -175,7 +180,9 @@ __device__ __forceinline__ E6Row e6_row(const Ecl6Params& P, int r) {
     const int step = P.p.op[d].step;
     const int cs = int(P.p.cstride[d]);
     const int cn = c + step;
-    R.nb[d] = (cn < 0) ? (nc - 1) * cs : (cn >= nc ? -(nc - 1) * cs : step * cs);
+    const int cw = cn < 0 ? nc - 1 : (cn >= nc ? 0 : cn);  // periodic wrap
+    R.nb[d] = (cw - c) * cs;
+    if (d == 5 && (cw < P.lay0 || cw >= P.lay1)) R.ghost5 = 1;
   }
   return R;
 }
@@ -233,7 +240,7 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
       for (int d = 2; d < 6; ++d) bytes += P.p.op[d].active ? 4096u : 0u;
       auto take = [&]() -> int {
         const int t = atomicAdd(P.ticket, 1);
-        return t < P.n_rows ? t : -1;
+        return t < P.row_hi - P.row_lo ? P.row_lo + t : -1;
       };
       int q = 0, k = 0;
       int r = take();
@@ -269,8 +276,14 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
           tma_load_3d(st + 9216, &maps.tv0, 0, P.p.op[3].nb_node, int((gid + R.nb[3]) * 16), &full[s]);
         if (P.p.op[4].active)
           tma_load_3d(st + 10240, &maps.tv1, 0, P.p.op[4].nb_node, int((gid + R.nb[4]) * 4), &full[s]);
-        if (P.p.op[5].active)
-          bulk_load(st + 11264, P.p.tin + (gid + R.nb[5]) * 4096 + P.p.op[5].nb_node * 1024, 4096u, &full[s]);
+          if (P.p.op[5].active) {
+          // the v2 face: the neighbour's slab, or its face in the ghost region
+          // (a part's layer starts at a multiple of the layer size, so the
+          // neighbour's in-layer slot is this cell's)
+          const float* src5 = R.ghost5 ? P.p.ghost + (gid % P.p.layer) * 1024
+                                       : P.p.tin + (gid + R.nb[5]) * 4096 + P.p.op[5].nb_node * 1024;
+          bulk_load(st + 11264, src5, 4096u, &full[s]);
+        }
         ++issued;
         if (++k == P.row_len) {
           k = 0;

@@ -47,6 +47,8 @@ struct hd_adv {
   int variant;         // HD_KERNEL_AUTO / _GENERIC / _PIPELINED
   int arith;           // HD_ARITH_NATIVE / _FP32X2 (FP64 storage)
   int gauss;           // 1: Gauss quadrature (non-collocation) path
+  hd_part_layout part; // v-slab part of a partitioned operator (n_parts = 1: the whole mesh)
+  int n_parts, part_index;
   GaussTables gt;
   hd::GaussExtra<double> g64;
   hd::GaussExtra<float> g32;

@@ -62,7 +62,7 @@ __global__ void interpolate_kernel(VecGeom g, DevFunction f, const double* __res
                                    long long n_cells) {
   for (long long gid = blockIdx.x; gid < n_cells; gid += gridDim.x) {
     int toff[kMaxDim];
-    cell_offsets(g, gid, toff);
+    cell_offsets(g, g.gid0 + gid, toff);
     T* out = dst + gid * g.NC;
     for (int node = threadIdx.x; node < g.NC; node += blockDim.x) {
       double jxw;
@@ -78,7 +78,7 @@ __global__ void norm_error_kernel(VecGeom g, DevFunction f, const double* __rest
   double s0 = 0.0, s1 = 0.0;
   for (long long gid = blockIdx.x; gid < n_cells; gid += gridDim.x) {
     int toff[kMaxDim];
-    cell_offsets(g, gid, toff);
+    cell_offsets(g, g.gid0 + gid, toff);
     const T* in = src + gid * g.NC;
     for (int node = threadIdx.x; node < g.NC; node += blockDim.x) {
       double jxw;
@@ -141,7 +141,7 @@ __global__ void norm_error_gauss_kernel(VecGeom g, DevFunction f, const double* 
       __syncthreads();
     }
     int toff[kMaxDim];
-    cell_offsets(g, gid, toff);
+    cell_offsets(g, g.gid0 + gid, toff);
     for (int node = threadIdx.x; node < NC; node += blockDim.x) {
       double ex = f.kind == 0 ? 0.0 : f.amp, jxw = 1.0;
       int t = node;
@@ -266,6 +266,38 @@ cudaError_t launch_lsrk_update(int is_f32, long long n, double bi, double ai, co
   else
     lsrk_update_kernel<double><<<grid, 256, 0, s>>>(n, bi, ai, (const double*)K, (double*)sol,
                                                      (double*)next_T);
+  return cudaGetLastError();
+}
+
+// The face pack of a partitioned operator (hd_adv_pack_faces): one face slab
+// per cell of a layer, gathered into the contiguous buffer the receiving part
+// keeps as its ghost region.  16-byte words when every address and size
+// allows, 4-byte words otherwise; consecutive threads copy consecutive words.
+template <typename W>
+__global__ void pack_faces_kernel(const char* __restrict__ src, long long stride, long long words_per_face,
+                                  long long n_faces, char* __restrict__ dst) {
+  const long long total = words_per_face * n_faces;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long f = i / words_per_face, j = i - f * words_per_face;
+    reinterpret_cast<W*>(dst)[i] = __ldcs(reinterpret_cast<const W*>(src + f * stride) + j);
+  }
+}
+
+cudaError_t launch_pack_faces(const void* src, long long stride_bytes, long long face_bytes, long long n_faces,
+                              void* dst, cudaStream_t s) {
+  if (n_faces <= 0 || face_bytes <= 0) return cudaSuccess;
+  const bool w16 = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0 &&
+                   stride_bytes % 16 == 0 && face_bytes % 16 == 0;
+  const long long words = n_faces * (face_bytes / (w16 ? 16 : 4));
+  const long long want = (words + 255) / 256;
+  const unsigned grid = unsigned(want < 152 * 16 ? want : 152 * 16);
+  if (w16)
+    pack_faces_kernel<float4><<<grid, 256, 0, s>>>((const char*)src, stride_bytes, face_bytes / 16, n_faces,
+                                                   (char*)dst);
+  else
+    pack_faces_kernel<float><<<grid, 256, 0, s>>>((const char*)src, stride_bytes, face_bytes / 4, n_faces,
+                                                  (char*)dst);
   return cudaGetLastError();
 }
 

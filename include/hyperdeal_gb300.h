@@ -166,6 +166,67 @@ int hd_adv_apply(hd_adv *op, void *dst, const void *src, double time, void *stre
  * (operators/advection/cfl.h:56-124, Cartesian mesh). */
 double hd_adv_critical_time_step(const hd_adv *op);
 
+/* ---- partitioned operator: v-slabs with one ghost-face exchange per stage --
+ *
+ * Replaces the reference's distributed MatrixFree with a v-only process grid
+ * (size_x = 1) and its Contiguous ghost-face partitioner
+ * (include/hyper.deal/matrix_free/vector_partitioner.h:670-1381 set-up,
+ * :1385-1607 exchange) and the overlap of the exchange with the cells that do
+ * not need it (matrix_free.templates.h:1178-1234, :1494-1581).
+ *
+ * The mesh is cut into n_parts slabs of whole layers of the last direction
+ * (v_{dim_v-1}, the slowest in the cell numbering), so a part owns a
+ * contiguous range of cell ids: part p owns layers [p L / P, (p+1) L / P)
+ * (integer division; L = cells in that direction, P = n_parts <= L).  Only
+ * faces across that direction cross parts, and only the upwind face is read
+ * (the downwind neighbour's trace enters the reference's flux multiplied by
+ * zero), so each part needs the faces of ONE layer of ONE neighbour part.
+ *
+ * A part's vectors hold its cells -- n_cells (k+1)^D values numbered as the
+ * global vector restricted to the range -- followed by a ghost region of
+ * ghost_values values: the upwind neighbour layer's face traces, (k+1)^(D-1)
+ * values per cell (the nodes of the face slab in order), cells in their
+ * in-layer order (the reference keeps ghost faces after the local cells as
+ * well, vector_partitioner.h:916-993).  An exchange per stage: the sending
+ * part packs the faces (hd_adv_pack_faces) and the host's transport (NCCL,
+ * MPI, a peer copy) moves them into the receiving part's ghost region of the
+ * same vector.  The layout is computed on the host alone: */
+typedef struct hd_part_layout {
+  long long first_cell;      /* global id of the part's first cell                 */
+  long long n_cells;         /* cells of the part                                  */
+  long long layer_cells;     /* cells per layer of the last direction              */
+  long long face_values;     /* values per face, (k+1)^(D-1)                       */
+  long long ghost_values;    /* values of the ghost region (0: no ghost faces)     */
+  int recv_from;             /* part whose faces fill the ghost region (-1: none)  */
+  int send_to;               /* part whose ghost region this part fills (-1: none) */
+  long long send_first_cell; /* local id of the first cell of the sent layer       */
+  int send_slab;             /* node index along the last direction of sent faces  */
+  long long boundary_first;  /* local cells that read the ghost region: the       */
+  long long boundary_cells;  /*   range [boundary_first, +boundary_cells)          */
+} hd_part_layout;
+
+/* Layout of part `part` of `n_parts` for the descriptor (no CUDA call). */
+int hd_part_layout_get(const hd_adv_desc *desc, int n_parts, int part, hd_part_layout *out);
+
+/* The operator of one part (Gauss-Lobatto collocation; any dimension split,
+ * degree and dtype of hd_adv_create).  n_parts = 1 is hd_adv_create.  The
+ * part's operator works on its vectors (hd_adv_n_dofs() values + ghost
+ * region); hd_adv_apply reads the ghost region of src, which must hold the
+ * neighbour's faces of src. */
+int hd_adv_create_part(const hd_adv_desc *desc, int n_parts, int part, hd_adv **out);
+int hd_adv_part_layout(const hd_adv *op, hd_part_layout *out);
+
+/* Pack the faces of `vec` that part send_to reads into sendbuf
+ * (ghost_values of the receiver = layer_cells * face_values values of the
+ * handle's dtype, in the receiver's ghost-region order). */
+int hd_adv_pack_faces(hd_adv *op, const void *vec, void *sendbuf, void *stream);
+
+/* Cell subsets of a launch: the cells that read the ghost region (BOUNDARY,
+ * one layer at one end of the part) and the others (INTERIOR), so that
+ * INTERIOR runs while the ghost faces are in flight. */
+enum hd_cells { HD_CELLS_ALL = 0, HD_CELLS_INTERIOR = 1, HD_CELLS_BOUNDARY = 2 };
+int hd_adv_apply_cells(hd_adv *op, void *dst, const void *src, double time, int cells, void *stream);
+
 /* ---- vector tools --------------------------------------------------------- */
 
 /* dst = f(x_i, time) at the Gauss-Lobatto support points
@@ -211,9 +272,21 @@ int hd_lsrk_n_stages(const hd_lsrk *rk);
  * updated, so the three vectors rotate roles; on return the three pointers
  * are permuted so that *sol holds the new solution (the others are scratch).
  * The reference's own Ki/Ti vectors are scratch in the same way.  The values
- * equal the unfused step within round-off. */
+ * equal the unfused step within round-off.  A part with a ghost region steps
+ * with hd_lsrk_stage and an exchange between stages (HD_ERR_UNSUPPORTED). */
 int hd_lsrk_step(hd_adv *op, const hd_lsrk *rk, void **sol, void **Ki, void **Ti,
                  double time, double dt, void *stream);
+
+/* Stage `stage` of the same fused step on a subset of cells (enum hd_cells),
+ * for drivers that exchange ghost faces between stages (partitioned
+ * operators).  X[0..2] are the step's vectors sol, Ki, Ti in the roles they
+ * had when the step began; stage s reads X[hd_lsrk_stage_input(rk, s)] (whose
+ * ghost region must hold the neighbour's faces of that vector) and after the
+ * last stage the new solution is X[1] (hd_lsrk_step's permutation: sol <- X1,
+ * Ki <- X0, Ti <- X2).  hd_lsrk_step runs every stage on all cells. */
+int hd_lsrk_stage(hd_adv *op, const hd_lsrk *rk, int stage, void *const *X, double time, double dt, int cells,
+                  void *stream);
+int hd_lsrk_stage_input(const hd_lsrk *rk, int stage);
 
 /* The unfused reference form of the same step: op(Ti, Ki, t_s) followed by
  * the vector update, exactly in the reference's order
