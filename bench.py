@@ -600,6 +600,12 @@ def main():
     ap.add_argument("--steps-f64", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--l2-steps", type=int, default=20,
+                    help="rk45 steps after which the FP32 and FP64 forms are compared (default 20)")
+    ap.add_argument("--apply-reps", type=int, default=20, help="timed applies of the per-apply line (0: none)")
+    ap.add_argument("--backend", default="nccl", choices=["nccl", "gloo"],
+                    help="torch.distributed backend of the ghost-face exchange for --gpus N > 1 (gloo stages the "
+                         "faces through host memory)")
     ap.add_argument("--cells-x", type=int, default=CELLS,
                     help="x-cells per direction (8 = the benchmark workload; smaller only for profiling)")
     ap.add_argument("--workload", default="advection6d",
@@ -646,31 +652,53 @@ def main():
 
     from hyperdeal_gb300.replicas import Replicas, time_steps, whole_job_rate
 
-    rep = Replicas("nccl")
+    rep = Replicas(args.backend)
     world, rank, local = rep.world, rep.rank, rep.local_rank
-    torch.cuda.set_device(local)
+    torch.cuda.set_device(local % torch.cuda.device_count())
     dist = rep.dist
 
+    def make_params(dtype, layers_v2=CELLS):
+        # N > 1: the v2 direction is extended to N x 8 layers (h unchanged), one v-slab of 8 layers per rank
+        return A.AdvectionParameters(DIM_X, DIM_V, DEGREE, [args.cells_x] * 3, [CELLS, CELLS, layers_v2],
+                                     [0.0] * 3, [1.0] * 3, [0.0] * 3, [1.0, 1.0, layers_v2 / CELLS], VELOCITY,
+                                     dtype=dtype)
+
     def make_op(dtype):
-        p = A.AdvectionParameters(DIM_X, DIM_V, DEGREE, [args.cells_x] * 3, [CELLS] * 3, [0.0] * 3, [1.0] * 3,
-                                  [0.0] * 3, [1.0] * 3, VELOCITY, dtype=dtype)
-        return A.AdvectionOperation(p)
+        return A.AdvectionOperation(make_params(dtype))
 
     rng = np.random.default_rng(0)
     phi = list(rng.uniform(0, 2 * math.pi, 6))
     f0 = A.Function(2, 1.0, omega=[2 * math.pi] * 6, speed=[0.0] * 6, phase=phi)
 
-    op = make_op("f32")
+    stream = torch.cuda.current_stream()
+    if world > 1:
+        # weak scaling over v-slabs: rank r owns layers [8r, 8r + 8) of v2; the upwind v2 faces of its
+        # first layer come from rank r - 1 before every stage (NCCL point-to-point, overlapped with the
+        # interior cells)
+        from hyperdeal_gb300 import partition as Pt
+        op = Pt.PartitionedAdvectionOperation(make_params("f32", CELLS * world), world, rank)
+        exchange = Pt.DistributedExchange(op)
+        sol = op.initialize_dof_vector()
+        op.interpolate(f0, sol, 0.0)
+        Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
+        integ = A.LowStorageRungeKuttaIntegrator(Ki, Ti, "rk45")
+
+        def advance(t_):
+            op.perform_time_step(integ, sol, t_, dt, exchange)
+    else:
+        op = make_op("f32")
+        sol = op.initialize_dof_vector()
+        A.VectorTools.interpolate(op, f0, sol, 0.0)
+        Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
+        integ = A.LowStorageRungeKuttaIntegrator(Ki, Ti, "rk45")
+
+        def advance(t_):
+            integ.perform_time_step(sol, t_, dt, op)
     n = op.n_dofs
     dt = CFL * op.critical_time_step() / DEGREE ** 1.5
-    sol = op.initialize_dof_vector()
-    A.VectorTools.interpolate(op, f0, sol, 0.0)
-    Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
-    integ = A.LowStorageRungeKuttaIntegrator(Ki, Ti, "rk45")
-    stream = torch.cuda.current_stream()
     t = 0.0
     for _ in range(args.warmup):
-        integ.perform_time_step(sol, t, dt, op)
+        advance(t)
         t += dt
     torch.cuda.synchronize()
     rep.barrier()
@@ -681,7 +709,7 @@ def main():
     tt = {"t": t}
 
     def one_step():
-        integ.perform_time_step(sol, tt["t"], dt, op)
+        advance(tt["t"])
         tt["t"] += dt
 
     def cuda_clock():
@@ -712,10 +740,35 @@ def main():
                 "kernel": ("hd::ecl6_kernel<stage> (persistent, TMA-pipelined)" if op.kernel == "pipelined"
                            else "hd::ecl_kernel<6,4,float,stage> (generic)")}
 
+    # per-apply figures (the reference's operator benchmark, performance/operators_advection_01.likwid.cc:
+    # 341-348: DoFs * applies / time): src read, dst written, 2 S N algorithmic bytes per apply
+    def time_applies(o, src, reps):
+        dst = o.initialize_dof_vector()
+        for _ in range(2):
+            o.apply(dst, src, 0.0)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            o.apply(dst, src, 0.0)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        S = 4 if o.dtype == torch.float32 else 8
+        gbs = 2 * S * o.n_dofs / (ms / 1e3) / 1e9
+        del dst
+        return {"ms_per_apply": round(ms, 4), "gdof_per_s": round(o.n_dofs / (ms / 1e3) / 1e9, 3),
+                "hbm_gb_per_s": round(gbs, 1), "frac": round(gbs / measured_peak_hbm()[0], 4), "applies": reps}
+
+    apply_lines = {}
+    if world == 1 and args.apply_reps > 0:
+        apply_lines["f32"] = dict(time_applies(op, sol, args.apply_reps),
+                                  kernel="hd::ecl6_kernel<kApply>" if op.kernel == "pipelined" else "generic")
+        torch.cuda.empty_cache()
+
     # FP64 form of the same steps, and the L2 difference of the two solutions
     f64 = {}
     l2 = None
-    if args.steps_f64 > 0:
+    if args.steps_f64 > 0 and world == 1:
         op64 = make_op("f64")
         s64 = op64.initialize_dof_vector()
         A.VectorTools.interpolate(op64, f0, s64, 0.0)
@@ -751,13 +804,19 @@ def main():
         msx = e0.elapsed_time(e1) / args.steps_f64
         f64x = {"value": round(n * N_STAGES / (msx / 1e3) / 1e9, 3), "ms_per_step": round(msx, 3),
                 "steps": args.steps_f64, "arithmetic": "FP32x2 (double-word FP32) contractions, FP64 storage"}
-        # same number of steps from the same initial data in the three forms
+        if args.apply_reps > 0:
+            reps64 = max(2, args.apply_reps // 10)
+            apply_lines["f64_fp32x2"] = time_applies(op64, s64, reps64)
+            op64.set_arithmetic("native")
+            apply_lines["f64"] = time_applies(op64, s64, reps64)
+            op64.set_arithmetic("fp32x2")
+        # the same number of steps from the same initial data in the three forms
         s32 = op.initialize_dof_vector()
         A.VectorTools.interpolate(op, f0, s32, 0.0)
         s64b = op64.initialize_dof_vector()
         A.VectorTools.interpolate(op64, f0, s64b, 0.0)
         s64x = s64b.clone()
-        nsteps = args.warmup + args.steps_f64
+        nsteps = args.l2_steps
         tt = 0.0
         for _ in range(nsteps):
             integ.perform_time_step(s32, tt, dt, op)
@@ -781,7 +840,27 @@ def main():
     # H2D / compute / D2H on three streams so that the copies of neighbouring steps overlap the
     # step in between (both copy directions run concurrently over the host link).
     e2e = None
-    if not args.no_e2e:
+    if not args.no_e2e and world > 1:
+        # N ranks: each rank's part through the partitioned public API, its state copied in from pinned
+        # host memory and back every step (H2D, step with the ghost exchanges, D2H on one stream)
+        host_in = torch.empty(n, dtype=torch.float32, pin_memory=True)
+        host_in.copy_(op.owned(sol))
+        host_out = torch.empty(n, dtype=torch.float32, pin_memory=True)
+        k_e2e = max(4, min(args.steps, 8))
+
+        def e2e_step():
+            op.owned(sol).copy_(host_in, non_blocking=True)
+            advance(t)
+            host_out.copy_(op.owned(sol), non_blocking=True)
+
+        ms_seq = time_steps(rep, e2e_step, k_e2e, 2, torch.cuda.synchronize, cuda_clock)
+        e2e = {"value": round(world * n * N_STAGES / (ms_seq / 1e3) / 1e9, 3), "unit": UNIT,
+               "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": 4 * n, "ms_per_step": round(ms_seq, 3),
+               "steps": k_e2e, "path": "PartitionedAdvectionOperation.perform_time_step (C ABI stages, NCCL "
+                                       "ghost exchange) on each rank's part copied in from and out to pinned "
+                                       "host memory every step; per-rank bytes"}
+        del host_in, host_out
+    if not args.no_e2e and world == 1:
         import ctypes
 
         from hyperdeal_gb300 import _lib as hdl
@@ -858,21 +937,24 @@ def main():
         torch.cuda.empty_cache()
 
     cpu = None
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample()
 
     if rank == 0:
         out = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-               "config": workload_config({"parallelism": "replicas" if world > 1 else "single GPU",
+               "config": workload_config({"parallelism": ("v-slabs: %d ranks x 8 layers of v2, one NCCL ghost-face "
+                                                          "exchange per stage" % world) if world > 1
+                                          else "single GPU",
                                           **({} if args.cells_x == CELLS else
                                              {"profiling_case_cells": "%d^3 x 8^3" % args.cells_x,
                                               "n_dofs": n})}),
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-               "gpu_launches": N_STAGES * args.steps,
+               # per stage: the stage kernel; with N ranks also the face pack and the boundary-layer launch
+               "gpu_launches": N_STAGES * args.steps * (3 if world > 1 else 1),
                "f64_form": f64, "f32_over_f64": round(value / f64["value"], 3) if f64 else None,
-               "l2_rel_err_f32_vs_f64": l2}
+               "l2_rel_err_f32_vs_f64": l2, "apply": apply_lines or None}
         print(json.dumps(out))
     rep.close()
     return 0

@@ -30,7 +30,7 @@ EXPORTED_SYMBOLS = (
     "hd_adv_autotune", "hd_vp_lsrk_step_fused", "hd_adv_set_arithmetic", "hd_adv_arithmetic",
     "hd_batch_class_arithmetic", "hd_vp_set_arithmetic",
     "hd_part_layout_get", "hd_adv_create_part", "hd_adv_part_layout", "hd_adv_pack_faces", "hd_adv_apply_cells",
-    "hd_lsrk_stage", "hd_lsrk_stage_input",
+    "hd_lsrk_stage", "hd_lsrk_stage_input", "hd_adv_set_wait_test",
 )
 HD_KERNEL_AUTO, HD_KERNEL_GENERIC, HD_KERNEL_PIPELINED = 0, 1, 2
 HD_ARITH_NATIVE, HD_ARITH_FP32X2 = 0, 1
@@ -86,7 +86,9 @@ _lib = None
 
 
 def lib_path() -> str:
-    return _build.LIB_PATH
+    """The library this process loads: the in-tree build, or its bounds-checked variant when the
+    environment sets HYPERDEAL_GB300_CHECK=1 (hyperdeal_gb300/build.py --check)."""
+    return _build.CHECK_LIB_PATH if os.environ.get("HYPERDEAL_GB300_CHECK") == "1" else _build.LIB_PATH
 
 
 def load(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -94,11 +96,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     global _lib
     if _lib is not None:
         return _lib
-    path = _build.LIB_PATH
+    path = lib_path()
     if not os.path.exists(path):
         if not build_if_missing:
             raise HdError(HD_ERR_UNSUPPORTED, "CUDA library %s is not built" % path)
-        _build.build()
+        _build.build(check=path == _build.CHECK_LIB_PATH)
     L = ctypes.CDLL(path)
     vp = ctypes.c_void_p
     dp = ctypes.POINTER(ctypes.c_double)
@@ -174,6 +176,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.hd_adv_apply_cells.argtypes = [vp, vp, vp, ctypes.c_double, ctypes.c_int, vp]
     L.hd_lsrk_stage.argtypes = [vp, vp, ctypes.c_int, vpp, ctypes.c_double, ctypes.c_double, ctypes.c_int, vp]
     L.hd_lsrk_stage_input.argtypes = [vp, ctypes.c_int]
+    L.hd_adv_set_wait_test.argtypes = [vp, ctypes.c_uint, ctypes.c_int]
     _lib = L
     return L
 

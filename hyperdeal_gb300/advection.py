@@ -201,6 +201,10 @@ class AdvectionOperation:
         check(self._L.hd_adv_tile_limits(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def set_wait_test(self, wait_limit: int = 0, skip_issue: int = -1) -> None:
+        """Test hook of the pipelined kernel's bounded waits (hd_adv_set_wait_test)."""
+        check(self._L.hd_adv_set_wait_test(self._h, int(wait_limit), int(skip_issue)))
+
     def device_status(self) -> int:
         """Error code recorded by the device since the last call (0 = none); synchronises."""
         st = ctypes.c_int(0)

@@ -23,6 +23,9 @@ OUT_DIR = os.path.join(PKG, "_lib")
 BUILD_DIR = os.path.join(PKG, "_build")
 LIB_NAME = "libhyperdeal_gb300.so"
 LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
+# the bounds-checked variant (-DHD_CHECK): every global load and store of the ECL kernels checks
+# its index and records a violation in the operator's device status instead of accessing memory
+CHECK_LIB_PATH = os.path.join(OUT_DIR, "libhyperdeal_gb300_check.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
@@ -51,8 +54,8 @@ GEN_UNITS = ([("ecl", "hd_ecl.cuh", "EclLaunchers", "make_launchers", D, N) for 
                 for D in range(2, 7) for N in range(2, 6)])
 
 
-def _generate_units() -> list:
-    gen = os.path.join(BUILD_DIR, "gen")
+def _generate_units(build_dir: str = BUILD_DIR) -> list:
+    gen = os.path.join(build_dir, "gen")
     os.makedirs(gen, exist_ok=True)
     out = []
     for fam, header, ret, factory, D, N in GEN_UNITS:
@@ -66,21 +69,22 @@ def _generate_units() -> list:
     return out
 
 
-def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> str:
-    """Compile and link the library; returns its path."""
-    os.makedirs(BUILD_DIR, exist_ok=True)
-    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu"))) + _generate_units()
-    flags = ARCH + NVCC_FLAGS + ["-I", CSRC]
-    stamp = os.path.join(OUT_DIR, ".stamp")
+def build(force: bool = False, verbose: bool = False, jobs: int | None = None, check: bool = False) -> str:
+    """Compile and link the library (check=True: the bounds-checked variant); returns its path."""
+    build_dir = BUILD_DIR + ("_check" if check else "")
+    lib_path = CHECK_LIB_PATH if check else LIB_PATH
+    os.makedirs(build_dir, exist_ok=True)
+    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu"))) + _generate_units(build_dir)
+    flags = ARCH + NVCC_FLAGS + ["-I", CSRC] + (["-DHD_CHECK"] if check else [])
+    stamp = os.path.join(OUT_DIR, ".stamp_check" if check else ".stamp")
     digest = _deps_hash(" ".join(flags))
-    if not force and os.path.exists(LIB_PATH) and os.path.exists(stamp) and open(stamp).read() == digest:
-        return LIB_PATH
-    os.makedirs(BUILD_DIR, exist_ok=True)
+    if not force and os.path.exists(lib_path) and os.path.exists(stamp) and open(stamp).read() == digest:
+        return lib_path
     os.makedirs(OUT_DIR, exist_ok=True)
 
     def compile_one(src: str) -> str:
-        obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
-        key = os.path.join(BUILD_DIR, os.path.basename(src) + ".key")
+        obj = os.path.join(build_dir, os.path.basename(src) + ".o")
+        key = os.path.join(build_dir, os.path.basename(src) + ".key")
         if not force and os.path.exists(obj) and os.path.exists(key) and open(key).read() == digest:
             return obj
         cmd = [nvcc()] + flags + ["-c", src, "-o", obj]
@@ -99,15 +103,15 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
                                            else 1 if os.path.basename(p).startswith(("ecl_4", "batch_4")) else 2))
     with ThreadPoolExecutor(max_workers=jobs) as ex:
         objs = list(ex.map(compile_one, order))
-    tmp = LIB_PATH + ".tmp%d" % os.getpid()
+    tmp = lib_path + ".tmp%d" % os.getpid()
     cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "shared", "-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
-    os.replace(tmp, LIB_PATH)
+    os.replace(tmp, lib_path)
     with open(stamp, "w") as f:
         f.write(digest)
-    return LIB_PATH
+    return lib_path
 
 
 def build_cpp_app(name: str = "advection_hyperrectangle") -> str:
@@ -131,4 +135,4 @@ def build_cpp_app(name: str = "advection_hyperrectangle") -> str:
 
 if __name__ == "__main__":
     import sys
-    print(build(force="--force" in sys.argv, verbose=True))
+    print(build(force="--force" in sys.argv, verbose=True, check="--check" in sys.argv))

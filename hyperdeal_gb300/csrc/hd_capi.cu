@@ -261,6 +261,7 @@ void fill_params(const hd_adv* op, hd::EclParams<T>* P) {
   P->c_hi = op->n_cells;
   P->layer = op->part.layer_cells;
   P->ghost = nullptr;
+  P->err = nullptr;
   for (int i = 0; i < op->N; ++i) P->gl[i] = op->gl[i];
   P->bc_inhom = op->desc.bc_kind == HD_BC_FUNCTION;
   P->bc = to_dev(op->desc.bc);
@@ -331,7 +332,7 @@ int launch(hd_adv* op, int mode, const void* tin, const void* uin, void* uout, v
     hd::EclParams<float> P = op->p32;
     set_launch(op, &P, tin, uin, uout, tout, fb, fa, time, c_lo, c_hi);
     int* ticket = op->d_tickets + (op->ticket_slot++ % hd::kTicketSlots);
-    e = hd::launch_ecl6(P, op->d_err, ticket, mode, s);
+    e = hd::launch_ecl6(P, op->d_err, ticket, mode, s, op->wait_limit, op->skip_issue);
   } else if (op->dtype == HD_F64) {
     hd::EclParams<double> P = op->p64;
     set_launch(op, &P, tin, uin, uout, tout, fb, fa, time, c_lo, c_hi);
@@ -556,12 +557,16 @@ static int create_impl(const hd_adv_desc* desc, int n_parts, int part, bool layo
     e = cudaMalloc(&op->d_partials, sizeof(double) * (2 * hd::kNormBlocks + 3 + hd::kTicketSlots / 2));
     if (e != cudaSuccess) { delete op; return cuda_fail(e, "cudaMalloc (norm scratch)"); }
     op->d_err = reinterpret_cast<int*>(op->d_partials + 2 * hd::kNormBlocks + 2);
+    op->p64.err = op->d_err;  // (bounds-checked builds record violations here)
+    op->p32.err = op->d_err;
     op->d_tickets = reinterpret_cast<int*>(op->d_partials + 2 * hd::kNormBlocks + 3);
     op->ticket_slot = 0;
     e = cudaMemset(op->d_err, 0, sizeof(int));
     if (e != cudaSuccess) { cudaFree(op->d_partials); delete op; return cuda_fail(e, "cudaMemset (error flag)"); }
     op->variant = HD_KERNEL_AUTO;
     op->arith = HD_ARITH_NATIVE;
+    op->wait_limit = 0;
+    op->skip_issue = -1;
     {
       size_t tsize = 0;
       for (int i = 0; i < op->D; ++i) tsize += size_t(op->cells[i]) * op->N;
@@ -713,6 +718,14 @@ int hd_adv_set_arithmetic(hd_adv* op, int arithmetic) {
 }
 
 int hd_adv_arithmetic(const hd_adv* op) { return op ? op->arith : -1; }
+
+int hd_adv_set_wait_test(hd_adv* op, unsigned wait_limit, int skip_issue) {
+  if (!op) return fail(HD_ERR_INVALID, "hd_adv_set_wait_test: null handle");
+  if (skip_issue < -1) return fail(HD_ERR_INVALID, "hd_adv_set_wait_test: skip_issue must be >= -1");
+  op->wait_limit = wait_limit;
+  op->skip_issue = skip_issue;
+  return HD_OK;
+}
 
 int hd_adv_device_status(hd_adv* op, int* status) {
   if (!op || !status) return fail(HD_ERR_INVALID, "hd_adv_device_status: null argument");

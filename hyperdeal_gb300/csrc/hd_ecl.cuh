@@ -85,7 +85,32 @@ struct EclParams {
   // c_hi = n_cells, ghost = nullptr.
   long long gid0, c_lo, c_hi, layer;
   const T* ghost;
+  int* err;  // the operator's device status (bounds-checked builds record violations there)
 };
+
+// Device status code of a failed bounds check (builds with -DHD_CHECK only).
+constexpr int kCheckError = 4;
+
+// Bounds-checked build (-DHD_CHECK; hyperdeal_gb300/build.py --check): the
+// global loads and stores of the ECL kernels check their element index
+// against the buffer they address -- the part's cells (n_cells NC values) or
+// the ghost region (layer NC/N values) -- and a violation records kCheckError
+// in the device status and skips the access instead of trapping.  In the
+// normal build the check is the constant true and costs nothing.
+template <int NC, int N, typename T>
+__device__ __forceinline__ bool checked(const EclParams<T>& P, const T* base, long long idx) {
+#ifdef HD_CHECK
+  const long long bound = (base == P.ghost && base != P.tin) ? P.layer * (NC / N) : P.n_cells * NC;
+  if (idx >= 0 && idx < bound) return true;
+  if (P.err) atomicExch(P.err, kCheckError);
+  return false;
+#else
+  (void)P;
+  (void)base;
+  (void)idx;
+  return true;
+#endif
+}
 
 enum EclMode { kApply = 0, kStageFirst = 1, kStageMid = 2, kStageLast = 3 };
 
@@ -321,34 +346,40 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
   for (int ph = 0; ph < S::NPH; ++ph) {
     const int dA = 2 * ph;
     const int dB = (2 * ph + 1 < D) ? 2 * ph + 1 : -1;
+    const int dBi = dB >= 0 ? dB : dA;  // an index that is valid also where dB = -1 is never used
     const int strideA = ipow(N, dA);
     const int strideB = strideA * N;
     const int nitems = dB >= 0 ? ipow(N, D - 2) : ipow(N, D - 1);
     const bool last = (ph == S::NPH - 1);
     const bool actA = valid && P.op[dA].active;
-    const bool actB = dB >= 0 && valid && P.op[dB].active;
+    const bool actB = dB >= 0 && valid && P.op[dBi].active;
     const long long nbA = actA ? neighbour(P, gg, cc, dA) : -1;
-    const long long nbB = actB ? neighbour(P, gg, cc, dB) : -1;
+    const long long nbB = actB ? neighbour(P, gg, cc, dBi) : -1;
     // trace sources: the neighbour (here or in the ghost region), or cell 0
     // where there is none, so that every load address is valid even if the
     // compiler issues the guarded loads unconditionally
     long long oA = 0, oB = 0;
     const T* const sA = trace_src<NC, N>(P, nbA, P.op[dA].nb_node, &oA);
-    const T* const sB = dB >= 0 ? trace_src<NC, N>(P, nbB, P.op[dB].nb_node, &oB) : P.tin;
+    const T* const sB = dB >= 0 ? trace_src<NC, N>(P, nbB, P.op[dBi].nb_node, &oB) : P.tin;
 
     for (int item = tl; item < nitems; item += TPC) {
       const int base = item_base<D, N>(item, dA, dB);
       if (dB >= 0) {
         const LineOp<T>& LA = P.op[dA];
-        const LineOp<T>& LB = P.op[dB];
+        const LineOp<T>& LB = P.op[dBi];
         // upwind face values of the N lines of both directions, issued first
         T upA[N], upB[N];
 #pragma unroll
         for (int b = 0; b < N; ++b)
-          upA[b] = nbA >= 0 ? __ldg(sA + (oA + base + LA.nb_node * strideA + b * strideB)) : T(0);
+        {
+          const long long ia = oA + base + LA.nb_node * strideA + b * strideB;
+          upA[b] = nbA >= 0 && checked<NC, N>(P, sA, ia) ? __ldg(sA + ia) : T(0);
+        }
 #pragma unroll
-        for (int a = 0; a < N; ++a)
-          upB[a] = nbB >= 0 ? __ldg(sB + (oB + base + a * strideA + LB.nb_node * strideB)) : T(0);
+        for (int a = 0; a < N; ++a) {
+          const long long ib = oB + base + a * strideA + LB.nb_node * strideB;
+          upB[a] = nbB >= 0 && checked<NC, N>(P, sB, ib) ? __ldg(sB + ib) : T(0);
+        }
         T uu[N][N], acc[N][N];  // [a][b]: node base + a*strideA + b*strideB
         // phase 0: the plane of directions 0, 1 is N*N contiguous values; when
         // that is a whole number of 16-byte words it is read as such (far
@@ -444,6 +475,7 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
             for (int a = 0; a < N; ++a) {
               const long long gi = g0 + base + a * strideA + b * strideB;
               const T k = acc[a][b];
+              if (!checked<NC, N>(P, P.tin, gi)) continue;
               if constexpr (MODE == kApply) {
                 P.uout[gi] = k;
               } else {
@@ -458,7 +490,8 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
       } else {
         // single-direction phase (odd D): lines along dA
         const LineOp<T>& LA = P.op[dA];
-        const T upf = nbA >= 0 ? __ldg(sA + (oA + base + LA.nb_node * strideA)) : T(0);
+        const long long iu = oA + base + LA.nb_node * strideA;
+        const T upf = nbA >= 0 && checked<NC, N>(P, sA, iu) ? __ldg(sA + iu) : T(0);
         T uu[N], acc[N];
 #pragma unroll
         for (int a = 0; a < N; ++a) {
@@ -491,6 +524,7 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
           for (int a = 0; a < N; ++a) {
             const long long gi = g0 + base + a * strideA;
             const T k = acc[a];
+            if (!checked<NC, N>(P, P.tin, gi)) continue;
             if constexpr (MODE == kApply) {
               P.uout[gi] = k;
             } else {
@@ -558,7 +592,10 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
       const int base = item_base<D, N>(item, dA, dB);
 #pragma unroll 1
       for (int dd = 0; dd < ndir; ++dd) {
-        const int d = dd == 0 ? dA : dB;
+        // (dB is -1 in the single-direction phase of an odd dimension; d never
+        // takes that value, even where a compiler evaluates this ahead of the
+        // loop bound, so cc[d] and opx[d] always index inside their arrays)
+        const int d = (dd == 0 || dB < 0) ? dA : dB;
         const int st = dd == 0 ? strideA : strideB;   // along the line
         const int lst = dd == 0 ? strideB : strideA;  // between the lines
         const LineOp<f32x2>& L = P.opx[d];
@@ -573,13 +610,15 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
         const double* const fs = trace_src<NC, N>(P, nb, L.nb_node, &fo);
         const double* face = fs + (fo + L.nb_node * st);
         int l = rot;
-        double upn = nb >= 0 ? __ldg(face + base + l * lst) : 0.0;
+        const long long fbase = fo + L.nb_node * st;  // index of `face` relative to fs
+        double upn = nb >= 0 && checked<NC, N>(P, fs, fbase + base + l * lst) ? __ldg(face + base + l * lst) : 0.0;
 #pragma unroll 1
         for (int j = 0; j < nl; ++j) {
           const int lb = base + l * lst;
           const double upd = upn;
           l = l + 1 < nl ? l + 1 : 0;
-          if (nb >= 0 && j + 1 < nl) upn = __ldg(face + base + l * lst);  // next line's trace
+          if (nb >= 0 && j + 1 < nl && checked<NC, N>(P, fs, fbase + base + l * lst))
+            upn = __ldg(face + base + l * lst);  // next line's trace
           f32x2 u[N], acc[N];
           if ((N % 2) == 0 && st == 1) {
 #pragma unroll
@@ -635,6 +674,7 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
               const int node = lb + i * st;
               const long long gi = g0 + node;
               const double k = x2_to_double(acc[i]);
+              if (!checked<NC, N>(P, P.tin, gi)) continue;
               if constexpr (MODE == kApply) {
                 P.uout[gi] = k;
               } else {
@@ -690,7 +730,8 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
   const long long nblk = (P.c_hi - P.c_lo + cpb - 1) / cpb;
   auto stage = [&](T* dst, T* dstu, long long blk) {
     const long long c0 = P.c_lo + blk * cpb;
-    const long long ncell = (P.c_hi - c0) < cpb ? (P.c_hi - c0) : cpb;
+    long long ncell = (P.c_hi - c0) < cpb ? (P.c_hi - c0) : cpb;
+    if (!checked<NC, N>(P, P.tin, (c0 + ncell) * NC - 1)) ncell = 0;
     stage_cells<D, N, T>(dst, P.tin + c0 * NC, ncell, tid, nthr);
     if constexpr (SU) stage_cells<D, N, T>(dstu, P.uin + c0 * NC, ncell, tid, nthr);
   };
@@ -818,7 +859,10 @@ void set_last_error(const char* msg);
 // 3x+3v meshes; err receives a device error code on a bounded-wait time-out;
 // ticket is a device int the launch uses as its row counter
 bool ecl6_eligible(const EclParams<float>& P);
-cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int* ticket, int mode, cudaStream_t stream);
+// wait_limit: try_wait rounds of the bounded waits (0: the default); skip_issue: test
+// hook, nothing is issued for cell skip_issue of the launch's first row (-1: off)
+cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int* ticket, int mode, cudaStream_t stream,
+                        unsigned wait_limit = 0, int skip_issue = -1);
 
 // defined in hd_ecl_d{2..6}.cu
 EclLaunchers ecl_launchers_d2(int N);

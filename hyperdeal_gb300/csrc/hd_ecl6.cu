@@ -77,9 +77,12 @@ bool ecl6_eligible(const EclParams<float>& P) {
   return true;
 }
 
-cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int* ticket, int mode, cudaStream_t stream) {
+cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int* ticket, int mode, cudaStream_t stream,
+                        unsigned wait_limit, int skip_issue) {
   Ecl6Params E;
   E.p = P;
+  E.wait_limit = wait_limit ? wait_limit : E6_WAIT_LIMIT;
+  E.skip_issue = skip_issue;
   E.row_len = P.cells[0];
   // parts hold whole layers of v2, so every boundary below falls on a row
   E.row_lo = int(P.c_lo / P.cells[0]);

@@ -79,9 +79,9 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
 }
 
 // bounded wait for the phase with the given parity; false on time-out
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = E6_WAIT_LIMIT) {
   const uint32_t a = smem_u32(bar);
-  for (uint32_t it = 0; it < E6_WAIT_LIMIT; ++it) {
+  for (uint32_t it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
@@ -155,7 +155,28 @@ struct Ecl6Params {
   int lay0, lay1;      // this part's layers [lay0, lay1) of direction v2
   int* err;            // device error flag
   int* ticket;         // next unclaimed row (zeroed before every launch)
+  unsigned wait_limit; // try_wait rounds of every bounded wait (E6_WAIT_LIMIT)
+  int skip_issue;      // test hook (hd_adv_set_wait_test): the producer holding the launch's
+                       // first row (always some CTA's first claim) issues nothing for cell
+                       // skip_issue of that row (-1: off), so that the compute warps' wait
+                       // for that slot runs out
 };
+
+// Cell index c checked against [0, n) in builds with -DHD_CHECK: outside, the
+// violation is recorded (kCheckError) and cell 0 is used instead, so that the
+// copy or access stays valid and the barrier accounting intact.
+__device__ __forceinline__ long long e6_checked(const Ecl6Params& P, long long c, long long n) {
+#ifdef HD_CHECK
+  if (c < 0 || c >= n) {
+    atomicExch(P.err, kCheckError);
+    return 0;
+  }
+#else
+  (void)P;
+  (void)n;
+#endif
+  return c;
+}
 
 // first (local) cell id of row r and the upwind-neighbour offsets (in cells)
 // of the row's cells in directions 1..5 (inside a row only x0 varies); ghost5:
@@ -250,7 +271,7 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
       if (r < 0) mbar_arrive(&full[0]);  // no row for this CTA: release the compute warps
       for (int it = 0; r >= 0; ++it) {
         const int s = it % E6_STAGES;
-        if (it >= E6_STAGES && !mbar_wait(&empty[s], ((it / E6_STAGES) - 1) & 1)) {
+        if (it >= E6_STAGES && !mbar_wait(&empty[s], ((it / E6_STAGES) - 1) & 1, P.wait_limit)) {
           atomicExch(P.err, E6_ERR_TIMEOUT_EMPTY);
           *s_abort = 1;
           ok = false;
@@ -265,23 +286,38 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
         }
         const long long gid = e6_cell(P, R.first, k);
         float* st = s_stage + s * E6_STAGE_FLOATS;
+        if (k == P.skip_issue && R.first == (long long)P.row_lo * P.row_len) {
+          // test hook: nothing arrives on this slot, its consumers' bounded wait runs out
+          ++issued;
+          if (++k == P.row_len) {
+            k = 0;
+            ++q;
+          }
+          continue;
+        }
+        const long long nc = P.p.n_cells;
+        const long long gc = e6_checked(P, gid, nc);
         mbar_arrive_expect_tx(&full[s], bytes);
-        tma_load_2d(st, &maps.tcell, 0, int(gid * 128), &full[s]);
+        tma_load_2d(st, &maps.tcell, 0, int(gc * 128), &full[s]);
         // U is read once per stage: evict it first, so that L2 keeps the stage
         // input T, whose faces the neighbours read again later
-        if (READ_U) tma_load_2d_hint(st + 4096, &maps.ucell, 0, int(gid * 128), &full[s], pol_u);
+        if (READ_U) tma_load_2d_hint(st + 4096, &maps.ucell, 0, int(gc * 128), &full[s], pol_u);
         if (P.p.op[2].active)
-          tma_load_3d(st + 8192, &maps.tx2, 0, P.p.op[2].nb_node, int((gid + R.nb[2]) * 64), &full[s]);
+          tma_load_3d(st + 8192, &maps.tx2, 0, P.p.op[2].nb_node, int(e6_checked(P, gid + R.nb[2], nc) * 64),
+                      &full[s]);
         if (P.p.op[3].active)
-          tma_load_3d(st + 9216, &maps.tv0, 0, P.p.op[3].nb_node, int((gid + R.nb[3]) * 16), &full[s]);
+          tma_load_3d(st + 9216, &maps.tv0, 0, P.p.op[3].nb_node, int(e6_checked(P, gid + R.nb[3], nc) * 16),
+                      &full[s]);
         if (P.p.op[4].active)
-          tma_load_3d(st + 10240, &maps.tv1, 0, P.p.op[4].nb_node, int((gid + R.nb[4]) * 4), &full[s]);
-          if (P.p.op[5].active) {
+          tma_load_3d(st + 10240, &maps.tv1, 0, P.p.op[4].nb_node, int(e6_checked(P, gid + R.nb[4], nc) * 4),
+                      &full[s]);
+        if (P.p.op[5].active) {
           // the v2 face: the neighbour's slab, or its face in the ghost region
           // (a part's layer starts at a multiple of the layer size, so the
           // neighbour's in-layer slot is this cell's)
-          const float* src5 = R.ghost5 ? P.p.ghost + (gid % P.p.layer) * 1024
-                                       : P.p.tin + (gid + R.nb[5]) * 4096 + P.p.op[5].nb_node * 1024;
+          const float* src5 =
+              R.ghost5 ? P.p.ghost + e6_checked(P, gid % P.p.layer, P.p.layer) * 1024
+                       : P.p.tin + e6_checked(P, gid + R.nb[5], nc) * 4096 + P.p.op[5].nb_node * 1024;
           bulk_load(st + 11264, src5, 4096u, &full[s]);
         }
         ++issued;
@@ -293,7 +329,7 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
       // on an abort, wait (bounded) for the copies still in flight before leaving
       if (!ok) {
         for (int it = issued - E6_STAGES < 0 ? 0 : issued - E6_STAGES; it < issued; ++it)
-          mbar_wait(&full[it % E6_STAGES], (it / E6_STAGES) & 1);
+          mbar_wait(&full[it % E6_STAGES], (it / E6_STAGES) & 1, P.wait_limit);
       }
     }
     return;
@@ -331,11 +367,12 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
   float4 px1 = make_float4(0.f, 0.f, 0.f, 0.f);  // x1 face values of this thread's plane
   auto fetch_x1 = [&](long long g, int nb1) {
     if (L[1].active)
-      px1 = __ldg(reinterpret_cast<const float4*>(P.p.tin + (g + nb1) * NC + 16 * tid + 4 * L[1].nb_node));
+      px1 = __ldg(reinterpret_cast<const float4*>(P.p.tin + e6_checked(P, g + nb1, P.p.n_cells) * NC + 16 * tid +
+                                                  4 * L[1].nb_node));
   };
 
   // the first cell (or the producer's "no row" signal) decides whether there is work
-  if (lane == 0 && !mbar_wait(&full[0], 0)) {
+  if (lane == 0 && !mbar_wait(&full[0], 0, P.wait_limit)) {
     *s_abort = 1;
     atomicExch(P.err, E6_ERR_TIMEOUT_FULL);
   }
@@ -355,14 +392,14 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
     // row start: x0 face of the upwind neighbour of the row's first cell (periodic wrap)
     if (k == 0 && L[0].active) {
       const long long g0 = R.first + (L[0].step < 0 ? P.row_len - 1 : 0);
-      const float* src = P.p.tin + g0 * NC + 16 * tid + L[0].nb_node;
+      const float* src = P.p.tin + e6_checked(P, g0, P.p.n_cells) * NC + 16 * tid + L[0].nb_node;
 #pragma unroll
       for (int b = 0; b < 4; ++b) carry[b] = __ldg(src + 4 * b);
     }
 
     // one lane per warp waits for the slot (bounded); a time-out turns the rest
     // of the CTA's work into no-ops (no stores) without leaving any barrier
-    if (lane == 0 && !*s_abort && !mbar_wait(&full[s], (it / E6_STAGES) & 1)) {
+    if (lane == 0 && !*s_abort && !mbar_wait(&full[s], (it / E6_STAGES) & 1, P.wait_limit)) {
       *s_abort = 1;
       atomicExch(P.err, E6_ERR_TIMEOUT_FULL);
     }
@@ -545,7 +582,13 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
 #pragma unroll
         for (int b = 0; b < 4; ++b) so[ob2[a & 1] + 256 * a + 1024 * b] = acc[a][b];
       __syncwarp();
-      if (!*s_abort) {
+#ifdef HD_CHECK
+      const bool store_ok = gid >= P.p.c_lo && gid < P.p.c_hi;
+      if (!store_ok) atomicExch(P.err, kCheckError);
+#else
+      constexpr bool store_ok = true;
+#endif
+      if (!*s_abort && store_ok) {
         float4* go = reinterpret_cast<float4*>(P.p.uout + gid * NC + vnode);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {

@@ -49,6 +49,8 @@ struct hd_adv {
   int gauss;           // 1: Gauss quadrature (non-collocation) path
   hd_part_layout part; // v-slab part of a partitioned operator (n_parts = 1: the whole mesh)
   int n_parts, part_index;
+  unsigned wait_limit;  // pipelined kernel: try_wait rounds of its bounded waits (0: default)
+  int skip_issue;       // pipelined kernel test hook (hd_adv_set_wait_test; -1: off)
   GaussTables gt;
   hd::GaussExtra<double> g64;
   hd::GaussExtra<float> g32;

@@ -56,17 +56,41 @@ __global__ void moment_partials(VpGeom g, const T* __restrict__ f, const double*
       const long long gvc = gv < g.ncv ? gv : g.ncv - 1;  // valid address even if loaded unconditionally
       vals[k] = gv < g.ncv ? __ldg(f + (gxc + g.ncx * gvc) * g.NC + node) : T(0);
     }
-    // FP32 storage: the chunk is summed pairwise in FP32 (the FP64 pipe is the
-    // scarce resource here; the values carry FP32 precision anyway);
-    // FP64 storage: summed in FP64
-    T h[kMomChunk];
+    double chunk_sum;
+    if constexpr (sizeof(T) == 4) {
+      // FP32 storage: compensated pairwise sum on the FP32 pipe (the FP64 pipe
+      // is the scarce resource here): every pairwise add is Knuth's TwoSum,
+      // whose rounding error is kept in a second float and summed alongside,
+      // so the chunk sum hi + lo carries about twice FP32's precision before
+      // it is widened to FP64 (Ogita, Rump, Oishi, SIAM J. Sci. Comput. 2005)
+      float hi[kMomChunk], lo[kMomChunk];
 #pragma unroll
-    for (int k = 0; k < kMomChunk; ++k) h[k] = vals[k];
+      for (int k = 0; k < kMomChunk; ++k) {
+        hi[k] = vals[k];
+        lo[k] = 0.f;
+      }
 #pragma unroll
-    for (int w = kMomChunk / 2; w > 0; w /= 2)
+      for (int w = kMomChunk / 2; w > 0; w /= 2)
 #pragma unroll
-      for (int k = 0; k < w; ++k) h[k] += h[k + w];
-    sh[node] = double(h[0]) * wv[node / g.NCx];
+        for (int k = 0; k < w; ++k) {
+          float sum, err;
+          two_sum(hi[k], hi[k + w], sum, err);
+          hi[k] = sum;
+          lo[k] = __fadd_rn(__fadd_rn(lo[k], lo[k + w]), err);
+        }
+      chunk_sum = x2_to_double(f32x2{hi[0], lo[0]});
+    } else {
+      // FP64 storage: summed pairwise in FP64
+      T h[kMomChunk];
+#pragma unroll
+      for (int k = 0; k < kMomChunk; ++k) h[k] = vals[k];
+#pragma unroll
+      for (int w = kMomChunk / 2; w > 0; w /= 2)
+#pragma unroll
+        for (int k = 0; k < w; ++k) h[k] += h[k + w];
+      chunk_sum = double(h[0]);
+    }
+    sh[node] = chunk_sum * wv[node / g.NCx];
   }
   __syncthreads();
   for (int ix = threadIdx.x; ix < g.NCx; ix += blockDim.x) {

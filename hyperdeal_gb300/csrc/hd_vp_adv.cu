@@ -294,7 +294,8 @@ __device__ __forceinline__ void vp_block_x2(const VpAdvParams<double>& P, const 
       const int base = item_base<D, N>(item, dA, dB);
 #pragma unroll 1
       for (int dd = 0; dd < ndir; ++dd) {
-        const int d = dd == 0 ? dA : dB;
+        // (never the -1 of a single-direction phase, even if evaluated ahead of the bound)
+        const int d = (dd == 0 || dB < 0) ? dA : dB;
         const int st = dd == 0 ? strideA : strideB;   // along the line
         const int lst = dd == 0 ? strideB : strideA;  // between the lines
         const bool first = ph == 0 && dd == 0;

@@ -1,8 +1,9 @@
-"""Replica timing for ``bench.py --gpus N`` (one process per GPU, launched by
-torchrun): every rank advances its own copy of the problem (the path shards
-into independent replicas here -- no collective on the data path); the timed
-region is bracketed by a barrier and a device synchronisation on both sides
-and the reported time is the maximum over the ranks.
+"""Rank bookkeeping and timing for ``bench.py --gpus N`` (one process per GPU,
+launched by torchrun): every rank advances its own part of the problem (a
+v-slab of the partitioned operator, hyperdeal_gb300/partition.py, whose ghost
+faces it exchanges with its neighbours once per stage); the timed region is
+bracketed by a barrier and a device synchronisation on both sides and the
+reported time is the maximum over the ranks.
 
 The same helpers run with the ``gloo`` backend and a host clock, which is how
 the multi-rank logic is tested without GPUs.

@@ -151,10 +151,22 @@ enum hd_arithmetic { HD_ARITH_NATIVE = 0, HD_ARITH_FP32X2 = 1 };
 int hd_adv_set_arithmetic(hd_adv *op, int arithmetic);
 int hd_adv_arithmetic(const hd_adv *op);
 
-/* Device-side error code of the pipelined kernel since the last call (0 = none;
- * 1/2 = a bounded wait on a copy / buffer slot timed out and the kernel
- * returned early).  Synchronises the device; clears the flag. */
+/* Device-side error code since the last call (0 = none; 1/2 = a bounded wait
+ * of the pipelined kernel on a copy / buffer slot timed out and the kernel
+ * returned early; 4 = a bounds check failed and the access was skipped, in a
+ * library built with -DHD_CHECK only).  Synchronises the device; clears the
+ * flag. */
 int hd_adv_device_status(hd_adv *op, int *status);
+
+/* Test hook of the bounded waits (no reference counterpart): wait_limit sets
+ * the try_wait rounds of every bounded wait of the pipelined kernel (0 = the
+ * default, about seconds), and skip_issue >= 0 makes the producer warp that
+ * claims the launch's first row of cells issue nothing for cell skip_issue of
+ * that row (0 <= skip_issue < cells in x0), so that the compute warps' wait
+ * for that slot runs out: the kernel records status 1 or 2, stops that CTA's
+ * remaining work without stores, waits (bounded) for its own copies in flight
+ * and returns.  skip_issue = -1 turns the hook off.  Nothing faults or hangs. */
+int hd_adv_set_wait_test(hd_adv *op, unsigned wait_limit, int skip_issue);
 
 /* dst = M^{-1} A(src) at `time` (boundary data time), i.e.
  * AdvectionOperation::apply<all>(dst, src, time) in its ECL branch

@@ -69,7 +69,7 @@ def test_noalloc_rejects_meshes_above_its_scratch():
 
 def test_noalloc_at_its_size_limit():
     """134,217,728 DoFs exactly (3x+3v, k=3, 32,768 cells): 16,384 block partials, the whole scratch."""
-    params, f = _case(3, 3, [8, 8, 8, 8, 8, 2], "f32")
+    params, f = _case(3, 3, [8, 8, 8, 8, 4, 2], "f32")
     op = A.AdvectionOperation(params)
     assert op.n_dofs == 134217728
     v = op.initialize_dof_vector()
