@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "../../include/hyperdeal_gb300.h"
 #include "hd_ecl.cuh"
@@ -264,7 +265,9 @@ struct PoissonArgs {
   double* r;
   double* p;
   double* Ap;
-  double* red;            // [2][gridDim] partial sums
+  double* red;            // [2][3 gridDim] partial sums
+  double* z;              // preconditioned residual (the residual itself without a preconditioner)
+  const double* binv;     // cell-block Jacobi: inverse of every x-cell's diagonal block (NCx x NCx), or null
   double rel_tol;
   int rhs_relative;       // 1: stop at ||r|| <= rel_tol ||rhs||; 0: at rel_tol ||r_0||
   int max_iter;
@@ -301,13 +304,62 @@ __device__ double2 grid_sum2(cgrp::grid_group& grid, double v0, double v1, doubl
   return make_double2(__shfl_sync(0xffffffffu, s0, 0), __shfl_sync(0xffffffffu, s1, 0));
 }
 
+// the same for three values (the preconditioned CG's (r,z), (Az,z) and (r,r))
+__device__ double3 grid_sum3(cgrp::grid_group& grid, double v0, double v1, double v2, double* red, int& slot,
+                             double* sh) {
+  const double b0 = block_sum(v0, sh);
+  const double b1 = block_sum(v1, sh);
+  const double b2 = block_sum(v2, sh);
+  double* part = red + slot * 3 * gridDim.x;
+  if (threadIdx.x == 0) {
+    part[3 * blockIdx.x] = b0;
+    part[3 * blockIdx.x + 1] = b1;
+    part[3 * blockIdx.x + 2] = b2;
+  }
+  grid.sync();
+  const int lane = threadIdx.x & 31;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (int k = lane; k < (int)gridDim.x; k += 32) {
+    s0 += __ldcg(part + 3 * k);
+    s1 += __ldcg(part + 3 * k + 1);
+    s2 += __ldcg(part + 3 * k + 2);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, o);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    s2 += __shfl_down_sync(0xffffffffu, s2, o);
+  }
+  slot ^= 1;
+  return make_double3(__shfl_sync(0xffffffffu, s0, 0), __shfl_sync(0xffffffffu, s1, 0),
+                      __shfl_sync(0xffffffffu, s2, 0));
+}
+
+// z_i = sum_j B^{-1}_c[i][j] r_j over the rows j of row i's x-cell c
+__device__ __forceinline__ double block_jacobi_row(const VpGeom& g, const double* __restrict__ binv,
+                                                   const double* r, long long i) {
+  const long long c = i / g.NCx;
+  const int il = int(i - c * g.NCx);
+  const double* B = binv + (c * g.NCx + il) * g.NCx;
+  const double* rc = r + c * g.NCx;
+  double z = 0.0;
+  for (int j = 0; j < g.NCx; ++j) z = fma(__ldg(B + j), __ldcg(rc + j), z);
+  return z;
+}
+
 // One cooperative launch per solve (or two around the learned guess):
 // rho and the right-hand side (application.h:531-568: rho~ = rho - mean,
 // rhs = -M rho~, rhs -= mean), conjugate gradients on the SIPG system, and
 // the field E = grad(phi) at the x-nodes (derivative_container.h:158-251).
-// CG is the Chronopoulos-Gear form (one fused reduction of (r,r) and (Ar,r)
-// per iteration: two grid barriers instead of three); in exact arithmetic
-// it produces the iterates of plain CG.
+// CG is the Chronopoulos-Gear form (one fused reduction of (r,z), (Az,z)
+// and (r,r) per iteration: two grid barriers instead of three); in exact
+// arithmetic it produces the iterates of plain CG, preconditioned by
+// z = B^{-1} r with B the block diagonal of the x-cells (cell-block Jacobi)
+// or unpreconditioned (z = r).  The reference preconditions its CG as well,
+// with geometric multigrid (examples/vlasov_poisson/include/poisson.h:612-742).
+// The preconditioner needs the residual of the row's cell only; when the
+// block size is a multiple of the cell's DoFs every block holds whole cells
+// (rows are handed out in block-sized chunks), so a block barrier suffices,
+// otherwise a grid barrier separates the residual update from z.
 __global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
   cgrp::grid_group grid = cgrp::this_grid();
   __shared__ double sh[32];
@@ -342,31 +394,43 @@ __global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
   if (!(A.phases & 2)) return;
   double* const r = A.r;
   double* const p = A.p;
-  double* const w = A.Ap;    // A r
+  double* const w = A.Ap;    // A z
   double* const sv = A.Ap + n;  // A p
+  const bool pre = A.binv != nullptr;
+  double* const z = pre ? A.z : r;
+  const bool block_local = (blockDim.x % g.NCx) == 0;
+  // z = B^{-1} r for this thread's rows, after every residual entry of their cells is written
+  auto precondition = [&]() {
+    if (!pre) return;
+    if (block_local) __syncthreads();
+    else grid.sync();
+    for (long long i = t0; i < n; i += stride) z[i] = block_jacobi_row(g, A.binv, r, i);
+  };
   double lbb = 0.0;
   for (long long i = t0; i < n; i += stride) {
     r[i] = A.rhs[i] - spmv_row(A.W, n, A.col, A.val, A.x, i);
     lbb += A.rhs[i] * A.rhs[i];
   }
-  grid.sync();  // r complete before A r
-  double lrr = 0.0, lwr = 0.0;
+  precondition();
+  grid.sync();  // z complete before A z
+  double lrz = 0.0, lwz = 0.0, lrr = 0.0;
   for (long long i = t0; i < n; i += stride) {
-    const double wi = spmv_row(A.W, n, A.col, A.val, r, i);
+    const double wi = spmv_row(A.W, n, A.col, A.val, z, i);
     w[i] = wi;
+    lrz += r[i] * z[i];
+    lwz += wi * z[i];
     lrr += r[i] * r[i];
-    lwr += wi * r[i];
   }
-  double2 t = grid_sum2(grid, lrr, lwr, A.red, slot, sh);
+  double3 t = grid_sum3(grid, lrz, lwz, lrr, A.red, slot, sh);
   const double bb = grid_sum2(grid, lbb, 0.0, A.red, slot, sh).x;
-  double gamma = t.x, delta = t.y;
-  const double r0 = sqrt(gamma);
+  double gamma = t.x, delta = t.y, rnorm = sqrt(t.z);
+  const double r0 = rnorm;
   const double stop = A.rhs_relative ? A.rel_tol * sqrt(bb) : fmax(A.rel_tol * r0, 1e-14 * sqrt(bb));
   int it = 0;
   double alpha = delta > 0.0 ? gamma / delta : 0.0, beta = 0.0;
-  while (sqrt(gamma) > stop && it < A.max_iter && alpha > 0.0) {
+  while (rnorm > stop && it < A.max_iter && alpha > 0.0) {
     for (long long i = t0; i < n; i += stride) {
-      const double pi = r[i] + (it ? beta * p[i] : 0.0);
+      const double pi = z[i] + (it ? beta * p[i] : 0.0);
       const double si = w[i] + (it ? beta * sv[i] : 0.0);
       p[i] = pi;
       sv[i] = si;
@@ -374,18 +438,22 @@ __global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
       r[i] -= alpha * si;
     }
     ++it;
-    grid.sync();  // r complete before A r
+    precondition();
+    grid.sync();  // z complete before A z
+    lrz = 0.0;
+    lwz = 0.0;
     lrr = 0.0;
-    lwr = 0.0;
     for (long long i = t0; i < n; i += stride) {
-      const double wi = spmv_row(A.W, n, A.col, A.val, r, i);
+      const double wi = spmv_row(A.W, n, A.col, A.val, z, i);
       w[i] = wi;
+      lrz += r[i] * z[i];
+      lwz += wi * z[i];
       lrr += r[i] * r[i];
-      lwr += wi * r[i];
     }
-    t = grid_sum2(grid, lrr, lwr, A.red, slot, sh);
+    t = grid_sum3(grid, lrz, lwz, lrr, A.red, slot, sh);
     const double gn = t.x;
     delta = t.y;
+    rnorm = sqrt(t.z);
     beta = gn / gamma;
     const double den = delta - beta * gn / alpha;
     alpha = den > 0.0 ? gn / den : 0.0;
@@ -414,7 +482,7 @@ __global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
     A.stats->last_iters = it;
     A.stats->total_iters += it;
     A.stats->solves += 1;
-    A.stats->last_res = r0 > 0.0 ? sqrt(gamma) / r0 : 0.0;
+    A.stats->last_res = r0 > 0.0 ? rnorm / r0 : 0.0;
   }
 }
 
@@ -585,7 +653,8 @@ struct hd_vp {
   double* d_E;
   void* d_xs;         // x-line velocities / h_x in the storage precision
   void* d_es;         // E / h_v in the storage precision
-  double* d_cg;       // r, p, A r, A p (4 * nx) + reductions (2 halves * 2 values * cg_grid)
+  double* d_cg;       // r, p, A z, A p, z (5 * nx) + reductions (2 halves * 3 values * cg_grid)
+  double* d_binv;     // cell-block Jacobi preconditioner: ncx blocks of NCx x NCx (null: none)
   int ell_w;          // SIPG matrix in ELL form (ell_w entries per row, [k][row])
   int* d_ell_col;
   double* d_ell_val;
@@ -694,8 +763,59 @@ void vp_free(hd_vp* v) {
   cudaFree(v->d_dx);
   cudaFree(v->d_dy);
   cudaFree(v->d_judge);
+  cudaFree(v->d_binv);
   hd::vp_model_destroy(v->model);
   delete v;
+}
+
+// Cell-block Jacobi preconditioner: the diagonal block of every x-cell (the
+// entries of its rows whose columns lie in the same cell) read back from the
+// assembled ELL matrix, inverted on the host (Gauss-Jordan with partial
+// pivoting; the SIPG blocks are symmetric positive definite) and uploaded.
+int build_block_jacobi(hd_vp* v) {
+  const hd::VpGeom& g = v->g;
+  const long long nx = g.nx_dofs;
+  const int W = v->ell_w, m = g.NCx;
+  std::vector<int> col(size_t(W) * nx);
+  std::vector<double> val(size_t(W) * nx);
+  cudaError_t e = cudaMemcpy(col.data(), v->d_ell_col, sizeof(int) * col.size(), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(val.data(), v->d_ell_val, sizeof(double) * val.size(), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return vcuda(e, "hd_vp_create: matrix read-back");
+  std::vector<double> inv(size_t(g.ncx) * m * m);
+  std::vector<double> a(size_t(m) * 2 * m);
+  for (long long c = 0; c < g.ncx; ++c) {
+    std::fill(a.begin(), a.end(), 0.0);
+    for (int i = 0; i < m; ++i) {
+      const long long row = c * m + i;
+      for (int k = 0; k < W; ++k) {
+        const long long j = col[size_t(k) * nx + row];
+        if (j / m == c) a[size_t(i) * 2 * m + (j - c * m)] += val[size_t(k) * nx + row];
+      }
+      a[size_t(i) * 2 * m + m + i] = 1.0;
+    }
+    for (int k = 0; k < m; ++k) {
+      int piv = k;
+      for (int i = k + 1; i < m; ++i)
+        if (std::fabs(a[size_t(i) * 2 * m + k]) > std::fabs(a[size_t(piv) * 2 * m + k])) piv = i;
+      if (!(std::fabs(a[size_t(piv) * 2 * m + k]) > 0.0))
+        return vfail(HD_ERR_INVALID, "hd_vp_create: singular diagonal block of the Poisson matrix");
+      if (piv != k)
+        for (int j = 0; j < 2 * m; ++j) std::swap(a[size_t(k) * 2 * m + j], a[size_t(piv) * 2 * m + j]);
+      const double d = 1.0 / a[size_t(k) * 2 * m + k];
+      for (int j = 0; j < 2 * m; ++j) a[size_t(k) * 2 * m + j] *= d;
+      for (int i = 0; i < m; ++i) {
+        if (i == k) continue;
+        const double f = a[size_t(i) * 2 * m + k];
+        if (f != 0.0)
+          for (int j = 0; j < 2 * m; ++j) a[size_t(i) * 2 * m + j] -= f * a[size_t(k) * 2 * m + j];
+      }
+    }
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) inv[(size_t(c) * m + i) * m + j] = a[size_t(i) * 2 * m + m + j];
+  }
+  e = cudaMalloc(&v->d_binv, sizeof(double) * inv.size());
+  if (e == cudaSuccess) e = cudaMemcpy(v->d_binv, inv.data(), sizeof(double) * inv.size(), cudaMemcpyHostToDevice);
+  return vcuda(e, "hd_vp_create: preconditioner");
 }
 
 hd::PoissonArgs poisson_args(hd_vp* v, int phases) {
@@ -714,7 +834,9 @@ hd::PoissonArgs poisson_args(hd_vp* v, int phases) {
   A.r = v->d_cg;
   A.p = v->d_cg + nx;
   A.Ap = v->d_cg + 2 * nx;
-  A.red = v->d_cg + 4 * nx;
+  A.z = v->d_cg + 4 * nx;
+  A.red = v->d_cg + 5 * nx;
+  A.binv = v->d_binv;
   A.rel_tol = v->desc.cg_tol;
   A.rhs_relative = v->desc.cg_rhs_relative;
   A.max_iter = v->desc.cg_max_iter;
@@ -815,6 +937,8 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
   if (!(d.cg_tol > 0.0) || d.cg_max_iter < 1) return vfail(HD_ERR_INVALID, "hd_vp_create: cg_tol > 0, cg_max_iter >= 1");
   if (d.guess < HD_VP_GUESS_ZERO || d.guess > HD_VP_GUESS_LEARNED)
     return vfail(HD_ERR_INVALID, "hd_vp_create: unknown guess");
+  if (d.cg_precond != HD_VP_PRECOND_NONE && d.cg_precond != HD_VP_PRECOND_BLOCK_JACOBI)
+    return vfail(HD_ERR_INVALID, "hd_vp_create: unknown preconditioner");
   hd_vp* v = new (std::nothrow) hd_vp;
   if (!v) return vfail(HD_ERR_ALLOC, "out of host memory");
   std::memset(v, 0, sizeof(*v));
@@ -886,7 +1010,7 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
   alloc((void**)&v->d_E, sizeof(double) * nx * g.dx);
   alloc(&v->d_es, sizeof(double) * nx * g.dx);
   alloc(&v->d_xs, sizeof(double) * g.dx * 64 * hd::kMaxN);
-  alloc((void**)&v->d_cg, sizeof(double) * (4 * nx + 4 * v->cg_grid));
+  alloc((void**)&v->d_cg, sizeof(double) * (5 * nx + 6 * v->cg_grid));
   v->ell_w = 3 * N * g.dx;
   alloc((void**)&v->d_ell_col, sizeof(int) * size_t(v->ell_w) * nx);
   alloc((void**)&v->d_ell_val, sizeof(double) * size_t(v->ell_w) * nx);
@@ -938,6 +1062,10 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
     if (e == cudaSuccess) e = cudaMemset(v->d_phi, 0, sizeof(double) * nx);
     if (e == cudaSuccess) e = cudaMemset(v->d_E, 0, sizeof(double) * nx * g.dx);
     if (e != cudaSuccess) { vp_free(v); return vcuda(e, "hd_vp_create: init"); }
+  }
+  if (d.cg_precond == HD_VP_PRECOND_BLOCK_JACOBI) {
+    const int rc = build_block_jacobi(v);
+    if (rc) { vp_free(v); return rc; }
   }
   if (d.guess == HD_VP_GUESS_LEARNED) {
     v->model = hd::vp_model_create(nx, d.learn_rank > 0 ? d.learn_rank : 32, d.learn_history > 0 ? d.learn_history : 64);

@@ -52,6 +52,7 @@ class VlasovPoissonParameters:
     learn_history: int = 0
     cg_rhs_relative: bool = False  # False: ||r|| <= cg_tol ||r_0|| as deal.II's ReductionControl
     learn_every: int = 0  # Adam steps every n-th solve (0: every solve)
+    cg_precond: str = "block_jacobi"  # "none" or "block_jacobi" (x-cell diagonal blocks of the SIPG matrix)
 
     def c(self) -> _lib.hd_vp_desc:
         d = _lib.hd_vp_desc()
@@ -70,6 +71,8 @@ class VlasovPoissonParameters:
         d.learn_history = int(self.learn_history)
         d.cg_rhs_relative = int(bool(self.cg_rhs_relative))
         d.learn_every = int(self.learn_every)
+        d.cg_precond = {"none": _lib.HD_VP_PRECOND_NONE, "block_jacobi": _lib.HD_VP_PRECOND_BLOCK_JACOBI}[
+            self.cg_precond]
         return d
 
 

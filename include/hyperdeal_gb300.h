@@ -377,6 +377,13 @@ enum hd_vp_guess {
                                PREVIOUS by the initial residual               */
 };
 
+/* Preconditioner of the Poisson CG.  The reference preconditions its CG
+ * with geometric multigrid and a Chebyshev smoother (examples/vlasov_poisson/
+ * include/poisson.h:612-742); here the x-cells' diagonal blocks of the SIPG
+ * matrix are inverted once (cell-block Jacobi), which damps the high-frequency
+ * error that FP32 round-off in the density carries into the right-hand side. */
+enum hd_vp_precond { HD_VP_PRECOND_NONE = 0, HD_VP_PRECOND_BLOCK_JACOBI = 1 };
+
 typedef struct hd_vp_desc {
   int dim_x, dim_v, degree, dtype;
   int cells_x[3], cells_v[3];
@@ -394,6 +401,7 @@ typedef struct hd_vp_desc {
   int learn_every;      /* the learned guess stores every solve's pair and
                            takes its Adam steps every learn_every-th solve
                            (0: 1, every solve)                                */
+  int cg_precond;       /* enum hd_vp_precond (0: none)                       */
 } hd_vp_desc;
 
 typedef struct hd_vp hd_vp;

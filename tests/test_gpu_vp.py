@@ -21,13 +21,14 @@ if torch.cuda.is_available():
     from hyperdeal_gb300 import vlasov_poisson as V  # noqa: E402
 
 
-def _setup(dim_x, degree, cx, cv, dtype="f64", guess="previous", cg_tol=1e-12, rhs_relative=False):
+def _setup(dim_x, degree, cx, cv, dtype="f64", guess="previous", cg_tol=1e-12, rhs_relative=False,
+           cg_precond="block_jacobi"):
     D = 2 * dim_x
     lo = [0.0] * dim_x + [-6.0] * dim_x
     hi = [4 * math.pi] * dim_x + [6.0] * dim_x
     params = V.VlasovPoissonParameters(dim_x, degree, [cx] * dim_x, [cv] * dim_x, lo[:dim_x], hi[:dim_x],
                                        lo[dim_x:], hi[dim_x:], dtype=dtype, cg_tol=cg_tol, guess=guess,
-                                       cg_rhs_relative=rhs_relative)
+                                       cg_rhs_relative=rhs_relative, cg_precond=cg_precond)
     prob = O.Problem(dim_x, dim_x, degree, [cx] * dim_x + [cv] * dim_x, lo, hi, [1.0] * dim_x + [6.0] * dim_x,
                      collocation=True)
     assert len(lo) == D
@@ -283,3 +284,23 @@ def test_learned_guess_saves_iterations():
         if guess == "learned":
             assert st1["learned_picked"] - st0["learned_picked"] > 0
     assert per_solve["learned"] < per_solve["previous"], per_solve
+
+
+@pytest.mark.parametrize("dim_x,degree,cx,cv", [(1, 3, 8, 8), (2, 3, 4, 6), (2, 2, 3, 5), (3, 2, 2, 2)])
+def test_block_jacobi_preconditioner_same_potential_fewer_iterations(dim_x, degree, cx, cv):
+    """The cell-block Jacobi preconditioned CG (x-cell diagonal blocks of the SIPG matrix) meets the same
+    accuracy, ||A phi - rhs|| <= tol ||rhs||, gives the same potential as unpreconditioned CG to that
+    accuracy, and needs fewer iterations; degree 2 in 2D (9 DoFs per x-cell, not a divisor of the block
+    size) takes the grid-barrier variant of the preconditioner step."""
+    out = {}
+    for pre in ("none", "block_jacobi"):
+        op, prob = _setup(dim_x, degree, cx, cv, guess="zero", cg_tol=1e-11, rhs_relative=True, cg_precond=pre)
+        f = op.initialize_dof_vector()
+        op.interpolate(V.perturbed_maxwellian(dim_x, eps=0.05, perturbed_dims=tuple(range(dim_x))), f)
+        op.solve_field(f)
+        rho, phi, _ = (t.cpu().numpy() for t in op.fields())
+        rhs = O.poisson_rhs(prob, rho)
+        assert np.linalg.norm(O.poisson_apply(prob, phi) - rhs) <= 1.01e-11 * np.linalg.norm(rhs)
+        out[pre] = (phi - phi.mean(), op.cg_stats()["last_iterations"])
+    assert _rel(out["block_jacobi"][0], out["none"][0]) <= 1e-8
+    assert out["block_jacobi"][1] < out["none"][1], out
