@@ -459,6 +459,16 @@ __global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
     alpha = den > 0.0 ? gn / den : 0.0;
     gamma = gn;
   }
+  if (pre) {
+    // the block preconditioner does not keep the iterates orthogonal to the
+    // constants (the null space of the periodic problem); the residual never
+    // sees that component, so it is removed once at the end: phi mean-free
+    grid.sync();
+    double lx = 0.0;
+    for (long long i = t0; i < n; i += stride) lx += A.x[i];
+    const double mean_x = grid_sum2(grid, lx, 0.0, A.red, slot, sh).x / double(n);
+    for (long long i = t0; i < n; i += stride) A.x[i] -= mean_x;
+  }
   grid.sync();  // x complete before the field reads it
   const int N = g.N;
   for (long long i = t0; i < n; i += stride) {

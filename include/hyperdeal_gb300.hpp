@@ -13,6 +13,9 @@
 //   VlasovPoissonOperation (the right-hand side of the Vlasov-Poisson
 //   application: moments, Poisson solve, field, advection)
 //       examples/vlasov_poisson/include/application.h:516-602
+//   PartitionedAdvectionOperation + GhostExchange (a rank's part of the
+//   distributed operator and its ghost-face update)
+//       include/hyper.deal/matrix_free/vector_partitioner.h:1385-1607
 //
 // Vectors are DeviceVector<Number> (device memory, the reference's DoF
 // numbering).  Errors throw std::runtime_error with hd_last_error()'s message,
@@ -93,7 +96,7 @@ class DeviceVector {
     check_cuda(cudaMemcpy(h, data_, sizeof(Number) * size_t(n_), cudaMemcpyDeviceToHost), "copy to host");
   }
   std::vector<Number> to_host() const {
-    std::vector<Number> v(size_t(n_));
+    std::vector<Number> v(static_cast<size_t>(n_));
     copy_to_host(v.data());
     return v;
   }
@@ -161,6 +164,82 @@ class AdvectionOperation {
  private:
   hd_adv* h_ = nullptr;
   cudaStream_t stream_;
+};
+
+// Ghost-face transport of a partitioned operator.  start() begins sending
+// send_bytes of this part's packed faces to part send_to (if >= 0) and
+// receiving recv_bytes into `ghost` (the ghost region of the vector being
+// exchanged) from part recv_from (if >= 0), after the work already queued on
+// `stream`; finish() makes `stream` wait for both.  An MPI implementation
+// calls MPI_Isend / MPI_Irecv in start (CUDA-aware MPI, or through host
+// buffers after a stream synchronisation) and MPI_Waitall in finish, the way
+// the reference's Contiguous partitioner runs update_ghost_values_start /
+// _finish (include/hyper.deal/matrix_free/vector_partitioner.h:1385-1607).
+class GhostExchange {
+ public:
+  virtual ~GhostExchange() = default;
+  virtual void start(const void* sendbuf, size_t send_bytes, int send_to, void* ghost, size_t recv_bytes,
+                     int recv_from, cudaStream_t stream) = 0;
+  virtual void finish(cudaStream_t stream) = 0;
+};
+
+// One v-slab part of the advection operator (hd_adv_create_part): its vectors
+// hold the part's cells followed by the ghost region of the upwind part's
+// faces.  apply() and LowStorageRungeKuttaIntegrator::perform_time_step
+// exchange the operator input's faces before every evaluation and overlap the
+// exchange with the cells that do not read the ghost region
+// (matrix_free.templates.h:1178-1234, :1494-1581).
+template <typename Number>
+class PartitionedAdvectionOperation {
+ public:
+  PartitionedAdvectionOperation(hd_adv_desc desc, int n_parts, int part, cudaStream_t stream = nullptr)
+      : stream_(stream) {
+    desc.dtype = dtype_of<Number>::value;
+    desc.n_points = desc.degree + 1;
+    check(hd_adv_create_part(&desc, n_parts, part, &h_));
+    check(hd_adv_part_layout(h_, &layout_));
+    if (layout_.send_to >= 0) sendbuf_.reinit(layout_.layer_cells * layout_.face_values);
+  }
+  ~PartitionedAdvectionOperation() { hd_adv_destroy(h_); }
+  PartitionedAdvectionOperation(const PartitionedAdvectionOperation&) = delete;
+  PartitionedAdvectionOperation& operator=(const PartitionedAdvectionOperation&) = delete;
+
+  long long n_dofs() const { return hd_adv_n_dofs(h_); }
+  long long ghost_values() const { return layout_.ghost_values; }
+  const hd_part_layout& layout() const { return layout_; }
+  double critical_time_step() const { return hd_adv_critical_time_step(h_); }
+  DeviceVector<Number> create_vector() const { return DeviceVector<Number>(n_dofs() + ghost_values()); }
+  hd_adv* handle() const { return h_; }
+  cudaStream_t stream() const { return stream_; }
+  // this part's packed faces (valid after pack())
+  const DeviceVector<Number>& send_buffer() const { return sendbuf_; }
+
+  // the steps of an exchange, for drivers that interleave several parts
+  void pack(const DeviceVector<Number>& v) {
+    if (layout_.send_to >= 0) check(hd_adv_pack_faces(h_, v.data(), sendbuf_.data(), stream_));
+  }
+  void exchange_start(GhostExchange& ex, DeviceVector<Number>& v) {
+    ex.start(sendbuf_.data(), sizeof(Number) * size_t(layout_.send_to >= 0 ? sendbuf_.size() : 0), layout_.send_to,
+             v.data() + n_dofs(), sizeof(Number) * size_t(layout_.ghost_values), layout_.recv_from, stream_);
+  }
+  void apply_cells(DeviceVector<Number>& dst, const DeviceVector<Number>& src, const Number time, int cells) const {
+    check(hd_adv_apply_cells(h_, dst.data(), src.data(), double(time), cells, stream_));
+  }
+
+  // dst = M^{-1} A(src): src's ghost region is filled through `ex` first
+  void apply(DeviceVector<Number>& dst, DeviceVector<Number>& src, const Number time, GhostExchange& ex) {
+    pack(src);
+    exchange_start(ex, src);
+    apply_cells(dst, src, time, HD_CELLS_INTERIOR);
+    ex.finish(stream_);
+    apply_cells(dst, src, time, HD_CELLS_BOUNDARY);
+  }
+
+ private:
+  hd_adv* h_ = nullptr;
+  cudaStream_t stream_;
+  hd_part_layout layout_{};
+  DeviceVector<Number> sendbuf_;
 };
 
 // The Vlasov-Poisson right-hand side f -> A(f) with the field of f
@@ -264,6 +343,32 @@ class LowStorageRungeKuttaIntegrator {
     check(hd_vp_lsrk_step_fused(op.handle(), rk_, &s, &k, &t, double(current_time), double(time_step), op.stream()));
     if (s == ki_storage) solution.swap(Ki_);
   }
+
+  // A part of a partitioned operator: the fused step stage by stage, the
+  // stage input's faces exchanged through `ex` before every stage while the
+  // interior cells run; the vectors rotate and are swapped back as above.
+  void perform_time_step(DeviceVector<Number>& solution, const Number current_time, const Number time_step,
+                         PartitionedAdvectionOperation<Number>& op, GhostExchange& ex) {
+    DeviceVector<Number>* X[3] = {&solution, &Ki_, &Ti_};
+    for (int s = 0; s < ns_; ++s) {
+      DeviceVector<Number>& in = *X[hd_lsrk_stage_input(rk_, s)];
+      op.pack(in);
+      op.exchange_start(ex, in);
+      stage(op, s, X, current_time, time_step, HD_CELLS_INTERIOR);
+      ex.finish(op.stream());
+      stage(op, s, X, current_time, time_step, HD_CELLS_BOUNDARY);
+    }
+    solution.swap(Ki_);  // the new solution was accumulated in X[1] = vec_Ki
+  }
+
+  // one stage of the fused step of a part on a cell subset (drivers that
+  // interleave several parts call this between their exchanges)
+  void stage(const PartitionedAdvectionOperation<Number>& op, int s, DeviceVector<Number>* const X[3],
+             const Number current_time, const Number time_step, int cells) const {
+    void* ptr[3] = {X[0]->data(), X[1]->data(), X[2]->data()};
+    check(hd_lsrk_stage(op.handle(), rk_, s, ptr, double(current_time), double(time_step), cells, op.stream()));
+  }
+  int stage_input(int s) const { return hd_lsrk_stage_input(rk_, s); }
 
   // Any operator op(src, dst, t): the reference's stage sequence
   // (time_integrators.templates.h:91-184) with the CUDA vector update.
