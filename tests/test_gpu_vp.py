@@ -297,13 +297,13 @@ def test_block_jacobi_preconditioner_same_potential_fewer_iterations(dim_x, degr
         op, prob = _setup(dim_x, degree, cx, cv, guess="zero", cg_tol=1e-11, rhs_relative=True, cg_precond=pre)
         f = op.initialize_dof_vector()
         op.interpolate(V.perturbed_maxwellian(dim_x, eps=0.05, perturbed_dims=tuple(range(dim_x))), f)
+        # broadband noise in the density (as FP32 round-off brings in): many CG iterations without a preconditioner
+        noise = np.random.default_rng(6).standard_normal(f.numel()) * 1e-3
+        f += torch.tensor(noise, dtype=f.dtype, device="cuda")
         op.solve_field(f)
         rho, phi, _ = (t.cpu().numpy() for t in op.fields())
         rhs = O.poisson_rhs(prob, rho)
         assert np.linalg.norm(O.poisson_apply(prob, phi) - rhs) <= 1.01e-11 * np.linalg.norm(rhs)
         out[pre] = (phi - phi.mean(), op.cg_stats()["last_iterations"])
     assert _rel(out["block_jacobi"][0], out["none"][0]) <= 1e-8
-    if dim_x == 1:  # a handful of iterations either way on the small 1D mesh
-        assert out["block_jacobi"][1] <= out["none"][1], out
-    else:
-        assert out["block_jacobi"][1] < out["none"][1], out
+    assert out["block_jacobi"][1] < out["none"][1], out
