@@ -30,8 +30,7 @@ EXPORTED_SYMBOLS = (
     "hd_adv_autotune", "hd_vp_lsrk_step_fused", "hd_adv_set_arithmetic", "hd_adv_arithmetic",
     "hd_batch_class_arithmetic", "hd_vp_set_arithmetic",
     "hd_part_layout_get", "hd_adv_create_part", "hd_adv_part_layout", "hd_adv_pack_faces", "hd_adv_apply_cells",
-    "hd_lsrk_stage", "hd_lsrk_stage_input", "hd_adv_set_wait_test", "hd_adv_set_face_staging",
-    "hd_adv_face_staging",
+    "hd_lsrk_stage", "hd_lsrk_stage_input", "hd_adv_set_wait_test",
 )
 HD_KERNEL_AUTO, HD_KERNEL_GENERIC, HD_KERNEL_PIPELINED = 0, 1, 2
 HD_ARITH_NATIVE, HD_ARITH_FP32X2 = 0, 1
@@ -179,8 +178,6 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.hd_lsrk_stage.argtypes = [vp, vp, ctypes.c_int, vpp, ctypes.c_double, ctypes.c_double, ctypes.c_int, vp]
     L.hd_lsrk_stage_input.argtypes = [vp, ctypes.c_int]
     L.hd_adv_set_wait_test.argtypes = [vp, ctypes.c_uint, ctypes.c_int]
-    L.hd_adv_set_face_staging.argtypes = [vp, ctypes.c_int]
-    L.hd_adv_face_staging.argtypes = [vp]
     _lib = L
     return L
 

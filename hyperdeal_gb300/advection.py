@@ -193,22 +193,13 @@ class AdvectionOperation:
         c, p, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0.0)
         check(self._L.hd_adv_autotune(self._h, _ptr(src), _ptr(dst), int(reps), ctypes.byref(c), ctypes.byref(p),
                                       ctypes.byref(ms), _stream()))
-        return {"cells_per_cta": c.value, "ctas_per_sm": p.value, "ms_per_apply": ms.value,
-                "face_staging": self.face_staging}
+        return {"cells_per_cta": c.value, "ctas_per_sm": p.value, "ms_per_apply": ms.value}
 
     def tile_limits(self):
         """(max cells per CTA, threads per cell) of the generic kernel for this operator."""
         a, b = ctypes.c_int(0), ctypes.c_int(0)
         check(self._L.hd_adv_tile_limits(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
-
-    def set_face_staging(self, on: bool) -> None:
-        """Stage the upwind face slabs in shared memory with the cells (generic kernel; hd_adv_set_face_staging)."""
-        check(self._L.hd_adv_set_face_staging(self._h, 1 if on else 0))
-
-    @property
-    def face_staging(self) -> bool:
-        return bool(self._L.hd_adv_face_staging(self._h))
 
     def set_wait_test(self, wait_limit: int = 0, skip_issue: int = -1) -> None:
         """Test hook of the pipelined kernel's bounded waits (hd_adv_set_wait_test)."""

@@ -262,7 +262,6 @@ void fill_params(const hd_adv* op, hd::EclParams<T>* P) {
   P->layer = op->part.layer_cells;
   P->ghost = nullptr;
   P->err = nullptr;
-  P->stage_faces = 0;
   for (int i = 0; i < op->N; ++i) P->gl[i] = op->gl[i];
   P->bc_inhom = op->desc.bc_kind == HD_BC_FUNCTION;
   P->bc = to_dev(op->desc.bc);
@@ -659,13 +658,11 @@ int hd_adv_autotune(hd_adv* op, const void* src, void* dst, int reps, int* cells
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     return fail(HD_ERR_CUDA, "hd_adv_autotune: events");
   float best = 1e30f;
-  int best_c = 0, best_p = 0, best_sf = 0, rc = HD_OK;
-  for (int sf : {0, 1})
+  int best_c = 0, best_p = 0, rc = HD_OK;
   for (int c : cands)
     for (int per : {0, 2}) {
       op->p64.cpb = op->p32.cpb = c;
       op->p64.ctas_per_sm = op->p32.ctas_per_sm = per;
-      op->p64.stage_faces = op->p32.stage_faces = sf;
       rc = launch(op, hd::kApply, src, src, dst, nullptr, 0.0, 0.0, 0.0, s);  // warm-up
       if (rc) break;
       cudaEventRecord(e0, s);
@@ -675,13 +672,12 @@ int hd_adv_autotune(hd_adv* op, const void* src, void* dst, int reps, int* cells
       if (cudaEventSynchronize(e1) != cudaSuccess) { rc = fail(HD_ERR_CUDA, "hd_adv_autotune: timing"); break; }
       float t = 0.f;
       cudaEventElapsedTime(&t, e0, e1);
-      if (t < best) { best = t; best_c = c; best_p = per; best_sf = sf; }
+      if (t < best) { best = t; best_c = c; best_p = per; }
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   op->p64.cpb = op->p32.cpb = best_c;
   op->p64.ctas_per_sm = op->p32.ctas_per_sm = best_p;
-  op->p64.stage_faces = op->p32.stage_faces = best_sf;
   if (rc) return rc;
   if (cells_per_cta) *cells_per_cta = best_c;
   if (ctas_per_sm) *ctas_per_sm = best_p;
@@ -722,15 +718,6 @@ int hd_adv_set_arithmetic(hd_adv* op, int arithmetic) {
 }
 
 int hd_adv_arithmetic(const hd_adv* op) { return op ? op->arith : -1; }
-
-int hd_adv_set_face_staging(hd_adv* op, int on) {
-  if (!op) return fail(HD_ERR_INVALID, "hd_adv_set_face_staging: null handle");
-  if (on != 0 && on != 1) return fail(HD_ERR_INVALID, "hd_adv_set_face_staging: 0 or 1");
-  op->p64.stage_faces = op->p32.stage_faces = on;
-  return HD_OK;
-}
-
-int hd_adv_face_staging(const hd_adv* op) { return op ? op->p64.stage_faces : -1; }
 
 int hd_adv_set_wait_test(hd_adv* op, unsigned wait_limit, int skip_issue) {
   if (!op) return fail(HD_ERR_INVALID, "hd_adv_set_wait_test: null handle");

@@ -86,8 +86,6 @@ struct EclParams {
   long long gid0, c_lo, c_hi, layer;
   const T* ghost;
   int* err;  // the operator's device status (bounds-checked builds record violations there)
-  int stage_faces;  // generic kernel: stage the upwind face slabs with the cells (1) or read them
-                    // from global memory inside the line loops (0)
 };
 
 // Device status code of a failed bounds check (builds with -DHD_CHECK only).
@@ -291,92 +289,6 @@ __host__ __device__ constexpr long long ecl_buffer_elems(int cpb) {
   return ((bytes + 15) / 16) * 16 / (long long)sizeof(T);
 }
 
-// Upwind face slabs staged beside the cells: per cell and direction d the
-// neighbour's nb_node slab, NF = N^(D-1) values in the slab's own order (the
-// node index with digit d removed, compress_digit below).  In the cell the
-// slab is N^(D-1-d) runs of N^d contiguous values, run stride N^(d+1).
-template <int D, int N, typename T>
-__host__ __device__ constexpr long long ecl_face_elems(int cpb) {
-  const long long bytes = (long long)cpb * D * ipow(N, D - 1) * sizeof(T);
-  return ((bytes + 15) / 16) * 16 / (long long)sizeof(T);
-}
-// the per-(cell, direction) source offsets of one block's staged faces
-template <int D>
-__host__ __device__ constexpr long long ecl_face_table_bytes(int cpb) {
-  return (((long long)cpb * D * 8 + 15) / 16) * 16;
-}
-
-// node index with its digit of stride pd = N^d removed (pd1 = N^(d+1))
-__device__ __forceinline__ int compress_digit(int node, int pd, int pd1) { return node % pd + (node / pd1) * pd; }
-
-constexpr long long kFaceGhost = 1LL << 62;  // table tag: the offset is into the ghost region
-constexpr long long kFaceNone = -1;          // no neighbour (a domain boundary or an inactive direction)
-
-// Stage the upwind face slabs of the local cells [c0, c0 + ncell) into sf
-// ([cell][direction][NF]): first every (cell, direction) pair's source is
-// resolved once into `table` (the neighbour in this part, or its face in the
-// ghost region), then all threads issue the copies -- 16-byte words where a
-// run of the slab is a whole number of them, element copies otherwise.  The
-// copies join the caller's cp.async group.  Called by every thread.
-template <int D, int N, typename T>
-__device__ __forceinline__ void stage_faces(const EclParams<T>& P, T* sf, long long* table, long long c0,
-                                            long long ncell, int tid, int nthreads) {
-  constexpr int NC = ipow(N, D), NF = ipow(N, D - 1);
-  for (long long idx = tid; idx < ncell * D; idx += nthreads) {
-    const long long c = idx / D;
-    const int d = int(idx - c * D);
-    long long off = kFaceNone;
-    if (P.op[d].active) {
-      const long long gg = P.gid0 + c0 + c;
-      int cc[D];
-      long long gx = gg % P.cstride[P.dim_x], gv = gg / P.cstride[P.dim_x];
-#pragma unroll
-      for (int e = 0; e < D; ++e) {
-        if (e < P.dim_x) { cc[e] = int(gx % P.cells[e]); gx /= P.cells[e]; }
-        else { cc[e] = int(gv % P.cells[e]); gv /= P.cells[e]; }
-      }
-      const long long nb = neighbour(P, gg, cc, d);
-      if (nb >= 0) {
-        long long o = 0;
-        const T* src = trace_src<NC, N>(P, nb, P.op[d].nb_node, &o);
-        int pd = 1;
-        for (int e = 0; e < d; ++e) pd *= N;
-        o += (long long)P.op[d].nb_node * pd;  // run 0 of the slab
-        off = (src == P.ghost && src != P.tin) ? (o | kFaceGhost) : o;
-      }
-    }
-    table[idx] = off;
-  }
-  __syncthreads();
-  const bool al16 = ((reinterpret_cast<uintptr_t>(P.tin) | reinterpret_cast<uintptr_t>(P.ghost)) & 15u) == 0;
-  constexpr int VPW = 16 / sizeof(T);
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    int pd = 1;  // N^d
-    for (int e = 0; e < d; ++e) pd *= N;
-    const int pd1 = pd * N;
-    const bool w16 = al16 && (NC * sizeof(T)) % 16 == 0 && (pd * sizeof(T)) % 16 == 0;
-    const int per = w16 ? NF / VPW : NF;  // copies per slab
-    for (long long idx = tid; idx < ncell * per; idx += nthreads) {
-      const long long c = idx / per;
-      const int k = int(idx - c * per);
-      const long long t = table[c * D + d];
-      if (t == kFaceNone) continue;
-      const T* base = (t & kFaceGhost) ? P.ghost : P.tin;
-      const long long o = t & ~kFaceGhost;
-      T* dst = sf + (c * D + d) * NF;
-      if (w16) {
-        const int cpr = pd / VPW;  // 16-byte words per run
-        const int r = k / cpr, j = k - r * cpr;
-        cp_async_16(dst + r * pd + j * VPW, base + o + (long long)r * pd1 + j * VPW);
-      } else {
-        const int r = k / pd, j = k - r * pd;
-        cp_async_small<sizeof(T)>(dst + k, base + o + (long long)r * pd1 + j);
-      }
-    }
-  }
-}
-
 // stage `ncell` consecutive cells into a shared buffer with the cell stride
 // of EclTile (16-byte copies when the source is 16-byte aligned)
 template <int D, int N, typename T>
@@ -407,7 +319,7 @@ __device__ __forceinline__ void stage_cells(T* dst, const T* src, long long ncel
 // memory next to the operator input, or nullptr to read it from global memory)
 template <int D, int N, typename T, int MODE>
 __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0, int lc, int tl, const T* su_all,
-                                          T* so_all, const T* uu_all, const T* sf_all = nullptr) {
+                                          T* so_all, const T* uu_all) {
   using S = EclShape<D, N, T>;
   constexpr int NC = S::NC, TPC = S::TPC;
   const long long gid = cell0 + lc;  // local cell
@@ -449,10 +361,6 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
     long long oA = 0, oB = 0;
     const T* const sA = trace_src<NC, N>(P, nbA, P.op[dA].nb_node, &oA);
     const T* const sB = dB >= 0 ? trace_src<NC, N>(P, nbB, P.op[dBi].nb_node, &oB) : P.tin;
-    // the staged face slabs of this cell (sf_all: [cell][direction][NF]), when staged
-    constexpr int NF = NC / N;
-    const T* const fA = sf_all ? sf_all + ((long long)lc * D + dA) * NF : nullptr;
-    const T* const fB = sf_all ? sf_all + ((long long)lc * D + dBi) * NF : nullptr;
 
     for (int item = tl; item < nitems; item += TPC) {
       const int base = item_base<D, N>(item, dA, dB);
@@ -463,20 +371,14 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
         T upA[N], upB[N];
 #pragma unroll
         for (int b = 0; b < N; ++b)
-        if (fA) {
-          upA[b] = nbA >= 0 ? fA[compress_digit(base, strideA, strideB) + b * strideA] : T(0);
-        } else {
+        {
           const long long ia = oA + base + LA.nb_node * strideA + b * strideB;
           upA[b] = nbA >= 0 && checked<NC, N>(P, sA, ia) ? __ldg(sA + ia) : T(0);
         }
 #pragma unroll
         for (int a = 0; a < N; ++a) {
-          if (fB) {
-            upB[a] = nbB >= 0 ? fB[compress_digit(base, strideB, strideB * N) + a * strideA] : T(0);
-          } else {
-            const long long ib = oB + base + a * strideA + LB.nb_node * strideB;
-            upB[a] = nbB >= 0 && checked<NC, N>(P, sB, ib) ? __ldg(sB + ib) : T(0);
-          }
+          const long long ib = oB + base + a * strideA + LB.nb_node * strideB;
+          upB[a] = nbB >= 0 && checked<NC, N>(P, sB, ib) ? __ldg(sB + ib) : T(0);
         }
         T uu[N][N], acc[N][N];  // [a][b]: node base + a*strideA + b*strideB
         // phase 0: the plane of directions 0, 1 is N*N contiguous values; when
@@ -589,9 +491,7 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
         // single-direction phase (odd D): lines along dA
         const LineOp<T>& LA = P.op[dA];
         const long long iu = oA + base + LA.nb_node * strideA;
-        const T upf = nbA < 0 ? T(0)
-                      : fA     ? fA[compress_digit(base, strideA, strideA * N)]
-                      : (checked<NC, N>(P, sA, iu) ? __ldg(sA + iu) : T(0));
+        const T upf = nbA >= 0 && checked<NC, N>(P, sA, iu) ? __ldg(sA + iu) : T(0);
         T uu[N], acc[N];
 #pragma unroll
         for (int a = 0; a < N; ++a) {
@@ -653,8 +553,7 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
 // direction 0 (contiguous, 16-byte aligned for even N) are read as 16-byte words.
 template <int D, int N, int MODE>
 __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long long cell0, int lc, int tl,
-                                             const double* su_all, double* so_all, const double* uu_all,
-                                             const double* sf_all = nullptr) {
+                                             const double* su_all, double* so_all, const double* uu_all) {
   using S = EclShape<D, N, double>;
   constexpr int NC = S::NC, TPC = S::TPC;
   constexpr int CST = EclTile<D, N, double>::CST;
@@ -712,21 +611,14 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
         const double* face = fs + (fo + L.nb_node * st);
         int l = rot;
         const long long fbase = fo + L.nb_node * st;  // index of `face` relative to fs
-        // staged slab of this cell and direction: line l's trace at compress(base, d) + l * (its stride there)
-        const double* const sfd = sf_all ? sf_all + ((long long)lc * D + d) * (NC / N) : nullptr;
-        const int fc = compress_digit(base, st, st * N);
-        const int fls = dd == 0 ? strideA : lst;  // the line stride with digit d removed
-        auto trace = [&](int line) -> double {
-          if (sfd) return sfd[fc + line * fls];
-          return checked<NC, N>(P, fs, fbase + base + line * lst) ? __ldg(face + base + line * lst) : 0.0;
-        };
-        double upn = nb >= 0 ? trace(l) : 0.0;
+        double upn = nb >= 0 && checked<NC, N>(P, fs, fbase + base + l * lst) ? __ldg(face + base + l * lst) : 0.0;
 #pragma unroll 1
         for (int j = 0; j < nl; ++j) {
           const int lb = base + l * lst;
           const double upd = upn;
           l = l + 1 < nl ? l + 1 : 0;
-          if (nb >= 0 && j + 1 < nl) upn = trace(l);  // next line's trace
+          if (nb >= 0 && j + 1 < nl && checked<NC, N>(P, fs, fbase + base + l * lst))
+            upn = __ldg(face + base + l * lst);  // next line's trace
           f32x2 u[N], acc[N];
           if ((N % 2) == 0 && st == 1) {
 #pragma unroll
@@ -836,23 +728,15 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lc = tid / TPC, tl = tid % TPC;
   const long long nblk = (P.c_hi - P.c_lo + cpb - 1) / cpb;
-  // with staged faces: two face buffers and the source table after the cell buffers
-  constexpr int NBUF = EclStaging<D, N, T, MODE, A>::NBUF;
-  const long long fe = ecl_face_elems<D, N, T>(cpb);
-  T* const s_f0 = s_in0 + NBUF * bufe;
-  T* const s_f1 = s_f0 + fe;
-  long long* const s_tab = reinterpret_cast<long long*>(s_f1 + fe);
-  const bool SF = P.stage_faces != 0;
-  auto stage = [&](T* dst, T* dstu, T* dstf, long long blk) {
+  auto stage = [&](T* dst, T* dstu, long long blk) {
     const long long c0 = P.c_lo + blk * cpb;
     long long ncell = (P.c_hi - c0) < cpb ? (P.c_hi - c0) : cpb;
     if (!checked<NC, N>(P, P.tin, (c0 + ncell) * NC - 1)) ncell = 0;
     stage_cells<D, N, T>(dst, P.tin + c0 * NC, ncell, tid, nthr);
     if constexpr (SU) stage_cells<D, N, T>(dstu, P.uin + c0 * NC, ncell, tid, nthr);
-    if (SF) stage_faces<D, N, T>(P, dstf, s_tab, c0, ncell, tid, nthr);
   };
   long long b = blockIdx.x;
-  if (b < nblk) stage(s_in0, s_u0, s_f0, b);
+  if (b < nblk) stage(s_in0, s_u0, b);
   cp_async_commit();
   bool odd = false;
   for (; b < nblk; b += gridDim.x) {
@@ -860,10 +744,8 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
     T* const nxt = odd ? s_in0 : s_in1;
     T* const curu = odd ? s_u1 : s_u0;
     T* const nxtu = odd ? s_u0 : s_u1;
-    T* const curf = odd ? s_f1 : s_f0;
-    T* const nxtf = odd ? s_f0 : s_f1;
     const long long nb = b + gridDim.x;
-    if (nb < nblk) stage(nxt, nxtu, nxtf, nb);
+    if (nb < nblk) stage(nxt, nxtu, nb);
     cp_async_commit();
     cp_async_wait<1>();  // this thread's copies of block b are complete
     __syncthreads();     // ... and everybody's
@@ -878,9 +760,9 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
       __syncthreads();
     }
     if constexpr (std::is_same_v<A, f32x2>)
-      ecl_block_x2<D, N, MODE>(P, P.c_lo + b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr, SF ? curf : nullptr);
+      ecl_block_x2<D, N, MODE>(P, P.c_lo + b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
     else
-      ecl_block<D, N, T, MODE>(P, P.c_lo + b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr, SF ? curf : nullptr);
+      ecl_block<D, N, T, MODE>(P, P.c_lo + b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
     __syncthreads();     // cur and s_o are free for the next blocks
     odd = !odd;
   }
@@ -909,35 +791,19 @@ cudaError_t launch_ecl(const EclParams<T>& P0, int mode, cudaStream_t stream) {
     if (mode < kApply || mode > kStageLast) return cudaErrorInvalidValue;
     const int nbuf = mode == kStageMid ? EclStaging<D, N, T, kStageMid, A>::NBUF
                      : mode == kStageLast ? EclStaging<D, N, T, kStageLast, A>::NBUF : 3;
-    // shared memory of a tile: the cell buffers, and with staged faces two face buffers and the
-    // face source table
-    auto smem_of = [&](int cpb, bool sf) {
-      size_t b = size_t(nbuf * ecl_buffer_elems<D, N, T>(cpb)) * sizeof(T);
-      if (sf) b += size_t(2 * ecl_face_elems<D, N, T>(cpb)) * sizeof(T) + size_t(ecl_face_table_bytes<D>(cpb));
-      return b;
-    };
-    // the staged tiles of the largest shape may not fit: shrink the tile (and stage no faces
-    // where even one cell does not fit with them)
-    if (P.stage_faces && smem_of(1, true) > 220 * 1024) P.stage_faces = 0;
-    while (P.cpb > 1 && smem_of(P.cpb, P.stage_faces != 0) > 220 * 1024) --P.cpb;
+    // the staged tiles of the largest shape may not fit five times: shrink the tile
+    while (P.cpb > 1 && size_t(nbuf * ecl_buffer_elems<D, N, T>(P.cpb)) * sizeof(T) > 220 * 1024) --P.cpb;
     const int threads = S::TPC * P.cpb;
-    const size_t smem = smem_of(P.cpb, P.stage_faces != 0);
+    const size_t smem = size_t(nbuf * ecl_buffer_elems<D, N, T>(P.cpb)) * sizeof(T);
     // one flag per mode: the four kernels share this lambda's instantiation
     static bool attr_done[4] = {false, false, false, false};
     static int sms = 0;
     auto go = [&](auto kern) -> cudaError_t {
       if (!attr_done[mode]) {
-        // the most any launch of this kernel asks for: the largest tile without staged faces,
-        // or with them where they fit
         int cmax = S::CPB;
-        while (cmax > 1 && smem_of(cmax, false) > 220 * 1024) --cmax;
-        size_t most = smem_of(cmax, false);
-        if (smem_of(1, true) <= 220 * 1024) {
-          int c = S::CPB;
-          while (c > 1 && smem_of(c, true) > 220 * 1024) --c;
-          if (smem_of(c, true) > most) most = smem_of(c, true);
-        }
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(most));
+        while (cmax > 1 && size_t(nbuf * ecl_buffer_elems<D, N, T>(cmax)) * sizeof(T) > 220 * 1024) --cmax;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(nbuf * ecl_buffer_elems<D, N, T>(cmax) * sizeof(T)));
         if (e != cudaSuccess) return e;
         int dev = 0;
         cudaGetDevice(&dev);

@@ -106,9 +106,6 @@ class PartitionedAdvectionOperation:
         v = {"native": _lib.HD_ARITH_NATIVE, "fp32x2": _lib.HD_ARITH_FP32X2}[arithmetic]
         check(self._L.hd_adv_set_arithmetic(self._h, v))
 
-    def set_face_staging(self, on: bool) -> None:
-        check(self._L.hd_adv_set_face_staging(self._h, 1 if on else 0))
-
     def critical_time_step(self) -> float:
         return float(self._L.hd_adv_critical_time_step(self._h))
 

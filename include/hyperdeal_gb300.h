@@ -126,17 +126,9 @@ long long hd_adv_n_dofs(const hd_adv *op);
  * cells per CTA (1..max, 0 = max) and CTAs per SM of the persistent grid
  * (0 = as many as fit).  Results do not depend on the tile. */
 int hd_adv_set_tile(hd_adv *op, int cells_per_cta, int ctas_per_sm);
-/* Another knob of the generic kernel (no reference counterpart; the
- * autotuner tries both): stage the upwind neighbours' face slabs in shared
- * memory together with the next block's cells (1) instead of reading them
- * from global memory inside the line loops (0, the default).  Results do not
- * depend on it; shapes whose cells and faces do not fit fall back to 0. */
-int hd_adv_set_face_staging(hd_adv *op, int on);
-int hd_adv_face_staging(const hd_adv *op);
 int hd_adv_tile_limits(const hd_adv *op, int *max_cells_per_cta, int *threads_per_cell);
-/* time apply launches (src read, dst overwritten) for candidate tiles, with
- * and without staged faces, and keep the fastest; returns it and its time
- * per apply */
+/* time apply launches (src read, dst overwritten) for candidate tiles and
+ * keep the fastest; returns it and its time per apply */
 int hd_adv_autotune(hd_adv *op, const void *src, void *dst, int reps, int *cells_per_cta, int *ctas_per_sm,
                     double *ms, void *stream);
 

@@ -363,47 +363,3 @@ def test_pipelined_launches_on_two_streams_overlap():
     assert op.device_status() == 0
     for sol, ref in zip(sols, refs):
         assert torch.equal(sol, ref)
-
-
-STAGE_CASES = [
-    # dim_x, dim_v, degree, cells, velocity, dtype, arithmetic, periodic
-    (1, 1, 3, [5, 4], [1.0, -0.5], "f64", "native", (True, True)),
-    (2, 1, 2, [3, 4, 3], [0.5, -0.3, 0.8], "f32", "native", (True, True)),
-    (2, 2, 3, [3, 4, 2, 3], [1.0, 0.7, -0.5, 0.3], "f32", "native", (True, True)),
-    (2, 2, 3, [3, 4, 2, 3], [1.0, 0.7, -0.5, 0.3], "f64", "native", (True, False)),
-    (2, 2, 3, [3, 2, 2, 3], [-1.0, 0.7, 0.5, 0.3], "f64", "fp32x2", (True, True)),
-    (2, 3, 4, [2, 3, 2, 2, 2], [0.6, 0.5, -0.4, 0.3, 0.2], "f32", "native", (True, True)),
-    (3, 3, 3, [2, 2, 2, 2, 2, 2], [1.0, 0.8, 0.6, -0.4, 0.3, 0.2], "f32", "native", (True, True)),
-    (3, 3, 2, [2, 2, 2, 2, 2, 2], [1.0, 0.8, 0.6, -0.4, 0.3, 0.2], "f64", "fp32x2", (True, True)),
-]
-
-
-@pytest.mark.parametrize("case", STAGE_CASES, ids=["s%d" % i for i in range(len(STAGE_CASES))])
-def test_staged_faces_give_the_same_bits(case):
-    """The generic kernel with the upwind face slabs staged in shared memory beside the cells
-    (hd_adv_set_face_staging) reads the same values as with in-loop global loads: apply and fused
-    rk45 steps are bitwise equal, and both match the oracle."""
-    dx, dv, k, cells, vel, dtype, arith, periodic = case
-    op, prob = make(dx, dv, k, cells, vel, periodic=periodic, dtype=dtype,
-                    bc=None if periodic[1] else dict(kind=2, amp=0.5, omega=[3.0] * (dx + dv), speed=vel))
-    op.set_kernel("generic")
-    if arith != "native":
-        op.set_arithmetic(arith)
-    u = np.random.default_rng(4).standard_normal(prob.n_dofs)
-    src = torch.tensor(u, dtype=op.dtype, device="cuda")
-    out = {}
-    for sf in (False, True):
-        op.set_face_staging(sf)
-        assert op.face_staging == sf
-        dst = op.initialize_dof_vector()
-        op.apply(dst, src, 0.2)
-        sol = src.clone()
-        integ = A.LowStorageRungeKuttaIntegrator(op.initialize_dof_vector(), op.initialize_dof_vector(), "rk45")
-        for s in range(2):
-            integ.perform_time_step(sol, s * 1e-3, 1e-3, op)
-        out[sf] = (dst, sol)
-    assert torch.equal(out[False][0], out[True][0])
-    assert torch.equal(out[False][1], out[True][1])
-    ref = O.apply(prob, src.double().cpu().numpy(), 0.2)
-    tol = F64_TOL if dtype == "f64" else F32_TOL
-    assert rel_err(out[True][0].double().cpu().numpy(), ref) <= tol

@@ -221,26 +221,3 @@ def test_part_interpolate_and_norms_add_up_to_the_whole_mesh():
     assert torch.equal(g.gather(vecs), u)
     assert abs(math.sqrt(n2) - n_ref) <= 1e-13 * n_ref
     assert abs(math.sqrt(e2) - e_ref) <= 1e-12 * max(e_ref, 1e-300) + 1e-15 * n_ref
-
-
-@pytest.mark.parametrize("name,n_parts", [("2x2v_f64_negative", 3), ("3x2v_f32", 2), ("2x2v_fp32x2", 2)])
-def test_parts_with_staged_faces_equal_the_single_operator(name, n_parts):
-    """The generic kernel's staged face slabs (hd_adv_set_face_staging) also come from the ghost region
-    at the part boundary: parts with staging give the single operator's bits."""
-    op = _single(name)
-    u = torch.tensor(np.random.default_rng(8).standard_normal(op.n_dofs), dtype=op.dtype, device="cuda")
-    dt = 0.2 * op.critical_time_step() / 3 ** 1.5
-    sol = u.clone()
-    it = A.LowStorageRungeKuttaIntegrator(op.initialize_dof_vector(), op.initialize_dof_vector(), "rk45")
-    for s in range(2):
-        it.perform_time_step(sol, s * dt, dt, op)
-    g = _group(name, n_parts)
-    for p in g.ops:
-        p.set_face_staging(True)
-    sols = g.initialize_dof_vectors()
-    g.scatter(u, sols)
-    its = [A.LowStorageRungeKuttaIntegrator(p.initialize_dof_vector(), p.initialize_dof_vector(), "rk45")
-           for p in g.ops]
-    for s in range(2):
-        g.perform_time_step(its, sols, s * dt, dt)
-    assert torch.equal(g.gather(sols), sol)
