@@ -46,12 +46,22 @@ def _deps_hash(extra: str = "") -> str:
     return h.hexdigest()
 
 
-# (family, header, factory) of the generated instantiation units and their (D, N) pairs
+# (family, header, factory) of the generated instantiation units and their (D, N) pairs; the
+# generic kernels' ghost-region variants (family ecl_gh) compile in units of their own
 GEN_UNITS = ([("ecl", "hd_ecl.cuh", "EclLaunchers", "make_launchers", D, N) for D in range(2, 7) for N in range(2, 7)]
+             + [("ecl_gh", "hd_ecl.cuh", None, None, D, N) for D in range(2, 7) for N in range(2, 7)]
              + [("batch", "hd_batch.cuh", "BatchLaunchers", "make_batch_launchers", D, N)
                 for D in (4, 5) for N in range(3, 7)]
              + [("gauss", "hd_gauss.cuh", "GaussLaunchers", "make_gauss_launchers", D, N)
                 for D in range(2, 7) for N in range(2, 6)])
+
+
+def _unit_text(fam: str, header: str, ret, factory, D: int, N: int) -> str:
+    if fam == "ecl_gh":
+        return '#include "%s"\nnamespace hd {\nHD_ECL_GH_INSTANCES(, %d, %d)\n}\n' % (header, D, N)
+    extern = "HD_ECL_GH_INSTANCES(extern, %d, %d)\n" % (D, N) if fam == "ecl" else ""
+    return ('#include "%s"\nnamespace hd {\n%s%s %s_launchers_%d_%d() { return %s<%d, %d>(); }\n}\n'
+            % (header, extern, ret, fam, D, N, factory, D, N))
 
 
 def _generate_units(build_dir: str = BUILD_DIR) -> list:
@@ -60,8 +70,7 @@ def _generate_units(build_dir: str = BUILD_DIR) -> list:
     out = []
     for fam, header, ret, factory, D, N in GEN_UNITS:
         path = os.path.join(gen, "%s_%d_%d.cu" % (fam, D, N))
-        text = ('#include "%s"\nnamespace hd {\n%s %s_launchers_%d_%d() { return %s<%d, %d>(); }\n}\n'
-                % (header, ret, fam, D, N, factory, D, N))
+        text = _unit_text(fam, header, ret, factory, D, N)
         if not os.path.exists(path) or open(path).read() != text:
             with open(path, "w") as f:
                 f.write(text)

@@ -111,9 +111,9 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
         reinterpret_cast<f32x2*>(cur)[i] = x2_from_double(v);
       }
       __syncthreads();
-      ecl_block_x2<D, N, MODE>(params[inst], (b - s_prefix[inst]) * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+      ecl_block_x2<D, N, MODE, false>(params[inst], (b - s_prefix[inst]) * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
     } else {
-      ecl_block<D, N, T, MODE>(params[inst], (b - s_prefix[inst]) * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+      ecl_block<D, N, T, MODE, false>(params[inst], (b - s_prefix[inst]) * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
     }
     __syncthreads();
     odd = !odd;

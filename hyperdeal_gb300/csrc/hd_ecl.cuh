@@ -221,19 +221,31 @@ __device__ __forceinline__ long long neighbour(const EclParams<T>& P, long long 
 // [nb_node NC/N, (nb_node + 1) NC/N) -- is read from the ghost region, where
 // its face is the NC/N values of that range in order.  Every index formed for
 // a node of the slab lies inside the buffer it addresses.
-template <int NC, int N, typename T>
-__device__ __forceinline__ const T* trace_src(const EclParams<T>& P, long long nb, int nb_node, long long* off) {
+// `slot` is the cell's own position in its layer of the last direction, which
+// is also its upwind neighbour's across that direction (no division here).
+// GH = false: the launch has no ghost region (P.ghost == nullptr), every
+// neighbour is a cell of this part's vector; GH = true: the ghost region is
+// optional (the kernels of FP64 storage serve both kinds of launch).
+template <int NC, int N, bool GH, typename T>
+__device__ __forceinline__ const T* trace_src(const EclParams<T>& P, long long nb, int nb_node, long long slot,
+                                              long long* off) {
+  if constexpr (!GH) {
+    (void)nb_node;
+    (void)slot;
+    *off = nb >= 0 ? (nb - P.gid0) * NC : 0;
+    return P.tin;
+  }
   const long long l = nb - P.gid0;
   if (nb < 0) {
     *off = 0;
     return P.tin;
   }
-  if (l >= 0 && l < P.n_cells) {
+  if (P.ghost == nullptr || (l >= 0 && l < P.n_cells)) {
     *off = l * NC;
     return P.tin;
   }
   constexpr int NF = NC / N;
-  *off = (nb % P.layer) * NF - (long long)nb_node * NF;
+  *off = (slot - (long long)nb_node) * NF;
   return P.ghost;
 }
 
@@ -317,7 +329,7 @@ __device__ __forceinline__ void stage_cells(T* dst, const T* src, long long ncel
 // phase writing K or the fused stage update
 // (stage modes mid/last: `uu_all` is the block's RK solution staged in shared
 // memory next to the operator input, or nullptr to read it from global memory)
-template <int D, int N, typename T, int MODE>
+template <int D, int N, typename T, int MODE, bool GH>
 __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0, int lc, int tl, const T* su_all,
                                           T* so_all, const T* uu_all) {
   using S = EclShape<D, N, T>;
@@ -338,6 +350,8 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
       else { cc[d] = int(gv % P.cells[d]); gv /= P.cells[d]; }
     }
   }
+  // position in the layer of the last direction (ghost faces of parts)
+  const long long slot = gg - (long long)cc[D - 1] * P.cstride[D - 1];
   constexpr int CST = EclTile<D, N, T>::CST;
   const T* su = su_all + lc * CST;
   T* so = so_all + lc * CST;
@@ -359,8 +373,8 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
     // where there is none, so that every load address is valid even if the
     // compiler issues the guarded loads unconditionally
     long long oA = 0, oB = 0;
-    const T* const sA = trace_src<NC, N>(P, nbA, P.op[dA].nb_node, &oA);
-    const T* const sB = dB >= 0 ? trace_src<NC, N>(P, nbB, P.op[dBi].nb_node, &oB) : P.tin;
+    const T* const sA = trace_src<NC, N, GH>(P, nbA, P.op[dA].nb_node, slot, &oA);
+    const T* const sB = dB >= 0 ? trace_src<NC, N, GH>(P, nbB, P.op[dBi].nb_node, slot, &oB) : P.tin;
 
     for (int item = tl; item < nitems; item += TPC) {
       const int base = item_base<D, N>(item, dA, dB);
@@ -551,7 +565,7 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
 // A cell's threads visit their lines in a rotated order (planes of the first
 // phase lie N*N values apart, a multiple of the bank count), and lines along
 // direction 0 (contiguous, 16-byte aligned for even N) are read as 16-byte words.
-template <int D, int N, int MODE>
+template <int D, int N, int MODE, bool GH>
 __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long long cell0, int lc, int tl,
                                              const double* su_all, double* so_all, const double* uu_all) {
   using S = EclShape<D, N, double>;
@@ -570,6 +584,8 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
       else { cc[d] = int(gv % P.cells[d]); gv /= P.cells[d]; }
     }
   }
+  // position in the layer of the last direction (ghost faces of parts)
+  const long long slot = gg - (long long)cc[D - 1] * P.cstride[D - 1];
   // the staged input was converted to FP32x2 words in place (ecl_kernel)
   const f32x2* sx = reinterpret_cast<const f32x2*>(su_all + lc * CST);
   f32x2* so = reinterpret_cast<f32x2*>(so_all + lc * CST);
@@ -607,7 +623,7 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
         // neighbour: every load address stays valid even if the compiler issues
         // the guarded loads unconditionally)
         long long fo = 0;
-        const double* const fs = trace_src<NC, N>(P, nb, L.nb_node, &fo);
+        const double* const fs = trace_src<NC, N, GH>(P, nb, L.nb_node, slot, &fo);
         const double* face = fs + (fo + L.nb_node * st);
         int l = rot;
         const long long fbase = fo + L.nb_node * st;  // index of `face` relative to fs
@@ -710,7 +726,10 @@ struct EclStaging {
 // one is computed (two staging buffers + one accumulator tile).  The FP32x2
 // kernels are capped at 128 registers (two CTAs of the largest shape per SM):
 // their issue-bound line loops need the warps.
-template <int D, int N, typename T, int MODE, typename A = T>
+// GH: the launch may read a ghost region (P.ghost != nullptr; parts of a
+// partitioned mesh only) -- the kernels without it keep the plain neighbour
+// addressing of an unpartitioned vector
+template <int D, int N, typename T, int MODE, typename A = T, bool GH = false>
 __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
                                   std::is_same_v<A, f32x2> ? 2 : EclShape<D, N, T>::MINB)
     ecl_kernel(const __grid_constant__ EclParams<T> P) {
@@ -760,9 +779,9 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
       __syncthreads();
     }
     if constexpr (std::is_same_v<A, f32x2>)
-      ecl_block_x2<D, N, MODE>(P, P.c_lo + b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+      ecl_block_x2<D, N, MODE, GH>(P, P.c_lo + b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
     else
-      ecl_block<D, N, T, MODE>(P, P.c_lo + b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+      ecl_block<D, N, T, MODE, GH>(P, P.c_lo + b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
     __syncthreads();     // cur and s_o are free for the next blocks
     odd = !odd;
   }
@@ -778,21 +797,14 @@ __host__ __device__ constexpr int ecl_default_cpb() {
   return cpb < 1 ? 1 : (cpb > EclShape<D, N, T>::CPB ? EclShape<D, N, T>::CPB : cpb);
 }
 
-// host launcher for one (D, N, T, arithmetic A): P.cpb cells per CTA (1..CPB;
-// 0 = default) and ctas_per_sm CTAs per SM (0 = as many as fit), persistent grid
-template <int D, int N, typename T, typename A = T>
-cudaError_t launch_ecl(const EclParams<T>& P0, int mode, cudaStream_t stream) {
+// host launcher of the four kernels (one per mode) of one (D, N, T, A, GH):
+// P is the launch's final parameter block, nbuf its staging buffers per cell tile
+template <int D, int N, typename T, typename A, bool GH>
+cudaError_t launch_ecl_mode(const EclParams<T>& P, int mode, int nbuf, cudaStream_t stream) {
   using S = EclShape<D, N, T>;
   if constexpr (!S::SUPPORTED) {
     return cudaErrorNotSupported;
   } else {
-    EclParams<T> P = P0;
-    if (P.cpb < 1 || P.cpb > S::CPB) P.cpb = ecl_default_cpb<D, N, T>();
-    if (mode < kApply || mode > kStageLast) return cudaErrorInvalidValue;
-    const int nbuf = mode == kStageMid ? EclStaging<D, N, T, kStageMid, A>::NBUF
-                     : mode == kStageLast ? EclStaging<D, N, T, kStageLast, A>::NBUF : 3;
-    // the staged tiles of the largest shape may not fit five times: shrink the tile
-    while (P.cpb > 1 && size_t(nbuf * ecl_buffer_elems<D, N, T>(P.cpb)) * sizeof(T) > 220 * 1024) --P.cpb;
     const int threads = S::TPC * P.cpb;
     const size_t smem = size_t(nbuf * ecl_buffer_elems<D, N, T>(P.cpb)) * sizeof(T);
     // one flag per mode: the four kernels share this lambda's instantiation
@@ -824,14 +836,47 @@ cudaError_t launch_ecl(const EclParams<T>& P0, int mode, cudaStream_t stream) {
       return cudaGetLastError();
     };
     switch (mode) {
-      case kApply: return go(ecl_kernel<D, N, T, kApply, A>);
-      case kStageFirst: return go(ecl_kernel<D, N, T, kStageFirst, A>);
-      case kStageMid: return go(ecl_kernel<D, N, T, kStageMid, A>);
-      case kStageLast: return go(ecl_kernel<D, N, T, kStageLast, A>);
+      case kApply: return go(ecl_kernel<D, N, T, kApply, A, GH>);
+      case kStageFirst: return go(ecl_kernel<D, N, T, kStageFirst, A, GH>);
+      case kStageMid: return go(ecl_kernel<D, N, T, kStageMid, A, GH>);
+      case kStageLast: return go(ecl_kernel<D, N, T, kStageLast, A, GH>);
       default: return cudaErrorInvalidValue;
     }
   }
 }
+
+// host launcher for one (D, N, T, arithmetic A): P.cpb cells per CTA (1..CPB;
+// 0 = default) and ctas_per_sm CTAs per SM (0 = as many as fit), persistent
+// grid.  FP32 storage, bandwidth-bound with little arithmetic per cell, has
+// kernels without the ghost-region addressing for unpartitioned launches
+// (measured on GB300, 4D k = 3: 6% per rk45 step) and kernels with it for
+// parts, instantiated in units of their own (ecl_gh_<D>_<N>.cu) so that both
+// compile in parallel; the FP64 kernels, bound by their arithmetic, serve both.
+template <int D, int N, typename T, typename A = T>
+cudaError_t launch_ecl(const EclParams<T>& P0, int mode, cudaStream_t stream) {
+  using S = EclShape<D, N, T>;
+  if constexpr (!S::SUPPORTED) {
+    return cudaErrorNotSupported;
+  } else {
+    EclParams<T> P = P0;
+    if (P.cpb < 1 || P.cpb > S::CPB) P.cpb = ecl_default_cpb<D, N, T>();
+    if (mode < kApply || mode > kStageLast) return cudaErrorInvalidValue;
+    const int nbuf = mode == kStageMid ? EclStaging<D, N, T, kStageMid, A>::NBUF
+                     : mode == kStageLast ? EclStaging<D, N, T, kStageLast, A>::NBUF : 3;
+    // the staged tiles of the largest shape may not fit five times: shrink the tile
+    while (P.cpb > 1 && size_t(nbuf * ecl_buffer_elems<D, N, T>(P.cpb)) * sizeof(T) > 220 * 1024) --P.cpb;
+    if constexpr (std::is_same_v<T, float>)
+      return P.ghost ? launch_ecl_mode<D, N, T, A, true>(P, mode, nbuf, stream)
+                     : launch_ecl_mode<D, N, T, A, false>(P, mode, nbuf, stream);
+    else
+      return launch_ecl_mode<D, N, T, A, true>(P, mode, nbuf, stream);
+  }
+}
+
+// the FP32 ghost-region launcher of one (D, N): explicitly instantiated in
+// ecl_gh_<D>_<N>.cu, declared (not instantiated) in ecl_<D>_<N>.cu
+#define HD_ECL_GH_INSTANCES(PREFIX, D, N) \
+  PREFIX template cudaError_t launch_ecl_mode<D, N, float, float, true>(const EclParams<float>&, int, int, cudaStream_t);
 
 // launcher table entry
 struct EclLaunchers {
@@ -864,7 +909,7 @@ bool ecl6_eligible(const EclParams<float>& P);
 cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int* ticket, int mode, cudaStream_t stream,
                         unsigned wait_limit = 0, int skip_issue = -1);
 
-// defined in hd_ecl_d{2..6}.cu
+// defined in hd_dispatch.cu (over the generated units ecl_<D>_<N>.cu)
 EclLaunchers ecl_launchers_d2(int N);
 EclLaunchers ecl_launchers_d3(int N);
 EclLaunchers ecl_launchers_d4(int N);
