@@ -210,12 +210,12 @@ def run_vp(args):
     f0 = V.perturbed_maxwellian(VP_DIM_X, eps=0.01, k=0.5, perturbed_dims=(0, 1))
 
     def make(guess, dtype, tol, rhs_rel, precond=args.vp_precond):
-        # "learned5": the learned guess with its Adam steps every 5th solve (once per rk45 step)
+        # "learned": the least-squares fitted network; "learned_adam": the Adam-trained one
         p = V.VlasovPoissonParameters(VP_DIM_X, DEGREE, [VP_CELLS_X] * 2, [VP_CELLS_V] * 2, [0.0] * 2,
                                       [two_pi] * 2, [-6.0] * 2, [6.0] * 2, dtype=dtype, cg_tol=tol,
-                                      guess="learned" if guess == "learned5" else guess,
-                                      cg_rhs_relative=rhs_rel, learn_every=5 if guess == "learned5" else 0,
-                                      cg_precond=precond)
+                                      guess="learned" if guess.startswith("learned") else guess,
+                                      cg_rhs_relative=rhs_rel, cg_precond=precond,
+                                      learn_fit="adam" if guess == "learned_adam" else "least_squares")
         return V.VlasovPoissonOperation(p)
 
     stream = torch.cuda.current_stream()
@@ -224,7 +224,7 @@ def run_vp(args):
     clocks = None
     selected = [r.strip() for r in args.vp_runs.split(",")]
     for dtype in ("f64", "f64x", "f32"):  # f64x: FP64 storage, FP32x2 advection contractions
-        for guess in ("previous", "zero", "learned", "learned5", "previous_noprecond", "zero_noprecond",
+        for guess in ("previous", "zero", "learned", "learned_adam", "previous_noprecond", "zero_noprecond",
                       "learned_noprecond"):
             if "%s/%s" % (dtype, guess) not in selected:
                 continue
@@ -618,9 +618,10 @@ def main():
                     help="adv4d: keep the default tile instead of picking it with hd_adv_autotune")
     ap.add_argument("--vp-tol", type=float, default=1e-10, help="CG: ||r|| <= tol ||rhs|| (vp2x2v)")
     ap.add_argument("--vp-oracle-steps", type=int, default=2, help="steps compared with the FP64 oracle (vp2x2v)")
-    ap.add_argument("--vp-runs", default="f64/previous,f64/zero,f64/learned,f64/previous_noprecond,f64/zero_noprecond,"
-                                         "f64x/previous,f64x/zero,f64x/learned,f32/previous,f32/zero,f32/learned,"
-                                         "f32/previous_noprecond,f32/zero_noprecond",
+    ap.add_argument("--vp-runs", default="f64/previous,f64/zero,f64/learned,f64/learned_adam,f64/previous_noprecond,"
+                                         "f64/zero_noprecond,f64/learned_noprecond,f64x/previous,f64x/zero,"
+                                         "f64x/learned,f32/previous,f32/zero,f32/learned,f32/previous_noprecond,"
+                                         "f32/zero_noprecond,f32/learned_noprecond",
                     help="dtype/guess combinations timed (vp2x2v; _noprecond: CG without the preconditioner)")
     ap.add_argument("--vp-precond", default="block_jacobi", choices=["block_jacobi", "none"],
                     help="preconditioner of the Poisson CG (vp2x2v)")

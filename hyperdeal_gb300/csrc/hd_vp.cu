@@ -30,6 +30,9 @@ namespace {
 
 constexpr int kMomChunk = 16;   // v-cells summed by one block of the moment kernel
 constexpr int kCgThreads = 64;  // small blocks: the x-space system is small, spread it over many SMs
+constexpr int kLsMax = 16;      // basis columns of the least-squares learned guess (upper bound)
+constexpr int kLsRed = kLsMax + 1;
+constexpr double kLsCut = 1e-12;  // a pair joins the basis if its new direction is above this fraction
 
 // device-side solver statistics (read by hd_vp_cg_stats; no host synchronisation per solve)
 struct VpStats {
@@ -275,6 +278,21 @@ struct PoissonArgs {
   void* es;               // E / h_v in the storage precision
   int es_f32;
   VpStats* stats;
+  // least-squares learned guess (lsQ null: off).  The network phi = Z (Q^T rhs)
+  // has the layers W1 = Q^T (k x n) and W2 = Z (n x k): Q is an orthonormal
+  // basis of the right-hand sides A x_j of the recent solves and Z holds the
+  // same combinations of their potentials x_j, so that W2 W1 maps every
+  // recent rhs to its potential -- the minimum-norm least-squares fit of the
+  // recent (rhs, phi) pairs.  The ring lsX / lsB keeps the last ls_kkeep pairs
+  // (x, A x = rhs - r); when the basis holds ls_kmax columns it is rebuilt
+  // from the ring.
+  double* lsQ;
+  double* lsZ;
+  double* lsX;
+  double* lsB;
+  int* lsCount;   // basis columns (device; read at the start, written at the end)
+  double* redk;   // [2][kLsRed gridDim] partial sums of grid_sum_k
+  int ls_kmax, ls_kkeep, ls_head, ls_nraw;  // ring slot of this solve; ring entries including it
 };
 
 // fixed-order grid-wide sums of two values; consecutive calls alternate
@@ -334,6 +352,107 @@ __device__ double3 grid_sum3(cgrp::grid_group& grid, double v0, double v1, doubl
                       __shfl_sync(0xffffffffu, s2, 0));
 }
 
+// fixed-order grid-wide sums of v[0..k) (k <= kLsRed), in place; every
+// thread of the grid obtains identical values.  The halves of `red`
+// (2 x kLsRed x gridDim) alternate as in grid_sum2; the grid barrier also
+// frees `shk` (warps x kLsRed) for the next call.
+__device__ void grid_sum_k(cgrp::grid_group& grid, double* v, int k, double* red, int& slot, double* shk) {
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32, nw = blockDim.x / 32;
+#pragma unroll
+  for (int j = 0; j < kLsRed; ++j) {
+    if (j < k) {
+      double t = v[j];
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+      if (l == 0) shk[w * kLsRed + j] = t;
+    }
+  }
+  __syncthreads();
+  double* part = red + (size_t)slot * kLsRed * gridDim.x;
+  if ((int)threadIdx.x < k) {
+    double t = 0.0;
+    for (int q = 0; q < nw; ++q) t += shk[q * kLsRed + threadIdx.x];
+    part[(size_t)blockIdx.x * kLsRed + threadIdx.x] = t;
+  }
+  grid.sync();
+#pragma unroll
+  for (int j = 0; j < kLsRed; ++j) {
+    if (j < k) {
+      double t = 0.0;
+      for (int b = l; b < (int)gridDim.x; b += 32) t += __ldcg(part + (size_t)b * kLsRed + j);
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+      v[j] = __shfl_sync(0xffffffffu, t, 0);
+    }
+  }
+  slot ^= 1;
+}
+
+// Appends the pair of ring slot `src` to the basis of k columns: q = A x and
+// z = x are orthogonalised against Q (classical Gram-Schmidt, twice), with
+// the same operations on z, into column k; the column is kept (returns k + 1)
+// when ||q|| is above kLsCut of ||A x||, i.e. when the pair adds a direction
+// that is not round-off.  Each pass reduces its coefficients together with
+// the squared length of its input; the final length follows from the second
+// pass, ||q2||^2 = ||q1||^2 - sum a2_j^2 (Q orthonormal, a2 small).  Two
+// grid-wide sums per pair; row-local otherwise.
+template <typename Args>
+__device__ int ls_append(cgrp::grid_group& grid, const Args& A, int src, int k, long long t0, long long stride,
+                         int& slotk, double* shk) {
+  const long long n = A.g.nx_dofs;
+  const double* xs = A.lsX + (size_t)src * n;
+  const double* bs = A.lsB + (size_t)src * n;
+  double* q = A.lsQ + (size_t)k * n;
+  double* z = A.lsZ + (size_t)k * n;
+  for (long long i = t0; i < n; i += stride) {
+    q[i] = bs[i];
+    z[i] = xs[i];
+  }
+  double n0 = 0.0, len2 = 0.0;
+  for (int pass = 0; pass < 2; ++pass) {
+    double a[kLsRed];
+    double nn = 0.0;
+#pragma unroll
+    for (int j = 0; j < kLsRed; ++j) a[j] = 0.0;
+    for (long long i = t0; i < n; i += stride) {
+      const double qi = q[i];
+#pragma unroll
+      for (int j = 0; j < kLsMax; ++j)
+        if (j < k) a[j] = fma(A.lsQ[(size_t)j * n + i], qi, a[j]);
+      nn = fma(qi, qi, nn);
+    }
+#pragma unroll
+    for (int j = 0; j < kLsRed; ++j)
+      if (j == k) a[j] = nn;
+    grid_sum_k(grid, a, k + 1, A.redk, slotk, shk);
+    double sq = 0.0, aa = 0.0;
+#pragma unroll
+    for (int j = 0; j < kLsRed; ++j) {
+      if (j == k) sq = a[j];
+      if (j < k) aa = fma(a[j], a[j], aa);
+    }
+    if (pass == 0) n0 = sqrt(sq);
+    else len2 = sq - aa;
+    for (long long i = t0; i < n; i += stride) {
+      double qi = q[i], zi = z[i];
+#pragma unroll
+      for (int j = 0; j < kLsMax; ++j)
+        if (j < k) {
+          qi = fma(-a[j], A.lsQ[(size_t)j * n + i], qi);
+          zi = fma(-a[j], A.lsZ[(size_t)j * n + i], zi);
+        }
+      q[i] = qi;
+      z[i] = zi;
+    }
+  }
+  const double len = len2 > 0.0 ? sqrt(len2) : 0.0;
+  if (!(len > kLsCut * n0) || !(len > 0.0)) return k;
+  const double inv = 1.0 / len;
+  for (long long i = t0; i < n; i += stride) {
+    q[i] *= inv;
+    z[i] *= inv;
+  }
+  return k + 1;
+}
+
 // z_i = sum_j B^{-1}_c[i][j] r_j over the rows j of row i's x-cell c
 __device__ __forceinline__ double block_jacobi_row(const VpGeom& g, const double* __restrict__ binv,
                                                    const double* r, long long i) {
@@ -363,6 +482,7 @@ __device__ __forceinline__ double block_jacobi_row(const VpGeom& g, const double
 __global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
   cgrp::grid_group grid = cgrp::this_grid();
   __shared__ double sh[32];
+  __shared__ double shk[(kCgThreads / 32) * kLsRed];
   const VpGeom& g = A.g;
   const long long n = g.nx_dofs;
   const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x, stride = (long long)gridDim.x * blockDim.x;
@@ -392,6 +512,30 @@ __global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
     for (long long i = t0; i < n; i += stride) A.rhs[i] -= mean2;
   }
   if (!(A.phases & 2)) return;
+  // least-squares learned guess: x = Z (Q^T rhs), or 0 before the first pair
+  const bool ls = A.lsQ != nullptr;
+  int lsk = 0, slotk = 0;
+  if (ls) {
+    lsk = *A.lsCount;
+    double c[kLsRed];
+#pragma unroll
+    for (int j = 0; j < kLsRed; ++j) c[j] = 0.0;
+    for (long long i = t0; i < n; i += stride) {
+      const double b = A.rhs[i];
+#pragma unroll
+      for (int j = 0; j < kLsMax; ++j)
+        if (j < lsk) c[j] = fma(A.lsQ[(size_t)j * n + i], b, c[j]);
+    }
+    if (lsk > 0) grid_sum_k(grid, c, lsk, A.redk, slotk, shk);
+    for (long long i = t0; i < n; i += stride) {
+      double x = 0.0;
+#pragma unroll
+      for (int j = 0; j < kLsMax; ++j)
+        if (j < lsk) x = fma(c[j], A.lsZ[(size_t)j * n + i], x);
+      A.x[i] = x;
+    }
+    grid.sync();  // the guess complete before A x reads it
+  }
   double* const r = A.r;
   double* const p = A.p;
   double* const w = A.Ap;    // A z
@@ -406,10 +550,25 @@ __global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
     else grid.sync();
     for (long long i = t0; i < n; i += stride) z[i] = block_jacobi_row(g, A.binv, r, i);
   };
-  double lbb = 0.0;
+  double lbb = 0.0, lr0 = 0.0;
   for (long long i = t0; i < n; i += stride) {
-    r[i] = A.rhs[i] - spmv_row(A.W, n, A.col, A.val, A.x, i);
+    const double ri = A.rhs[i] - spmv_row(A.W, n, A.col, A.val, A.x, i);
+    r[i] = ri;
     lbb += A.rhs[i] * A.rhs[i];
+    lr0 += ri * ri;
+  }
+  double bb = -1.0;  // ||rhs||^2 once summed
+  if (ls && lsk > 0) {
+    // the judge: the guess starts CG only if its residual is below ||rhs|| (that of 0)
+    const double2 jb = grid_sum2(grid, lbb, lr0, A.red, slot, sh);
+    bb = jb.x;
+    const bool keep = jb.y < jb.x;
+    if (!keep)
+      for (long long i = t0; i < n; i += stride) {
+        A.x[i] = 0.0;
+        r[i] = A.rhs[i];
+      }
+    if (keep && t0 == 0) A.stats->learned_picked += 1;
   }
   precondition();
   grid.sync();  // z complete before A z
@@ -422,7 +581,7 @@ __global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
     lrr += r[i] * r[i];
   }
   double3 t = grid_sum3(grid, lrz, lwz, lrr, A.red, slot, sh);
-  const double bb = grid_sum2(grid, lbb, 0.0, A.red, slot, sh).x;
+  if (bb < 0.0) bb = grid_sum2(grid, lbb, 0.0, A.red, slot, sh).x;
   double gamma = t.x, delta = t.y, rnorm = sqrt(t.z);
   const double r0 = rnorm;
   const double stop = A.rhs_relative ? A.rel_tol * sqrt(bb) : fmax(A.rel_tol * r0, 1e-14 * sqrt(bb));
@@ -468,6 +627,26 @@ __global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
     for (long long i = t0; i < n; i += stride) lx += A.x[i];
     const double mean_x = grid_sum2(grid, lx, 0.0, A.red, slot, sh).x / double(n);
     for (long long i = t0; i < n; i += stride) A.x[i] -= mean_x;
+  }
+  if (ls) {
+    // this solve's pair (x, A x = rhs - r) into the ring, then into the basis
+    // (or the basis rebuilt from the ring when it is full)
+    double* xh = A.lsX + (size_t)A.ls_head * n;
+    double* bh = A.lsB + (size_t)A.ls_head * n;
+    for (long long i = t0; i < n; i += stride) {
+      xh[i] = A.x[i];
+      bh[i] = A.rhs[i] - r[i];
+    }
+    if (lsk >= A.ls_kmax) {
+      lsk = 0;
+      for (int e = 0; e < A.ls_nraw; ++e) {
+        const int src = (A.ls_head - A.ls_nraw + 1 + e + 2 * A.ls_kkeep) % A.ls_kkeep;
+        lsk = ls_append(grid, A, src, lsk, t0, stride, slotk, shk);
+      }
+    } else {
+      lsk = ls_append(grid, A, A.ls_head, lsk, t0, stride, slotk, shk);
+    }
+    if (t0 == 0) *A.lsCount = lsk;
   }
   grid.sync();  // x complete before the field reads it
   const int N = g.N;
@@ -680,7 +859,14 @@ struct hd_vp {
   double* d_judge;    // residual partials of the judge
   int cg_grid;
   int guess;
-  hd::VpModel* model;  // learned initial guess
+  hd::VpModel* model;  // learned initial guess, Adam-trained (HD_VP_FIT_ADAM)
+  // learned initial guess, least-squares fit (HD_VP_FIT_LEAST_SQUARES):
+  // basis Q, Z (ls_kmax x nx each), ring of pairs X, B (ls_kkeep x nx each),
+  // column count (device int), sums of the fit (2 x 17 x cg_grid)
+  double* d_ls;
+  int* d_ls_count;
+  double* d_redk;
+  int ls_kmax, ls_kkeep, ls_head, ls_nraw;
 };
 
 namespace {
@@ -774,6 +960,9 @@ void vp_free(hd_vp* v) {
   cudaFree(v->d_dy);
   cudaFree(v->d_judge);
   cudaFree(v->d_binv);
+  cudaFree(v->d_ls);
+  cudaFree(v->d_ls_count);
+  cudaFree(v->d_redk);
   hd::vp_model_destroy(v->model);
   delete v;
 }
@@ -854,7 +1043,49 @@ hd::PoissonArgs poisson_args(hd_vp* v, int phases) {
   A.es = v->d_es;
   A.es_f32 = v->dtype == HD_F32;
   A.stats = v->d_stats;
+  A.lsQ = A.lsZ = A.lsX = A.lsB = nullptr;
+  A.lsCount = nullptr;
+  A.redk = v->d_redk;
+  A.ls_kmax = v->ls_kmax;
+  A.ls_kkeep = v->ls_kkeep;
+  A.ls_head = v->ls_head;
+  A.ls_nraw = v->ls_nraw;
+  if (v->guess == HD_VP_GUESS_LEARNED && v->d_ls) {
+    const size_t kx = size_t(v->ls_kmax) * nx, kr = size_t(v->ls_kkeep) * nx;
+    A.lsQ = v->d_ls;
+    A.lsZ = v->d_ls + kx;
+    A.lsX = v->d_ls + 2 * kx;
+    A.lsB = v->d_ls + 2 * kx + kr;
+    A.lsCount = v->d_ls_count;
+  }
   return A;
+}
+
+// the least-squares learned guess's buffers (once) and an empty fit
+int ls_reset(hd_vp* v) {
+  const long long nx = v->g.nx_dofs;
+  if (!v->d_ls) {
+    const size_t n = size_t(2) * (v->ls_kmax + v->ls_kkeep) * nx;
+    int rc = vcuda(cudaMalloc((void**)&v->d_ls, sizeof(double) * n), "learned guess: cudaMalloc");
+    if (!rc) rc = vcuda(cudaMalloc((void**)&v->d_ls_count, sizeof(int)), "learned guess: cudaMalloc");
+    if (!rc) rc = vcuda(cudaMalloc((void**)&v->d_redk, sizeof(double) * 2 * hd::kLsRed * v->cg_grid),
+                        "learned guess: cudaMalloc");
+    if (rc) return rc;
+  }
+  v->ls_head = v->ls_kkeep - 1;
+  v->ls_nraw = 0;
+  return vcuda(cudaMemset(v->d_ls_count, 0, sizeof(int)), "learned guess: reset");
+}
+
+// the learned guess of the descriptor's fit, starting without pairs
+int learned_create(hd_vp* v) {
+  if (v->desc.learn_fit == HD_VP_FIT_LEAST_SQUARES) return ls_reset(v);
+  if (!v->model) {
+    v->model = hd::vp_model_create(v->g.nx_dofs, v->desc.learn_rank > 0 ? v->desc.learn_rank : 32,
+                                   v->desc.learn_history > 0 ? v->desc.learn_history : 64);
+    if (!v->model) return vfail(HD_ERR_ALLOC, "learned-guess model");
+  }
+  return HD_OK;
 }
 
 int launch_poisson(hd_vp* v, int phases, cudaStream_t s) {
@@ -872,6 +1103,12 @@ int solve_poisson(hd_vp* v, cudaStream_t s) {
   if (v->guess == HD_VP_GUESS_ZERO) {
     int rc = vcuda(cudaMemsetAsync(v->d_phi, 0, sizeof(double) * nx, s), "zero guess");
     if (rc) return rc;
+  }
+  if (v->guess == HD_VP_GUESS_LEARNED && v->d_ls) {
+    // least-squares fit: one launch predicts, judges, solves and adds the pair
+    v->ls_head = (v->ls_head + 1) % v->ls_kkeep;
+    if (v->ls_nraw < v->ls_kkeep) ++v->ls_nraw;
+    return launch_poisson(v, 3, s);
   }
   const bool learned = v->guess == HD_VP_GUESS_LEARNED && v->model;
   if (!learned) return launch_poisson(v, 3, s);
@@ -949,6 +1186,13 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
     return vfail(HD_ERR_INVALID, "hd_vp_create: unknown guess");
   if (d.cg_precond != HD_VP_PRECOND_NONE && d.cg_precond != HD_VP_PRECOND_BLOCK_JACOBI)
     return vfail(HD_ERR_INVALID, "hd_vp_create: unknown preconditioner");
+  if (d.learn_fit != HD_VP_FIT_LEAST_SQUARES && d.learn_fit != HD_VP_FIT_ADAM)
+    return vfail(HD_ERR_INVALID, "hd_vp_create: unknown learned-guess fit");
+  if (d.learn_fit == HD_VP_FIT_LEAST_SQUARES &&
+      (d.learn_rank < 0 || d.learn_rank > hd::kLsMax || d.learn_history < 0 ||
+       (d.learn_rank > 0 && d.learn_history >= d.learn_rank)))
+    return vfail(HD_ERR_INVALID, "hd_vp_create: least-squares guess needs learn_rank <= 16 and "
+                                 "learn_history < learn_rank");
   hd_vp* v = new (std::nothrow) hd_vp;
   if (!v) return vfail(HD_ERR_ALLOC, "out of host memory");
   std::memset(v, 0, sizeof(*v));
@@ -1077,9 +1321,15 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
     const int rc = build_block_jacobi(v);
     if (rc) { vp_free(v); return rc; }
   }
+  if (d.learn_fit == HD_VP_FIT_LEAST_SQUARES) {
+    v->ls_kmax = d.learn_rank > 0 ? d.learn_rank : 16;
+    v->ls_kkeep = d.learn_history > 0 ? d.learn_history : (v->ls_kmax * 3 + 7) / 8;
+    if (v->ls_kkeep >= v->ls_kmax) v->ls_kkeep = v->ls_kmax - 1;
+    if (v->ls_kkeep < 1) { vp_free(v); return vfail(HD_ERR_INVALID, "hd_vp_create: learn_rank >= 2"); }
+  }
   if (d.guess == HD_VP_GUESS_LEARNED) {
-    v->model = hd::vp_model_create(nx, d.learn_rank > 0 ? d.learn_rank : 32, d.learn_history > 0 ? d.learn_history : 64);
-    if (!v->model) { vp_free(v); return vfail(HD_ERR_ALLOC, "hd_vp_create: learned-guess model"); }
+    const int rc = learned_create(v);
+    if (rc) { vp_free(v); return rc; }
   }
   *out = v;
   return HD_OK;
@@ -1259,10 +1509,9 @@ int hd_vp_set_arithmetic(hd_vp* v, int arithmetic) {
 int hd_vp_set_guess(hd_vp* v, int guess) {
   if (!v) return vfail(HD_ERR_INVALID, "hd_vp_set_guess: null handle");
   if (guess < HD_VP_GUESS_ZERO || guess > HD_VP_GUESS_LEARNED) return vfail(HD_ERR_INVALID, "unknown guess");
-  if (guess == HD_VP_GUESS_LEARNED && !v->model) {
-    v->model = hd::vp_model_create(v->g.nx_dofs, v->desc.learn_rank > 0 ? v->desc.learn_rank : 32,
-                                   v->desc.learn_history > 0 ? v->desc.learn_history : 64);
-    if (!v->model) return vfail(HD_ERR_ALLOC, "learned-guess model");
+  if (guess == HD_VP_GUESS_LEARNED && guess != v->guess) {
+    const int rc = learned_create(v);
+    if (rc) return rc;
   }
   if (guess != v->guess) v->have_prev = false;
   v->guess = guess;

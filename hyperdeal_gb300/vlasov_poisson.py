@@ -6,10 +6,12 @@ evaluation computes rho = int f dv, solves the SIPG Poisson problem for the
 potential by conjugate gradients (FP64), takes grad(phi) at the x-nodes and
 applies the upwind-DG advection with the phase-space velocity (v, grad phi).
 The potential is kept between evaluations as the next CG initial guess (the
-reference's behaviour); ``guess="learned"`` replaces that guess by
-phi_prev + net(rho - rho_prev), a network trained online on the solver's own
-differences between consecutive solves, whenever its initial residual is
-smaller.  Diagnostics follow diagnostics.h:28-141.
+reference's behaviour); ``guess="learned"`` starts CG from a two-layer linear
+network trained online on the solver's own (right-hand side, potential)
+pairs: by default (``learn_fit="least_squares"``) the FP64 minimum-norm
+least-squares fit of the recent pairs, computed inside the Poisson launch;
+with ``learn_fit="adam"`` FP32 weights trained by Adam on the differences
+between consecutive solves.  Diagnostics follow diagnostics.h:28-141.
 
 Gauss-Lobatto collocation, dim_x == dim_v, periodic x- and v-meshes.
 """
@@ -53,6 +55,7 @@ class VlasovPoissonParameters:
     cg_rhs_relative: bool = False  # False: ||r|| <= cg_tol ||r_0|| as deal.II's ReductionControl
     learn_every: int = 0  # Adam steps every n-th solve (0: every solve)
     cg_precond: str = "block_jacobi"  # "none" or "block_jacobi" (x-cell diagonal blocks of the SIPG matrix)
+    learn_fit: str = "least_squares"  # or "adam" (hd_vp_learn_fit)
 
     def c(self) -> _lib.hd_vp_desc:
         d = _lib.hd_vp_desc()
@@ -73,6 +76,7 @@ class VlasovPoissonParameters:
         d.learn_every = int(self.learn_every)
         d.cg_precond = {"none": _lib.HD_VP_PRECOND_NONE, "block_jacobi": _lib.HD_VP_PRECOND_BLOCK_JACOBI}[
             self.cg_precond]
+        d.learn_fit = {"least_squares": _lib.HD_VP_FIT_LEAST_SQUARES, "adam": _lib.HD_VP_FIT_ADAM}[self.learn_fit]
         return d
 
 

@@ -371,11 +371,26 @@ int hd_batch_autotune(hd_batch *b, const void *const *src, void *const *dst, int
 enum hd_vp_guess {
   HD_VP_GUESS_ZERO = 0,     /* CG starts from 0                                 */
   HD_VP_GUESS_PREVIOUS = 1, /* from the previous potential (the reference's)    */
-  HD_VP_GUESS_LEARNED = 2   /* from phi_prev + net(rho - rho_prev), a network
-                               trained online on the solver's own differences
-                               between consecutive solves, judged against
-                               PREVIOUS by the initial residual               */
+  HD_VP_GUESS_LEARNED = 2   /* from a network trained online on the solver's
+                               own (right-hand side, potential) pairs; the fit
+                               is chosen by hd_vp_desc::learn_fit            */
 };
+
+/* How the learned guess's network -- two linear layers, W1 (r x n) and
+ * W2 (n x r), n = x-DoFs -- is fitted to the solver's pairs.
+ * LEAST_SQUARES (default): FP64, the minimum-norm least-squares fit of the
+ *   last pairs (rhs_j, phi_j), W2 W1 = [phi_j] [rhs_j]^+, computed by
+ *   Gram-Schmidt orthogonalisation inside the Poisson launch: W1 = Q^T with Q
+ *   an orthonormal basis of the rhs_j, W2 = Z the same combinations of the
+ *   phi_j.  guess = W2 W1 rhs, used when its residual is below ||rhs||.
+ *   learn_rank (0: 16, at most 16) basis columns; when they are used up the
+ *   basis is rebuilt from the last learn_history pairs (0: 3/8 of the rank,
+ *   less than the rank).
+ * ADAM: FP32 weights trained by Adam on normalised differences between
+ *   consecutive solves, guess = phi_prev + W2 W1 (rho - rho_prev), judged
+ *   against phi_prev (learn_rank 0: 32, learn_history 0: 64 pairs); its
+ *   loss and gradients are exposed by hd_vp_learn_loss_grad. */
+enum hd_vp_learn_fit { HD_VP_FIT_LEAST_SQUARES = 0, HD_VP_FIT_ADAM = 1 };
 
 /* Preconditioner of the Poisson CG.  The reference preconditions its CG
  * with geometric multigrid and a Chebyshev smoother (examples/vlasov_poisson/
@@ -393,15 +408,16 @@ typedef struct hd_vp_desc {
                            or at ||r|| <= cg_tol ||rhs|| with cg_rhs_relative */
   int cg_max_iter;
   int guess;            /* enum hd_vp_guess                                   */
-  int learn_rank;       /* bottleneck of the learned guess (0: 32)            */
-  int learn_history;    /* (rho, phi) pairs kept for training (0: 64)         */
+  int learn_rank;       /* bottleneck r of the learned guess (0: the fit's default) */
+  int learn_history;    /* pairs kept for the fit (0: the fit's default)      */
   int cg_rhs_relative;  /* 1: tolerance relative to ||rhs|| -- a fixed
                            accuracy, so a better initial guess saves
                            iterations                                         */
-  int learn_every;      /* the learned guess stores every solve's pair and
-                           takes its Adam steps every learn_every-th solve
-                           (0: 1, every solve)                                */
+  int learn_every;      /* ADAM fit: the learned guess stores every solve's
+                           pair and takes its Adam steps every learn_every-th
+                           solve (0: 1, every solve)                          */
   int cg_precond;       /* enum hd_vp_precond (0: none)                       */
+  int learn_fit;        /* enum hd_vp_learn_fit (0: least squares)            */
 } hd_vp_desc;
 
 typedef struct hd_vp hd_vp;
