@@ -70,7 +70,8 @@ class hd_vp_desc(ctypes.Structure):
                 ("lo_v", ctypes.c_double * 3), ("hi_v", ctypes.c_double * 3),
                 ("cg_tol", ctypes.c_double), ("cg_max_iter", ctypes.c_int), ("guess", ctypes.c_int),
                 ("learn_rank", ctypes.c_int), ("learn_history", ctypes.c_int), ("cg_rhs_relative", ctypes.c_int),
-                ("learn_every", ctypes.c_int), ("cg_precond", ctypes.c_int), ("learn_fit", ctypes.c_int)]
+                ("learn_every", ctypes.c_int), ("cg_precond", ctypes.c_int), ("learn_fit", ctypes.c_int),
+                ("quadrature", ctypes.c_int)]
 
 
 class hd_part_layout(ctypes.Structure):

@@ -19,6 +19,7 @@
 
 #include "../../include/hyperdeal_gb300.h"
 #include "hd_ecl.cuh"
+#include "hd_rules.h"
 #include "hd_vp.cuh"
 #include "hd_vp_learn.cuh"
 
@@ -113,6 +114,35 @@ __device__ double block_sum(double v, double* sh) {
   __syncthreads();
   double s = 0.0;
   for (int k = 0; k < (int)(blockDim.x / 32); ++k) s += sh[k];
+  return s;
+}
+
+// JxW of x-quadrature point ix (Gauss-Lobatto nodes, or Gauss points with g.gauss)
+__host__ __device__ double x_qw(const VpGeom& g, int ix) {
+  double j = 1.0;
+  for (int d = 0; d < g.dx; ++d) {
+    j *= g.h[d] * (g.gauss ? g.gw[ix % g.N] : g.glw[ix % g.N]);
+    ix /= g.N;
+  }
+  return j;
+}
+
+// Gauss quadrature: sum_j M[i][j] (u_j - shift) over the x-cell of row i, M
+// the x-cell mass matrix (M1 h_d in every direction, M1 = S^T W S)
+__device__ double x_mass_row(const VpGeom& g, const double* u, long long i, double shift) {
+  const long long c0 = (i / g.NCx) * g.NCx;
+  const int il = int(i - c0);
+  double s = 0.0;
+  for (int j = 0; j < g.NCx; ++j) {
+    double w = 1.0;
+    int a = il, b = j;
+    for (int d = 0; d < g.dx; ++d) {
+      w *= g.h[d] * g.M1[(a % g.N) * g.N + (b % g.N)];
+      a /= g.N;
+      b /= g.N;
+    }
+    s = fma(w, u[c0 + j] - shift, s);
+  }
   return s;
 }
 
@@ -504,7 +534,8 @@ __global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
     const double mean = grid_sum2(grid, ls, 0.0, A.red, slot, sh).x / double(n);
     double l2 = 0.0;
     for (long long i = t0; i < n; i += stride) {
-      const double v = -(A.rho[i] - mean) * x_jxw(g, int(i % g.NCx));
+      // rhs = -M (rho - mean): the diagonal Gauss-Lobatto mass, or the Gauss one
+      const double v = g.gauss ? -x_mass_row(g, A.rho, i, mean) : -(A.rho[i] - mean) * x_jxw(g, int(i % g.NCx));
       A.rhs[i] = v;
       l2 += v;
     }
@@ -658,7 +689,22 @@ __global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
       const int idd = (ix / s) % N;
       const int base = ix - idd * s;
       double a = 0.0;
-      for (int j = 0; j < N; ++j) a += g.Dm[idd * N + j] * A.x[gx * g.NCx + base + j * s];
+      if (g.gauss) {
+        // at Gauss point ix: the derivative along d, the values (S) along the others
+        for (int j = 0; j < g.NCx; ++j) {
+          double w = 1.0;
+          int qa = ix, jb = j;
+          for (int e2 = 0; e2 < g.dx; ++e2) {
+            const int q = qa % N, jj = jb % N;
+            w *= e2 == d ? g.GS[q * N + jj] : g.S[q * N + jj];
+            qa /= N;
+            jb /= N;
+          }
+          a = fma(w, A.x[gx * g.NCx + j], a);
+        }
+      } else {
+        for (int j = 0; j < N; ++j) a += g.Dm[idd * N + j] * A.x[gx * g.NCx + base + j * s];
+      }
       const double e = a / g.h[d];
       A.E[i * g.dx + d] = e;
       const double es = e / g.h[g.dx + d];
@@ -765,13 +811,61 @@ __global__ void phase_diag_kernel(VpGeom g, const T* __restrict__ f, double* __r
   }
 }
 
+// the same partials with Gauss quadrature: one block per cell (grid-stride),
+// the cell's values taken to the Gauss points (S along every direction) in
+// shared memory (NC doubles) before they are integrated
+template <typename T>
+__global__ void phase_diag_gauss_kernel(VpGeom g, const T* __restrict__ f, double* __restrict__ partial) {
+  extern __shared__ double vq[];
+  __shared__ double sh[32];
+  const int dv = g.D - g.dx;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (long long gid = blockIdx.x; gid < g.n_cells; gid += gridDim.x) {
+    int cc[kMaxDim];
+    long long a = gid % g.ncx, b = gid / g.ncx;
+    for (int d = 0; d < g.D; ++d) {
+      if (d < g.dx) { cc[d] = int(a % g.cells[d]); a /= g.cells[d]; }
+      else { cc[d] = int(b % g.cells[d]); b /= g.cells[d]; }
+    }
+    for (int i = threadIdx.x; i < g.NC; i += blockDim.x) vq[i] = double(f[gid * g.NC + i]);
+    __syncthreads();
+    for (int e = 0; e < g.D; ++e) {
+      vp_line_pass(vq, g.S, g.N, g.D, e, threadIdx.x, blockDim.x);
+      __syncthreads();
+    }
+    for (int q = threadIdx.x; q < g.NC; q += blockDim.x) {
+      const double fv = vq[q];
+      double jxw = 1.0, vv = 0.0, vel[3] = {0, 0, 0};
+      int t = q;
+      for (int d = 0; d < g.D; ++d) {
+        const int id = t % g.N;
+        t /= g.N;
+        jxw *= g.h[d] * g.gw[id];
+        if (d >= g.dx) {
+          vel[d - g.dx] = g.lo[d] + (cc[d] + g.gq[id]) * g.h[d];
+          vv += vel[d - g.dx] * vel[d - g.dx];
+        }
+      }
+      acc[0] += fv * jxw;
+      acc[1] += fv * fv * jxw;
+      acc[2] += vv * fv * jxw;
+      for (int d = 0; d < dv; ++d) acc[3 + d] += vel[d] * fv * jxw;
+    }
+    __syncthreads();  // vq is rewritten by the next cell
+  }
+  for (int k = 0; k < 3 + dv; ++k) {
+    const double s = block_sum(acc[k], sh);
+    if (threadIdx.x == 0) partial[blockIdx.x * 6 + k] = s;
+  }
+}
+
 __global__ void energy_kernel(VpGeom g, const double* __restrict__ E, double* __restrict__ out) {
   __shared__ double sh[32];
   for (int d = 0; d < g.dx; ++d) {
     double s = 0.0;
     for (long long i = threadIdx.x; i < g.nx_dofs; i += blockDim.x) {
       const double e = E[i * g.dx + d];
-      s += e * e * x_jxw(g, int(i % g.NCx));
+      s += e * e * x_qw(g, int(i % g.NCx));
     }
     const double t = block_sum(s, sh);
     if (threadIdx.x == 0) out[d] = t;
@@ -885,6 +979,32 @@ int vcuda(cudaError_t e, const char* what) {
 }
 
 // 1D tables on [0,1] from the Gauss-Lobatto rule (same construction as the operator's)
+// inverse of a small dense matrix (Gauss-Jordan, partial pivoting); false if singular
+bool invert_small(int n, const double* A, double* Ai) {
+  double a[hd::kMaxN][2 * hd::kMaxN];
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < 2 * n; ++j) a[i][j] = j < n ? A[i * n + j] : (j - n == i ? 1.0 : 0.0);
+  for (int k = 0; k < n; ++k) {
+    int piv = k;
+    for (int i = k + 1; i < n; ++i)
+      if (std::fabs(a[i][k]) > std::fabs(a[piv][k])) piv = i;
+    if (!(std::fabs(a[piv][k]) > 0.0)) return false;
+    if (piv != k)
+      for (int j = 0; j < 2 * n; ++j) std::swap(a[k][j], a[piv][j]);
+    const double dk = 1.0 / a[k][k];
+    for (int j = 0; j < 2 * n; ++j) a[k][j] *= dk;
+    for (int i = 0; i < n; ++i) {
+      if (i == k) continue;
+      const double f = a[i][k];
+      if (f != 0.0)
+        for (int j = 0; j < 2 * n; ++j) a[i][j] -= f * a[k][j];
+    }
+  }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) Ai[i * n + j] = a[i][n + j];
+  return true;
+}
+
 void vp_tables(int n, double* x, double* w, double* D) {
   const int m = n - 1;
   auto legendre = [](int nn, double z, double* p, double* dp) {
@@ -965,6 +1085,98 @@ void vp_free(hd_vp* v) {
   cudaFree(v->d_redk);
   hd::vp_model_destroy(v->model);
   delete v;
+}
+
+// The SIPG matrix with Gauss quadrature, assembled on the host into the ELL
+// arrays (row i: W = NCx (1 + 2 dim_x) entries, [k][i]).  With values and
+// gradients taken to the Gauss points through S and GS, the bilinear form of
+// poisson.h:131-255 is a sum of tensor products: the cell term
+// sum_d K_d (x) prod_{e != d} M_e and, for every face normal to d, the
+// one-dimensional face matrix F_d on the two cells' lines times the
+// tangential masses -- K = GS^T W GS / h, M = S^T W S h, and
+// F = sigma j j^T - j m^T - m j^T with j = (e_{N-1}, -e_0) the jump and
+// m = (l'(1), l'(0)) / (2h) the mean normal derivative of the two cells'
+// nodal bases.  All x-cells have the same extents, so the blocks are the same
+// for every cell; columns that coincide (1 or 2 cells along a direction,
+// periodic) are summed.
+void assemble_sipg_gauss(const hd::VpGeom& g, int W, std::vector<int>& col, std::vector<double>& val) {
+  const int N = g.N, m = g.NCx, dx = g.dx;
+  const long long nx = g.nx_dofs;
+  std::vector<double> K(N * N), M(N * N);
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j) {
+      double k = 0.0, mm = 0.0;
+      for (int q = 0; q < N; ++q) {
+        k += g.gw[q] * g.GS[q * N + i] * g.GS[q * N + j];
+        mm += g.gw[q] * g.S[q * N + i] * g.S[q * N + j];
+      }
+      K[i * N + j] = k;
+      M[i * N + j] = mm;
+    }
+  // blocks: own (row cell c), plus[d] (column cell c + e_d), minus[d] (c - e_d)
+  std::vector<double> own(size_t(m) * m, 0.0), plus(size_t(dx) * m * m, 0.0), minus(size_t(dx) * m * m, 0.0);
+  for (int d = 0; d < dx; ++d) {
+    const double h = g.h[d], sigma = (1.0 / h + 1.0 / h) * g.pen;
+    double jv[2 * hd::kMaxN], mv[2 * hd::kMaxN], F[4 * hd::kMaxN * hd::kMaxN];
+    for (int i = 0; i < N; ++i) {
+      jv[i] = i == N - 1 ? 1.0 : 0.0;
+      jv[N + i] = i == 0 ? -1.0 : 0.0;
+      mv[i] = 0.5 * g.Dm[(N - 1) * N + i] / h;
+      mv[N + i] = 0.5 * g.Dm[i] / h;
+    }
+    for (int a = 0; a < 2 * N; ++a)
+      for (int b = 0; b < 2 * N; ++b) F[a * 2 * N + b] = sigma * jv[a] * jv[b] - jv[a] * mv[b] - mv[a] * jv[b];
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) {
+        double t = 1.0;  // tangential mass
+        int a = i, b = j, id = 0, jd = 0;
+        for (int e = 0; e < dx; ++e) {
+          if (e == d) { id = a % N; jd = b % N; }
+          else t *= M[(a % N) * N + (b % N)] * g.h[e];
+          a /= N;
+          b /= N;
+        }
+        own[size_t(i) * m + j] += (K[id * N + jd] / h + F[(N + id) * 2 * N + N + jd] + F[id * 2 * N + jd]) * t;
+        plus[(size_t(d) * m + i) * m + j] = F[id * 2 * N + N + jd] * t;
+        minus[(size_t(d) * m + i) * m + j] = F[(N + id) * 2 * N + jd] * t;
+      }
+  }
+  col.assign(size_t(W) * nx, 0);
+  val.assign(size_t(W) * nx, 0.0);
+  std::vector<long long> cols;
+  std::vector<double> vals;
+  for (long long gx = 0; gx < g.ncx; ++gx) {
+    int cc[3] = {0, 0, 0};
+    long long t = gx;
+    for (int d = 0; d < dx; ++d) { cc[d] = int(t % g.cells[d]); t /= g.cells[d]; }
+    for (int i = 0; i < m; ++i) {
+      const long long row = gx * m + i;
+      cols.clear();
+      vals.clear();
+      auto add = [&](long long cell, const double* blk) {
+        for (int j = 0; j < m; ++j) {
+          const long long c2 = cell * m + j;
+          const double a = blk[size_t(i) * m + j];
+          size_t k = 0;
+          while (k < cols.size() && cols[k] != c2) ++k;
+          if (k == cols.size()) { cols.push_back(c2); vals.push_back(a); }
+          else vals[k] += a;
+        }
+      };
+      add(gx, own.data());
+      for (int d = 0; d < dx; ++d) {
+        const long long cs = g.cstride[d];
+        const long long gp = cc[d] + 1 < g.cells[d] ? gx + cs : gx - (long long)(g.cells[d] - 1) * cs;
+        const long long gm = cc[d] > 0 ? gx - cs : gx + (long long)(g.cells[d] - 1) * cs;
+        add(gp, plus.data() + size_t(d) * m * m);
+        add(gm, minus.data() + size_t(d) * m * m);
+      }
+      for (int k = 0; k < W; ++k) {
+        col[size_t(k) * nx + row] = int(k < (int)cols.size() ? cols[k] : row);
+        val[size_t(k) * nx + row] = k < (int)cols.size() ? vals[k] : 0.0;
+      }
+    }
+  }
 }
 
 // Cell-block Jacobi preconditioner: the diagonal block of every x-cell (the
@@ -1193,6 +1405,8 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
        (d.learn_rank > 0 && d.learn_history >= d.learn_rank)))
     return vfail(HD_ERR_INVALID, "hd_vp_create: least-squares guess needs learn_rank <= 16 and "
                                  "learn_history < learn_rank");
+  if (d.quadrature != HD_QUAD_GAUSS_LOBATTO && d.quadrature != HD_QUAD_GAUSS)
+    return vfail(HD_ERR_INVALID, "hd_vp_create: unknown quadrature");
   hd_vp* v = new (std::nothrow) hd_vp;
   if (!v) return vfail(HD_ERR_ALLOC, "out of host memory");
   std::memset(v, 0, sizeof(*v));
@@ -1236,6 +1450,45 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
       g.G[i * N + j] = g.Dm[j * N + i] * g.glw[j] / g.glw[i];
     }
   g.pen = double(d.degree > 1 ? d.degree : 1) * (d.degree + 1.0);
+  g.gauss = d.quadrature == HD_QUAD_GAUSS;
+  if (g.gauss) {
+    // Gauss points and the tables of the non-collocation path (hd_vp.cuh)
+    hd::rules::gauss_rule(N, g.gq, g.gw);
+    double Dg[hd::kMaxN * hd::kMaxN], f0[hd::kMaxN], f1[hd::kMaxN];
+    hd::rules::lagrange_derivative_matrix(N, g.gq, Dg);  // Dg[q*N + j] = L_j'(gq_q), Gauss-point basis
+    for (int q = 0; q < N; ++q) {
+      f0[q] = hd::rules::lagrange_value(N, g.gq, q, 0.0);
+      f1[q] = hd::rules::lagrange_value(N, g.gq, q, 1.0);
+      for (int j = 0; j < N; ++j) g.S[q * N + j] = hd::rules::lagrange_value(N, g.gl, j, g.gq[q]);
+    }
+    for (int q = 0; q < N; ++q)
+      for (int j = 0; j < N; ++j) {
+        double a = 0.0, m = 0.0;
+        for (int k = 0; k < N; ++k) {
+          a += Dg[q * N + k] * g.S[k * N + j];
+          m += g.gw[k] * g.S[k * N + q] * g.S[k * N + j];
+        }
+        g.GS[q * N + j] = a;
+        g.M1[q * N + j] = m;
+      }
+    if (!invert_small(N, g.S, g.Si)) { delete v; return vfail(HD_ERR_INVALID, "hd_vp_create: singular basis change"); }
+    // line operators in the Gauss-point basis (advection_operation.h:325-526 with
+    // the flux 0.5((u- + u+) a.n + |a.n| (u- - u+)) on both faces, divided by the weights)
+    for (int i = 0; i < N; ++i) {
+      for (int q = 0; q < N; ++q) {
+        const double vol = Dg[q * N + i] * g.gw[q];
+        g.Ap[i * N + q] = (vol - f1[i] * f1[q]) / g.gw[i];
+        g.Am[i * N + q] = (vol + f0[i] * f0[q]) / g.gw[i];
+      }
+      g.cp[i] = f0[i] / g.gw[i];
+      g.cm[i] = -f1[i] / g.gw[i];
+    }
+    const size_t smem = size_t(d.dtype == HD_F64 ? 8 : 4) * (size_t(2) * g.NC + size_t(2) * g.D * (g.NC / N));
+    if (smem > 220 * 1024) {
+      delete v;
+      return vfail(HD_ERR_UNSUPPORTED, "hd_vp_create: Gauss quadrature up to 3x+3v degree 3 (FP64)");
+    }
+  }
   // the advection kernel keeps two copies of CTA's cells in shared memory: 3x+3v up to degree 3
   if (g.D == 6 && N > 4) { delete v; return vfail(HD_ERR_UNSUPPORTED, "hd_vp_create: 3x+3v only for degree <= 3"); }
   for (int i = 0; i < g.dx; ++i)
@@ -1265,7 +1518,7 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
   alloc(&v->d_es, sizeof(double) * nx * g.dx);
   alloc(&v->d_xs, sizeof(double) * g.dx * 64 * hd::kMaxN);
   alloc((void**)&v->d_cg, sizeof(double) * (5 * nx + 6 * v->cg_grid));
-  v->ell_w = 3 * N * g.dx;
+  v->ell_w = g.gauss ? g.NCx * (1 + 2 * g.dx) : 3 * N * g.dx;
   alloc((void**)&v->d_ell_col, sizeof(int) * size_t(v->ell_w) * nx);
   alloc((void**)&v->d_ell_val, sizeof(double) * size_t(v->ell_w) * nx);
   alloc((void**)&v->d_stats, sizeof(hd::VpStats));
@@ -1298,7 +1551,7 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
         const int e2 = g.dx + d2;
         for (int c = 0; c < g.cells[e2]; ++c)
           for (int i = 0; i < N; ++i, ++k) {
-            xs64[k] = (g.lo[e2] + (c + g.gl[i]) * g.h[e2]) / g.h[d2];
+            xs64[k] = (g.lo[e2] + (c + (g.gauss ? g.gq[i] : g.gl[i])) * g.h[e2]) / g.h[d2];
             xs32[k] = float(xs64[k]);
           }
       }
@@ -1308,7 +1561,13 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
     }
     if (e == cudaSuccess) e = cudaMemset(v->d_es, 0, sizeof(double) * nx * g.dx);
     if (e == cudaSuccess) e = cudaMemset(v->d_stats, 0, sizeof(hd::VpStats));
-    if (e == cudaSuccess) {
+    if (e == cudaSuccess && g.gauss) {
+      std::vector<int> col;
+      std::vector<double> val;
+      assemble_sipg_gauss(g, v->ell_w, col, val);
+      e = cudaMemcpy(v->d_ell_col, col.data(), sizeof(int) * col.size(), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMemcpy(v->d_ell_val, val.data(), sizeof(double) * val.size(), cudaMemcpyHostToDevice);
+    } else if (e == cudaSuccess) {
       hd::assemble_sipg_ell<<<unsigned((nx + 127) / 128), 128>>>(g, v->ell_w, v->d_ell_col, v->d_ell_val);
       e = cudaGetLastError();
     }
@@ -1453,8 +1712,20 @@ int hd_vp_diagnostics(hd_vp* v, const void* f, double* out, void* stream) {
   const int blocks = 152 * 16, dv = g.D - g.dx;
   double* part = v->d_diag;
   double* res = v->d_diag + blocks * 6;
-  if (v->dtype == HD_F32) hd::phase_diag_kernel<float><<<blocks, 256, 0, s>>>(g, (const float*)f, part);
-  else hd::phase_diag_kernel<double><<<blocks, 256, 0, s>>>(g, (const double*)f, part);
+  if (g.gauss) {
+    const size_t sm = sizeof(double) * g.NC;
+    if (v->dtype == HD_F32) {
+      cudaFuncSetAttribute(hd::phase_diag_gauss_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+      hd::phase_diag_gauss_kernel<float><<<blocks, 128, sm, s>>>(g, (const float*)f, part);
+    } else {
+      cudaFuncSetAttribute(hd::phase_diag_gauss_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+      hd::phase_diag_gauss_kernel<double><<<blocks, 128, sm, s>>>(g, (const double*)f, part);
+    }
+  } else if (v->dtype == HD_F32) {
+    hd::phase_diag_kernel<float><<<blocks, 256, 0, s>>>(g, (const float*)f, part);
+  } else {
+    hd::phase_diag_kernel<double><<<blocks, 256, 0, s>>>(g, (const double*)f, part);
+  }
   hd::diag_finish<<<1, 1024, 0, s>>>(blocks, 3 + dv, part, res);
   hd::energy_kernel<<<1, 1024, 0, s>>>(g, v->d_E, res + 8);
   int rc = vcuda(cudaGetLastError(), "vp diagnostics");
@@ -1500,8 +1771,8 @@ int hd_vp_set_arithmetic(hd_vp* v, int arithmetic) {
   if (!v) return vfail(HD_ERR_INVALID, "hd_vp_set_arithmetic: null handle");
   if (arithmetic != HD_ARITH_NATIVE && arithmetic != HD_ARITH_FP32X2)
     return vfail(HD_ERR_INVALID, "unknown arithmetic");
-  if (arithmetic == HD_ARITH_FP32X2 && (v->dtype != HD_F64 || v->g.dx > 2))
-    return vfail(HD_ERR_UNSUPPORTED, "FP32x2 arithmetic needs FP64 storage and dim_x = dim_v <= 2");
+  if (arithmetic == HD_ARITH_FP32X2 && (v->dtype != HD_F64 || v->g.dx > 2 || v->g.gauss))
+    return vfail(HD_ERR_UNSUPPORTED, "FP32x2 arithmetic needs FP64 storage, collocation and dim_x = dim_v <= 2");
   v->arith = arithmetic;
   return HD_OK;
 }

@@ -497,8 +497,153 @@ static cudaError_t launch_vp_dn(const VpAdvParams<T>& P, int mode, cudaStream_t 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Gauss quadrature.  One CTA per cell (grid-stride): the cell's nodal values
+// are transformed to the Gauss points (S along every direction), both
+// neighbours' traces of every direction are gathered -- the neighbour's
+// Gauss-Lobatto end-node slab, S along the tangential directions -- and every
+// line of every direction adds (a/h)(A v + c u_up) with the operator of its
+// velocity's sign; S^{-1} along every direction takes the result back to
+// nodal values.  Shared memory (T): v and r (NC each), the 2D traces (NC/N
+// each).  Runtime D and N; this path serves the reference's Gauss cases, not
+// the benchmark's collocation meshes.
+
+template <typename T, int MODE>
+__global__ void vp_gauss_kernel(VpAdvParams<T> P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const VpGeom& g = P.g;
+  const int D = g.D, N = g.N, NC = g.NC, DX = g.dx, NF = NC / N;
+  T* v = reinterpret_cast<T*>(smem_raw);
+  T* r = v + NC;
+  T* face = r + NC;  // [2 d + side][NF]: side 0 the left neighbour's trace, 1 the right one's
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  for (long long gid = blockIdx.x; gid < g.n_cells; gid += gridDim.x) {
+    int cc[kMaxDim];
+    long long nb[kMaxDim][2];
+    const long long gx = gid % g.ncx;
+    {
+      long long a = gx, b = gid / g.ncx;
+      for (int d = 0; d < D; ++d) {
+        if (d < DX) { cc[d] = int(a % g.cells[d]); a /= g.cells[d]; }
+        else { cc[d] = int(b % g.cells[d]); b /= g.cells[d]; }
+        const long long cs = g.cstride[d];
+        nb[d][0] = cc[d] > 0 ? gid - cs : gid + (long long)(g.cells[d] - 1) * cs;
+        nb[d][1] = cc[d] + 1 < g.cells[d] ? gid + cs : gid - (long long)(g.cells[d] - 1) * cs;
+      }
+    }
+    for (int i = tid; i < NC; i += nthr) v[i] = P.src[gid * NC + i];
+    // traces: the left neighbour's slab i_d = N-1, the right one's slab i_d = 0,
+    // stored with the digit d removed
+    for (int k = tid; k < 2 * D * NF; k += nthr) {
+      const int fd = k / (2 * NF), side = (k / NF) % 2, l = k % NF;
+      int sd = 1;
+      for (int f = 0; f < fd; ++f) sd *= N;
+      const int node = (l % sd) + (side ? 0 : N - 1) * sd + (l / sd) * sd * N;
+      face[k] = P.src[nb[fd][side] * NC + node];
+    }
+    __syncthreads();
+    for (int e = 0; e < D; ++e) {
+      vp_line_pass(v, g.S, N, D, e, tid, nthr);
+      __syncthreads();
+    }
+    // tangential S on every trace: face fd, face-local direction t (rank of e != fd)
+    for (int t = 0; t < D - 1; ++t) {
+      for (int fs = 0; fs < 2 * D; ++fs) vp_line_pass(face + fs * NF, g.S, N, D - 1, t, tid, nthr);
+      __syncthreads();
+    }
+    for (int i = tid; i < NC; i += nthr) r[i] = T(0);
+    __syncthreads();
+    for (int d = 0; d < D; ++d) {
+      int sd = 1;
+      for (int f = 0; f < d; ++f) sd *= N;
+      for (int line = tid; line < NF; line += nthr) {
+        const int base = (line % sd) + (line / sd) * sd * N;  // node of the line with i_d = 0
+        // velocity / h of the line: x-direction d moves with v_d at the line's
+        // v-point, v-direction d with d_d phi at the line's x-point
+        T a;
+        if (d < DX) {
+          const int e = DX + d;
+          int se = 1;
+          for (int f = 0; f < e; ++f) se *= N;
+          a = __ldg(P.xs + (d * g.cells[e] + cc[e]) * N + (base / se) % N);
+        } else {
+          int sx = 1;
+          for (int f = 0; f < DX; ++f) sx *= N;
+          a = __ldg(P.es + (gx * g.NCx + (base % sx)) * DX + (d - DX));
+        }
+        const bool pos = a > T(0);
+        const double* Am = pos ? g.Ap : g.Am;
+        const double* cv = pos ? g.cp : g.cm;
+        const T up = face[(2 * d + (pos ? 0 : 1)) * NF + line];
+        T u[kMaxN];
+        for (int j = 0; j < N; ++j) u[j] = v[base + j * sd];
+        for (int i = 0; i < N; ++i) {
+          T acc = T(cv[i]) * up;
+          for (int j = 0; j < N; ++j) acc = fma(T(Am[i * N + j]), u[j], acc);
+          r[base + i * sd] += a * acc;
+        }
+      }
+      __syncthreads();
+    }
+    for (int e = 0; e < D; ++e) {
+      vp_line_pass(r, g.Si, N, D, e, tid, nthr);
+      __syncthreads();
+    }
+    for (int i = tid; i < NC; i += nthr) {
+      const long long gi = gid * NC + i;
+      const T k = r[i];
+      if constexpr (MODE == kApply) {
+        P.dst[gi] = k;
+      } else {
+        const T u = (MODE == kStageFirst) ? P.src[gi] : P.uin[gi];
+        P.dst[gi] = fma(P.fb, k, u);
+        if constexpr (MODE != kStageLast) P.tout[gi] = fma(P.fa, k, u);
+      }
+    }
+    __syncthreads();  // v, r and the traces are reused by the next cell
+  }
+}
+
+// shared memory of the Gauss kernel for a geometry (bytes)
+template <typename T>
+static size_t vp_gauss_smem(const VpGeom& g) {
+  return sizeof(T) * (size_t(2) * g.NC + size_t(2) * g.D * (g.NC / g.N));
+}
+
+template <typename T>
+static cudaError_t launch_vp_gauss(const VpAdvParams<T>& P, int mode, cudaStream_t s) {
+  const size_t smem = vp_gauss_smem<T>(P.g);
+  if (smem > 220 * 1024) return cudaErrorNotSupported;
+  const int threads = 128;
+  static int sms = 0;
+  auto go = [&](auto kern) -> cudaError_t {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    if (!sms) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    const long long want = (long long)sms * per_sm;
+    kern<<<unsigned(P.g.n_cells < want ? P.g.n_cells : want), threads, smem, s>>>(P);
+    return cudaGetLastError();
+  };
+  switch (mode) {
+    case kApply: return go(vp_gauss_kernel<T, kApply>);
+    case kStageFirst: return go(vp_gauss_kernel<T, kStageFirst>);
+    case kStageMid: return go(vp_gauss_kernel<T, kStageMid>);
+    case kStageLast: return go(vp_gauss_kernel<T, kStageLast>);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 template <typename T>
 static cudaError_t launch_vp_any(const VpAdvParams<T>& P, int mode, cudaStream_t s, bool x2) {
+  if (P.g.gauss) return x2 ? cudaErrorNotSupported : launch_vp_gauss(P, mode, s);
 #define HD_VP_CASE(DD, NN) \
   if (P.g.D == DD && P.g.N == NN) return launch_vp_dn<DD, NN, T>(P, mode, s, x2);
   HD_VP_CASE(2, 2) HD_VP_CASE(2, 3) HD_VP_CASE(2, 4) HD_VP_CASE(2, 5) HD_VP_CASE(2, 6)

@@ -13,7 +13,8 @@ least-squares fit of the recent pairs, computed inside the Poisson launch;
 with ``learn_fit="adam"`` FP32 weights trained by Adam on the differences
 between consecutive solves.  Diagnostics follow diagnostics.h:28-141.
 
-Gauss-Lobatto collocation, dim_x == dim_v, periodic x- and v-meshes.
+Gauss-Lobatto collocation or Gauss quadrature, dim_x == dim_v, periodic x- and
+v-meshes.
 """
 from __future__ import annotations
 
@@ -56,6 +57,7 @@ class VlasovPoissonParameters:
     learn_every: int = 0  # Adam steps every n-th solve (0: every solve)
     cg_precond: str = "block_jacobi"  # "none" or "block_jacobi" (x-cell diagonal blocks of the SIPG matrix)
     learn_fit: str = "least_squares"  # or "adam" (hd_vp_learn_fit)
+    quadrature: str = "gauss_lobatto"  # or "gauss" (n_points = degree + 1, the reference's non-collocation runs)
 
     def c(self) -> _lib.hd_vp_desc:
         d = _lib.hd_vp_desc()
@@ -77,6 +79,7 @@ class VlasovPoissonParameters:
         d.cg_precond = {"none": _lib.HD_VP_PRECOND_NONE, "block_jacobi": _lib.HD_VP_PRECOND_BLOCK_JACOBI}[
             self.cg_precond]
         d.learn_fit = {"least_squares": _lib.HD_VP_FIT_LEAST_SQUARES, "adam": _lib.HD_VP_FIT_ADAM}[self.learn_fit]
+        d.quadrature = {"gauss_lobatto": _lib.HD_QUAD_GAUSS_LOBATTO, "gauss": _lib.HD_QUAD_GAUSS}[self.quadrature]
         return d
 
 
@@ -224,7 +227,8 @@ def learn_loss_grad(W1: torch.Tensor, W2: torch.Tensor, X: torch.Tensor, Y: torc
 
 def run_hyperrectangle(dim_x: int = 2, degree: int = 3, cells_x: int = 4, cells_v: int = 4, dtype: str = "f64",
                        final_time: float = 0.5, time_step: float = 0.1, cfl: float = 0.05, tick: float = 0.1,
-                       rk: str = "rk45", cg_tol: float = 1e-12, guess: str = "previous"):
+                       rk: str = "rk45", cg_tol: float = 1e-12, guess: str = "previous",
+                       quadrature: str = "gauss_lobatto"):
     """The reference's Vlasov-Poisson application on its hyperrectangle case: x in [0, 4 pi]^dim_x,
     v in [-6, 6]^dim_x, periodic, the time-step rule with transport velocity (1, .., 6, ..)
     (examples/vlasov_poisson/cases/hyperrectangle.h, application.h:345-602).  Returns the
@@ -232,7 +236,7 @@ def run_hyperrectangle(dim_x: int = 2, degree: int = 3, cells_x: int = 4, cells_
     and the operator."""
     params = VlasovPoissonParameters(dim_x, degree, [cells_x] * dim_x, [cells_v] * dim_x, [0.0] * dim_x,
                                      [4 * math.pi] * dim_x, [-6.0] * dim_x, [6.0] * dim_x, dtype=dtype,
-                                     cg_tol=cg_tol, guess=guess)
+                                     cg_tol=cg_tol, guess=guess, quadrature=quadrature)
     op = VlasovPoissonOperation(params)
     sol = op.initialize_dof_vector()
     op.interpolate(perturbed_maxwellian(dim_x), sol)

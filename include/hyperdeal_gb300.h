@@ -359,7 +359,8 @@ int hd_batch_autotune(hd_batch *b, const void *const *src, void *const *dst, int
 /* ---- Vlasov-Poisson ------------------------------------------------------- */
 
 /* Electrostatic Vlasov-Poisson on periodic x- and v-meshes (dim_x == dim_v),
- * Gauss-Lobatto collocation: one right-hand-side evaluation computes the
+ * Gauss-Lobatto collocation or Gauss quadrature (hd_vp_desc::quadrature):
+ * one right-hand-side evaluation computes the
  * charge density rho(x) = int f dv, solves the SIPG Poisson problem for the
  * potential by conjugate gradients in FP64, takes E = grad(phi) at the
  * x-nodes and applies the advection operator with the phase-space velocity
@@ -418,6 +419,12 @@ typedef struct hd_vp_desc {
                            solve (0: 1, every solve)                          */
   int cg_precond;       /* enum hd_vp_precond (0: none)                       */
   int learn_fit;        /* enum hd_vp_learn_fit (0: least squares)            */
+  int quadrature;       /* enum hd_quadrature: Gauss-Lobatto collocation (0)
+                           or Gauss points (n_points = degree + 1; DoFs stay
+                           Gauss-Lobatto nodal values; rho, E and every
+                           integral at the Gauss points as the reference's
+                           non-collocation runs; up to 3x+3v degree 3 in
+                           FP64; FP32x2 arithmetic refused)                  */
 } hd_vp_desc;
 
 typedef struct hd_vp hd_vp;

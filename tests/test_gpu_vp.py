@@ -23,15 +23,16 @@ if torch.cuda.is_available():
 
 
 def _setup(dim_x, degree, cx, cv, dtype="f64", guess="previous", cg_tol=1e-12, rhs_relative=False,
-           cg_precond="block_jacobi", learn_fit="least_squares"):
+           cg_precond="block_jacobi", learn_fit="least_squares", quadrature="gauss_lobatto"):
     D = 2 * dim_x
     lo = [0.0] * dim_x + [-6.0] * dim_x
     hi = [4 * math.pi] * dim_x + [6.0] * dim_x
     params = V.VlasovPoissonParameters(dim_x, degree, [cx] * dim_x, [cv] * dim_x, lo[:dim_x], hi[:dim_x],
                                        lo[dim_x:], hi[dim_x:], dtype=dtype, cg_tol=cg_tol, guess=guess,
-                                       cg_rhs_relative=rhs_relative, cg_precond=cg_precond, learn_fit=learn_fit)
+                                       cg_rhs_relative=rhs_relative, cg_precond=cg_precond, learn_fit=learn_fit,
+                                       quadrature=quadrature)
     prob = O.Problem(dim_x, dim_x, degree, [cx] * dim_x + [cv] * dim_x, lo, hi, [1.0] * dim_x + [6.0] * dim_x,
-                     collocation=True)
+                     collocation=quadrature == "gauss_lobatto")
     assert len(lo) == D
     return V.VlasovPoissonOperation(params), prob
 
@@ -43,9 +44,16 @@ def _rel(a, b):
 CASES = [(1, 3, 8, 8), (2, 3, 4, 4), (2, 2, 3, 5), (3, 2, 2, 2)]
 
 
+QUADS = ["gauss_lobatto", "gauss"]
+
+
+@pytest.mark.parametrize("quadrature", QUADS)
 @pytest.mark.parametrize("dim_x,degree,cx,cv", CASES)
-def test_interpolate_moment_rhs_field(dim_x, degree, cx, cv):
-    op, prob = _setup(dim_x, degree, cx, cv, guess="zero")
+def test_interpolate_moment_rhs_field(dim_x, degree, cx, cv, quadrature):
+    """With Gauss quadrature the right-hand side takes the Gauss mass matrix, the SIPG matrix the
+    Gauss-point integrals, and the field lives at the Gauss points -- each against the oracle's
+    non-collocation branch."""
+    op, prob = _setup(dim_x, degree, cx, cv, guess="zero", quadrature=quadrature)
     f0 = V.perturbed_maxwellian(dim_x, perturbed_dims=tuple(range(dim_x)))
     f = op.initialize_dof_vector()
     op.interpolate(f0, f)
@@ -68,10 +76,11 @@ def test_interpolate_moment_rhs_field(dim_x, degree, cx, cv):
     assert st["solves"] == 1 and st["last_iterations"] > 0 and st["last_residual"] <= 1e-12
 
 
+@pytest.mark.parametrize("quadrature", QUADS)
 @pytest.mark.parametrize("dim_x,degree,cx,cv", CASES)
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
-def test_apply_matches_oracle(dim_x, degree, cx, cv, dtype):
-    op, prob = _setup(dim_x, degree, cx, cv, dtype=dtype)
+def test_apply_matches_oracle(dim_x, degree, cx, cv, dtype, quadrature):
+    op, prob = _setup(dim_x, degree, cx, cv, dtype=dtype, quadrature=quadrature)
     rng = np.random.default_rng(7 + dim_x * 10 + degree)
     fo = O.interpolate(prob, O.vp_initial_function(dim_x, dim_x, eps=0.2))
     fo = fo * (1.0 + 0.05 * rng.standard_normal(fo.size))
@@ -92,6 +101,51 @@ def test_apply_matches_oracle(dim_x, degree, cx, cv, dtype):
     assert _rel(dst2.cpu().numpy(), dst.cpu().numpy()) <= (1e-10 if dtype == "f64" else 1e-5)
 
 
+def test_gauss_golden_vp_2D_2D_k3_hyperrectangle_01():
+    """The reference's Vlasov-Poisson golden examples/vlasov_poisson/tests/vp_2D_2D_k3.hyperrectangle_01
+    (2x2v, k = 3, 4 cells per direction, Gauss quadrature with k + 1 points, rk45 to t = 0.5) replayed
+    on the GPU through the C ABI: every diagnostics row within numdiff's tolerances, mass, L2 norm
+    and kinetic energy to 1e-12, the field energy to 1e-7 (the reference solves Poisson with
+    multigrid to a 1e-4 reduction)."""
+    from test_oracle_golden import GOLD, numdiff_equal
+    case = GOLD["vlasov_poisson"][0]
+    assert case["name"] == "vp_2D_2D_k3.hyperrectangle_01" and not case["collocation"]
+    rows, op = V.run_hyperrectangle(case["dim_x"], case["degree"], case["cells_x"], case["cells_v"],
+                                    final_time=case["final_time"], time_step=case["time_step"], cfl=case["cfl"],
+                                    quadrature="gauss")
+    ref = case["rows"]
+    assert len(rows) == len(ref)
+    dx = case["dim_x"]
+    for r, g in zip(rows, ref):
+        assert abs(r[0] - g[0]) <= 1e-3
+        got, exp = list(r[1:]), g[1:]
+        for a, b in zip(got, exp):
+            assert numdiff_equal(a, b), (r[0], a, b)
+        for a, b in zip(got[dx:dx + 3], exp[dx:dx + 3]):
+            assert abs(a - b) <= 1e-12 * abs(b), (r[0], a, b)
+        if g[1] > 1e-6:
+            assert abs(got[0] - g[1]) <= 1e-7 * g[1], (r[0], got[0], g[1])
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_gauss_fused_step_equals_unfused_and_refuses_fp32x2(dtype):
+    dim_x, degree, cx, cv = 2, 3, 4, 6
+    out = {}
+    for fused in (True, False):
+        op, _ = _setup(dim_x, degree, cx, cv, dtype=dtype, guess="zero", quadrature="gauss")
+        f = op.initialize_dof_vector()
+        op.interpolate(V.perturbed_maxwellian(dim_x, eps=0.05, perturbed_dims=(0, 1)), f)
+        Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
+        integ = V.LowStorageRungeKuttaIntegrator(Ki, Ti, "rk45", fused=fused)
+        for s in range(3):
+            op.perform_time_step(integ, f, s * 1e-3, 1e-3)
+        out[fused] = f.double().cpu().numpy()
+    assert _rel(out[True], out[False]) <= (1e-12 if dtype == "f64" else 2e-6)
+    if dtype == "f64":
+        with pytest.raises(V.HdError):
+            op.set_arithmetic("fp32x2")
+
+
 def test_apply_rejects_bad_input():
     op, _ = _setup(1, 3, 4, 4)
     a = op.initialize_dof_vector()
@@ -104,11 +158,12 @@ def test_apply_rejects_bad_input():
                                                            cg_tol=0.0))
 
 
+@pytest.mark.parametrize("quadrature", QUADS)
 @pytest.mark.parametrize("dim_x,degree,cells", [(1, 3, 8), (2, 3, 4)])
-def test_time_loop_diagnostics_match_oracle(dim_x, degree, cells):
-    rows, op = V.run_hyperrectangle(dim_x, degree, cells, cells, final_time=0.05, tick=0.01)
-    rows_o, st = O.run_vp_hyperrectangle(dim_x, dim_x, degree, cells, cells, collocation=True, final_time=0.05,
-                                         tick=0.01)
+def test_time_loop_diagnostics_match_oracle(dim_x, degree, cells, quadrature):
+    rows, op = V.run_hyperrectangle(dim_x, degree, cells, cells, final_time=0.05, tick=0.01, quadrature=quadrature)
+    rows_o, st = O.run_vp_hyperrectangle(dim_x, dim_x, degree, cells, cells,
+                                         collocation=quadrature == "gauss_lobatto", final_time=0.05, tick=0.01)
     assert len(rows) == len(rows_o) and len(rows) >= 5
     for r, ro in zip(rows, rows_o):
         assert abs(r[0] - ro[0]) <= 1e-14
