@@ -592,7 +592,7 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
   const double* uu = uu_all ? uu_all + lc * CST : nullptr;
   const long long g0 = gid * NC;
 
-#pragma unroll 1
+#pragma unroll
   for (int ph = 0; ph < S::NPH; ++ph) {
     const int dA = 2 * ph;
     const int dB = (2 * ph + 1 < D) ? 2 * ph + 1 : -1;
@@ -606,7 +606,7 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
     const bool lastph = ph == S::NPH - 1;
     for (int item = tl; item < nitems; item += TPC) {
       const int base = item_base<D, N>(item, dA, dB);
-#pragma unroll 1
+#pragma unroll
       for (int dd = 0; dd < ndir; ++dd) {
         // (dB is -1 in the single-direction phase of an odd dimension; d never
         // takes that value, even where a compiler evaluates this ahead of the
@@ -617,6 +617,12 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
         const LineOp<f32x2>& L = P.opx[d];
         const bool act = valid && L.active;
         const long long nb = act ? neighbour(P, gg, cc, d) : -1;
+        // the direction's coefficients in registers for its lines (d is not a
+        // compile-time index here: each use would be a constant-bank load)
+        f32x2 Mr[N * N];
+#pragma unroll
+        for (int k = 0; k < N * N; ++k) Mr[k] = L.M[k];
+        const f32x2 cin = L.cin;
         const bool first = ph == 0 && dd == 0;
         const bool fin = lastph && dd == ndir - 1;
         // upwind trace (here or in the ghost region; cell 0 where there is no
@@ -665,13 +671,13 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
 #pragma unroll
             for (int i = 0; i < N; ++i)
 #pragma unroll
-              for (int q = 0; q < N; ++q) x2_mac(acc[i], L.M[i * N + q], u[q]);
+              for (int q = 0; q < N; ++q) x2_mac(acc[i], Mr[i * N + q], u[q]);
             const int in = L.in_node;
             const double upv =
                 nb >= 0 ? upd : boundary_value<D, N, double>(P, cc, d, lb + in * st, x2_to_double(sx[lb + in * st]));
             const f32x2 up = x2_from_double(upv);
-            if (in == 0) x2_mac(acc[0], L.cin, up);
-            else x2_mac(acc[N - 1], L.cin, up);
+            if (in == 0) x2_mac(acc[0], cin, up);
+            else x2_mac(acc[N - 1], cin, up);
           }
           if (!fin) {
             if ((N % 2) == 0 && st == 1) {
