@@ -2,7 +2,7 @@
 (-DHD_CHECK: every global load and store of the ECL kernels checks its index and
 records a violation in the device status, status 4, instead of accessing
 memory), plus a sweep that asserts status 0 after launches of every generic
-kernel shape.  Building the checked library takes minutes, so this runs only
+kernel shape (FP64 storage in both arithmetics).  Building the checked library takes minutes, so this runs only
 when HYPERDEAL_GB300_RUN_CHECK_BUILD=1 is set:
 
     HYPERDEAL_GB300_RUN_CHECK_BUILD=1 python -m pytest tests/test_gpu_check_build.py -m gpu
@@ -38,11 +38,13 @@ for dx, dv in itertools.product((1, 2, 3), (1, 2, 3)):
                 op = A.AdvectionOperation(p)
             except A.HdError:
                 continue
-            u = torch.randn(op.n_dofs, dtype=op.dtype, device="cuda")
-            it = A.LowStorageRungeKuttaIntegrator(op.initialize_dof_vector(), op.initialize_dof_vector(), "rk45")
-            it.perform_time_step(u, 0.0, 1e-3, op)
-            if op.device_status() != 0:
-                bad.append((dx, dv, k, dtype))
+            for arith in (("native", "fp32x2") if dtype == "f64" else ("native",)):
+                op.set_arithmetic(arith)
+                u = torch.randn(op.n_dofs, dtype=op.dtype, device="cuda")
+                it = A.LowStorageRungeKuttaIntegrator(op.initialize_dof_vector(), op.initialize_dof_vector(), "rk45")
+                it.perform_time_step(u, 0.0, 1e-3, op)
+                if op.device_status() != 0:
+                    bad.append((dx, dv, k, dtype, arith))
 g = Pt.LocalPartGroup(A.AdvectionParameters(3, 3, 3, [2] * 3, [2, 2, 4], [0] * 3, [1] * 3, [0] * 3, [1] * 3,
                                             [1, .8, .6, .4, .3, .2], dtype="f32"), 2)
 sols = g.initialize_dof_vectors()
