@@ -561,7 +561,12 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
 // direction of the last phase, the result written to global memory.  The line
 // loop is not unrolled: a double-word multiply-add is about twelve FP32
 // instructions, and fully unrolled planes overflow the instruction cache; the
-// phase and direction loops are not unrolled either (one copy of the line code).
+// phase and direction loops are unrolled (one copy of the line code per
+// direction, whose coefficients and strides are then constant operands).
+// The accumulators are stored between directions as they are, hi + lo not
+// renormalised: they are only ever added to (the TwoSum of x2_mac is exact
+// for any hi, lo), and the few dozen low parts summed per value stay far
+// below hi; the result's conversion adds hi and lo in FP64.
 // A cell's threads visit their lines in a rotated order (planes of the first
 // phase lie N*N values apart, a multiple of the bank count), and lines along
 // direction 0 (contiguous, 16-byte aligned for even N) are read as 16-byte words.
@@ -682,13 +687,11 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
           if (!fin) {
             if ((N % 2) == 0 && st == 1) {
 #pragma unroll
-              for (int i = 0; i < N; i += 2) {
-                const f32x2 a0 = x2_norm(acc[i]), a1 = x2_norm(acc[i + 1]);
-                *reinterpret_cast<float4*>(so + lb + i) = make_float4(a0.hi, a0.lo, a1.hi, a1.lo);
-              }
+              for (int i = 0; i < N; i += 2)
+                *reinterpret_cast<float4*>(so + lb + i) = make_float4(acc[i].hi, acc[i].lo, acc[i + 1].hi, acc[i + 1].lo);
             } else {
 #pragma unroll
-              for (int i = 0; i < N; ++i) so[lb + i * st] = x2_norm(acc[i]);
+              for (int i = 0; i < N; ++i) so[lb + i * st] = acc[i];
             }
           } else if (valid) {
 #pragma unroll
