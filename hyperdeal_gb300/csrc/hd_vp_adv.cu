@@ -278,7 +278,9 @@ __device__ __forceinline__ void vp_block_x2(const VpAdvParams<double>& P, const 
     return __ldg(P.es + (gx * g.NCx + (bnode % ipow(N, DX))) * DX + (d - DX));
   };
 
-#pragma unroll 1
+  // phase and direction loops unrolled (each direction's line code compiled
+  // once, with its strides constant), the line loop rolled
+#pragma unroll
   for (int ph = 0; ph < S::NPH; ++ph) {
     const int dA = 2 * ph;
     const int dB = (2 * ph + 1 < D) ? 2 * ph + 1 : -1;
@@ -292,7 +294,7 @@ __device__ __forceinline__ void vp_block_x2(const VpAdvParams<double>& P, const 
     const bool lastph = ph == S::NPH - 1;
     for (int item = tl; item < nitems; item += TPC) {
       const int base = item_base<D, N>(item, dA, dB);
-#pragma unroll 1
+#pragma unroll
       for (int dd = 0; dd < ndir; ++dd) {
         // (never the -1 of a single-direction phase, even if evaluated ahead of the bound)
         const int d = (dd == 0 || dB < 0) ? dA : dB;
@@ -306,8 +308,13 @@ __device__ __forceinline__ void vp_block_x2(const VpAdvParams<double>& P, const 
           const int lb = base + l * lst;
           l = l + 1 < nl ? l + 1 : 0;
           const double sc = valid ? line_scale(d, lb) : 0.0;
+          // the scale in double-word form; its sign (that of hi; +-0 only where
+          // |sc| < 2^-126, whose terms vanish) picks the upwind side without an
+          // FP64 comparison
+          const f32x2 s2 = x2_from_double(sc);
+          const bool pos = s2.hi > 0.f;
           // upwind trace (the neighbour cells are valid cells even for an invalid gid)
-          const double up = __ldg(P.src + (sc > 0.0 ? nbL[d] * NC + lb + (N - 1) * st : nbR[d] * NC + lb));
+          const double up = __ldg(P.src + (pos ? nbL[d] * NC + lb + (N - 1) * st : nbR[d] * NC + lb));
           f32x2 u[N], acc[N];
           if ((N % 2) == 0 && st == 1) {
 #pragma unroll
@@ -327,8 +334,7 @@ __device__ __forceinline__ void vp_block_x2(const VpAdvParams<double>& P, const 
 #pragma unroll
             for (int i = 0; i < N; ++i) acc[i] = so[lb + i * st];
           }
-          if (sc != 0.0) {
-            const f32x2 s2 = x2_from_double(sc);
+          if (s2.hi != 0.f) {
 #pragma unroll
             for (int i = 0; i < N; ++i) {
               f32x2 t{0.f, 0.f};
@@ -344,7 +350,7 @@ __device__ __forceinline__ void vp_block_x2(const VpAdvParams<double>& P, const 
             ck = x2_norm(ck);
             const f32x2 nck{-ck.hi, -ck.lo};
             const f32x2 upx = x2_from_double(up);
-            if (sc > 0.0) {
+            if (pos) {
               x2_mac(acc[N - 1], nck, u[N - 1]);
               x2_mac(acc[0], c0, upx);
             } else {
@@ -353,8 +359,9 @@ __device__ __forceinline__ void vp_block_x2(const VpAdvParams<double>& P, const 
             }
           }
           if (!fin) {
+            // accumulators stored as they are between directions (only added to)
 #pragma unroll
-            for (int i = 0; i < N; ++i) so[lb + i * st] = x2_norm(acc[i]);
+            for (int i = 0; i < N; ++i) so[lb + i * st] = acc[i];
           } else if (valid) {
 #pragma unroll
             for (int i = 0; i < N; ++i) {
