@@ -511,8 +511,10 @@ def run_adv2d(args):
 
 def run_adv4d(args):
     """4D (2x+2v) k=3, 16^2 x 16^2 cells (16,777,216 DoFs), velocity (1.0, 0.7, 0.5, 0.3),
-    f0 = prod sin(2 pi coord): fused rk45 steps in FP32 and FP64 storage through the generic
-    kernel, the FP32 - FP64 difference after the same steps, and the oracle's FP64 step time."""
+    f0 = prod sin(2 pi coord): fused rk45 steps in FP32 storage (the TMA-pipelined kernel, whose
+    unit is one x0-row of 16 cells; the generic kernel beside it) and FP64 storage (generic kernel,
+    FP64 and FP32x2 contractions), the FP32 - FP64 difference after the same steps, and the
+    oracle's FP64 step time."""
     import numpy as np
     import torch
 
@@ -526,16 +528,19 @@ def run_adv4d(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     res, sols = {}, {}
     clocks = None
-    for dtype in ("f32", "f64", "f64_fp32x2"):
+    for dtype in ("f32", "f32_generic", "f64", "f64_fp32x2"):
         p = A.AdvectionParameters(2, 2, k4, [16, 16], [16, 16], [0.0] * 2, [1.0] * 2, [0.0] * 2, [1.0] * 2, vel,
                                   dtype=dtype[:3])
         op = A.AdvectionOperation(p)
         if dtype == "f64_fp32x2":
             op.set_arithmetic("fp32x2")
+        if dtype == "f32_generic":
+            op.set_kernel("generic")
         sol = op.initialize_dof_vector()
         A.VectorTools.interpolate(op, f0, sol, 0.0)
         Ki, Ti = op.initialize_dof_vector(), op.initialize_dof_vector()
-        tuned = None if args.adv4d_default_tile else op.autotune(sol, Ki, reps=2)  # outside the timed region
+        # the generic kernel's tile, picked outside the timed region (the pipelined kernel has none)
+        tuned = None if args.adv4d_default_tile or op.kernel == "pipelined" else op.autotune(sol, Ki, reps=2)
         integ = A.LowStorageRungeKuttaIntegrator(Ki, Ti, "rk45")
         dt = CFL * op.critical_time_step() / k4 ** 1.5
         t = 0.0
@@ -560,7 +565,7 @@ def run_adv4d(args):
         S = 4 if dtype == "f32" else 8
         res[dtype] = {"ms_per_step": round(ms, 4), "gdof_per_s": round(op.n_dofs * N_STAGES / (ms / 1e3) / 1e9, 2),
                       "hbm_gb_per_s": round(18 * S * op.n_dofs / (ms / 1e3) / 1e9, 1),
-                      "tile": op.tile_limits(), "autotuned": tuned}
+                      "kernel": op.kernel, "tile": op.tile_limits(), "autotuned": tuned}
         sols[dtype] = sol.double()
         n = op.n_dofs
     l2 = float(torch.linalg.vector_norm(sols["f32"] - sols["f64"]) / torch.linalg.vector_norm(sols["f64"]))
@@ -586,10 +591,13 @@ def run_adv4d(args):
                                   "(65,536 cells, %d DoFs), periodic unit box, velocity (1.0, 0.7, 0.5, 0.3), "
                                   "f0 = prod sin(2 pi coord), fused rk45, CFL 0.2" % (k4, n),
                       "l2_flush": "none: %d MB per FP32 vector (3 vectors > 129 MB L2)" % (4 * n // 10 ** 6)},
-           "f32": res["f32"], "f64": res["f64"], "f64_fp32x2": res["f64_fp32x2"], "l2_rel_err_f32_vs_f64": l2,
+           "f32": res["f32"], "f32_generic": res["f32_generic"], "f64": res["f64"], "f64_fp32x2": res["f64_fp32x2"],
+           "l2_rel_err_f32_vs_f64": l2,
            "roofline": {"bound": "hbm", "achieved": res["f32"]["hbm_gb_per_s"], "peak": peak, "unit": "GB/s",
                         "frac": round(res["f32"]["hbm_gb_per_s"] / peak, 4), "peak_source": peak_kind},
-           "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": N_STAGES * args.steps}
+           "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": N_STAGES * args.steps,
+           "kernel": ("hd::ecl6_kernel<stage, 4> (persistent, TMA-pipelined, units of 16 cells)"
+                      if res["f32"]["kernel"] == "pipelined" else "hd::ecl_kernel<4,4,float,stage> (generic)")}
     print(json.dumps(out))
     return 0
 

@@ -1,5 +1,6 @@
-// hd_ecl6.cu -- host side of the pipelined 6D degree-3 FP32 kernel:
-// tensor-map encoding (through the driver entry point, no -lcuda) and launch.
+// hd_ecl6.cu -- host side of the pipelined degree-3 FP32 kernel (6D cells,
+// or 4D x0-rows of 16 cells): tensor-map encoding (through the driver entry
+// point, no -lcuda) and launch.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -70,10 +71,17 @@ cudaError_t encode_ecl6_maps(const float* tin, const float* uin, long long n, Ec
 }
 
 bool ecl6_eligible(const EclParams<float>& P) {
-  if (P.D != 6 || P.dim_x != 3) return false;
-  for (int d = 0; d < 6; ++d)
+  if (!((P.D == 6 && P.dim_x == 3) || (P.D == 4 && P.dim_x == 2))) return false;
+  for (int d = 0; d < P.D; ++d)
     if (!P.periodic[d]) return false;
-  if (P.n_cells * 4096LL > (1LL << 36)) return false;  // TMA row coordinate range
+  const long long nc = P.D == 6 ? 4096LL : 256LL;
+  if (P.n_cells * nc > (1LL << 36)) return false;  // TMA row coordinate range
+  if (P.D == 4) {
+    // units are whole x0-rows of 16 cells; not for parts (no ghost faces)
+    long long total = 1;
+    for (int d = 0; d < 4; ++d) total *= P.cells[d];
+    if (P.cells[0] != 16 || P.n_cells != total) return false;
+  }
   return true;
 }
 
@@ -83,31 +91,45 @@ cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int* ticket, int mo
   E.p = P;
   E.wait_limit = wait_limit ? wait_limit : E6_WAIT_LIMIT;
   E.skip_issue = skip_issue;
-  E.row_len = P.cells[0];
-  // parts hold whole layers of v2, so every boundary below falls on a row
-  E.row_lo = int(P.c_lo / P.cells[0]);
-  E.row_hi = int(P.c_hi / P.cells[0]);
-  E.row0 = int(P.gid0 / P.cells[0]);
-  E.lay0 = int(P.gid0 / P.layer);
-  E.lay1 = int((P.gid0 + P.n_cells) / P.layer);
+  const bool d4 = P.D == 4;
+  if (d4) {
+    // units of 16 cells (one x0-row each), claimed one at a time
+    E.row_len = 1;
+    E.row_lo = int(P.c_lo / 16);
+    E.row_hi = int(P.c_hi / 16);
+    E.row0 = int(P.gid0 / 16);
+    E.lay0 = 0;
+    E.lay1 = 1 << 30;
+    E.n_units = P.n_cells / 16;
+  } else {
+    E.row_len = P.cells[0];
+    // parts hold whole layers of v2, so every boundary below falls on a row
+    E.row_lo = int(P.c_lo / P.cells[0]);
+    E.row_hi = int(P.c_hi / P.cells[0]);
+    E.row0 = int(P.gid0 / P.cells[0]);
+    E.lay0 = int(P.gid0 / P.layer);
+    E.lay1 = int((P.gid0 + P.n_cells) / P.layer);
+    E.n_units = P.n_cells;
+  }
   E.err = err;
   E.ticket = ticket;
   const int n_rows = E.row_hi - E.row_lo;
   if (n_rows <= 0) return cudaSuccess;  // an empty cell range launches nothing
   Ecl6Maps maps;
-  cudaError_t e = encode_ecl6_maps(P.tin, P.uin, P.n_cells * 4096LL, &maps);
+  cudaError_t e = encode_ecl6_maps(P.tin, P.uin, P.n_cells * (d4 ? 256LL : 4096LL), &maps);
   if (e != cudaSuccess) return e;
-  static bool attr_done[4] = {false, false, false, false};
+  static bool attr_done[8] = {false, false, false, false, false, false, false, false};
+  const int ki = mode + (d4 ? 4 : 0);
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int grid = 2 * sms;
   if (grid > n_rows) grid = n_rows;
   auto go = [&](auto kern) -> cudaError_t {
-    if (!attr_done[mode]) {
+    if (!attr_done[ki]) {
       cudaError_t ee = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, E6_SMEM);
       if (ee != cudaSuccess) return ee;
-      attr_done[mode] = true;
+      attr_done[ki] = true;
     }
     // the row tickets start at 0 for every launch (stream-ordered, also inside a captured graph)
     cudaError_t ee = cudaMemsetAsync(ticket, 0, sizeof(int), stream);
@@ -115,6 +137,15 @@ cudaError_t launch_ecl6(const EclParams<float>& P, int* err, int* ticket, int mo
     kern<<<grid, E6_THREADS, E6_SMEM, stream>>>(E, maps);
     return cudaGetLastError();
   };
+  if (d4) {
+    switch (mode) {
+      case kApply: return go(ecl6_kernel<kApply, 4>);
+      case kStageFirst: return go(ecl6_kernel<kStageFirst, 4>);
+      case kStageMid: return go(ecl6_kernel<kStageMid, 4>);
+      case kStageLast: return go(ecl6_kernel<kStageLast, 4>);
+      default: return cudaErrorInvalidValue;
+    }
+  }
   switch (mode) {
     case kApply: return go(ecl6_kernel<kApply>);
     case kStageFirst: return go(ecl6_kernel<kStageFirst>);

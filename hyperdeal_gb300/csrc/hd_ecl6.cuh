@@ -24,6 +24,16 @@
 //   * Every mbarrier wait is bounded: on time-out the kernel records an
 //     error code, drains its own in-flight copies (bounded) and returns.
 //
+// The same kernel serves the 4D (2x+2v) degree-3 case (DIM = 4) when the
+// mesh has 16 cells along x0: one x0-row of 16 cells (256 values each) is a
+// unit of 4,096 values laid out exactly like one 6D cell, the 4D cell index
+// taking the place of the 6D digits (i4, i5).  Phase 0 (x0, x1) and phase 1
+// (v0, v1 at node strides 16 and 64, the 6D x2 and v0 strides) are then the
+// 6D phases; the x0 upwind trace is a cell of the same unit (the unit is a
+// whole periodic x0-row), read from the staged tile; the v0 and v1 traces of
+// the 16 cells are the 6D x2 and v0 boxes of the neighbouring unit; there is
+// no third phase.  Units are claimed one at a time (rows of length 1).
+//
 // Reference operator: include/hyper.deal/operators/advection/
 // advection_operation.h:218-566; LSRK stage: base/time_integrators.templates.h:111-135.
 #pragma once
@@ -153,6 +163,7 @@ struct Ecl6Params {
   int row_len;         // cells per row (cells in x0)
   int row0;            // global row index of local row 0 (parts hold whole layers)
   int lay0, lay1;      // this part's layers [lay0, lay1) of direction v2
+  long long n_units;   // cells (6D) or x0-rows of 16 cells (4D) of the launch's vectors
   int* err;            // device error flag
   int* ticket;         // next unclaimed row (zeroed before every launch)
   unsigned wait_limit; // try_wait rounds of every bounded wait (E6_WAIT_LIMIT)
@@ -180,30 +191,48 @@ __device__ __forceinline__ long long e6_checked(const Ecl6Params& P, long long c
 
 // first (local) cell id of row r and the upwind-neighbour offsets (in cells)
 // of the row's cells in directions 1..5 (inside a row only x0 varies); ghost5:
-// the v2 neighbour belongs to another part (its face is in the ghost region)
+// the v2 neighbour belongs to another part (its face is in the ghost region).
+// DIM = 4: unit r (one x0-row of 16 cells) and its neighbours' offsets in
+// units along x1, v0, v1.
 struct E6Row {
   long long first;
   int nb[6];
   int ghost5;
 };
 
+template <int DIM>
 __device__ __forceinline__ E6Row e6_row(const Ecl6Params& P, int r) {
   E6Row R;
   R.first = (long long)r * P.row_len;
   R.nb[0] = 0;
   R.ghost5 = 0;
   int rem = P.row0 + r;  // global row: coordinates of the global mesh
+  if constexpr (DIM == 4) {
+    int us = 1;  // unit stride of direction d
 #pragma unroll
-  for (int d = 1; d < 6; ++d) {
-    const int nc = P.p.cells[d];
-    const int c = rem % nc;
-    rem /= nc;
-    const int step = P.p.op[d].step;
-    const int cs = int(P.p.cstride[d]);
-    const int cn = c + step;
-    const int cw = cn < 0 ? nc - 1 : (cn >= nc ? 0 : cn);  // periodic wrap
-    R.nb[d] = (cw - c) * cs;
-    if (d == 5 && (cw < P.lay0 || cw >= P.lay1)) R.ghost5 = 1;
+    for (int d = 1; d < 4; ++d) {
+      const int nc = P.p.cells[d];
+      const int c = rem % nc;
+      rem /= nc;
+      const int cn = c + P.p.op[d].step;
+      const int cw = cn < 0 ? nc - 1 : (cn >= nc ? 0 : cn);  // periodic wrap
+      R.nb[d] = (cw - c) * us;
+      us *= nc;
+    }
+    R.nb[4] = R.nb[5] = 0;
+  } else {
+#pragma unroll
+    for (int d = 1; d < 6; ++d) {
+      const int nc = P.p.cells[d];
+      const int c = rem % nc;
+      rem /= nc;
+      const int step = P.p.op[d].step;
+      const int cs = int(P.p.cstride[d]);
+      const int cn = c + step;
+      const int cw = cn < 0 ? nc - 1 : (cn >= nc ? 0 : cn);  // periodic wrap
+      R.nb[d] = (cw - c) * cs;
+      if (d == 5 && (cw < P.lay0 || cw >= P.lay1)) R.ghost5 = 1;
+    }
   }
   return R;
 }
@@ -213,7 +242,7 @@ __device__ __forceinline__ long long e6_cell(const Ecl6Params& P, long long firs
   return first + (P.p.op[0].step < 0 ? k : (P.row_len - 1 - k));
 }
 
-template <int MODE>
+template <int MODE, int DIM = 6>
 __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params P,
                                              const __grid_constant__ Ecl6Maps maps) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -267,7 +296,7 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
       int r = take();
       s_rows[0] = r;
       s_rows[1] = r >= 0 ? take() : -1;
-      E6Row R = e6_row(P, r >= 0 ? r : 0);
+      E6Row R = e6_row<DIM>(P, r >= 0 ? r : 0);
       if (r < 0) mbar_arrive(&full[0]);  // no row for this CTA: release the compute warps
       for (int it = 0; r >= 0; ++it) {
         const int s = it % E6_STAGES;
@@ -282,7 +311,7 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
           r = s_rows[q % 4];
           if (r < 0) break;  // the compute warps stop at the end of row q - 1 by themselves
           s_rows[(q + 1) % 4] = take();
-          R = e6_row(P, r);
+          R = e6_row<DIM>(P, r);
         }
         const long long gid = e6_cell(P, R.first, k);
         float* st = s_stage + s * E6_STAGE_FLOATS;
@@ -295,7 +324,7 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
           }
           continue;
         }
-        const long long nc = P.p.n_cells;
+        const long long nc = P.n_units;
         const long long gc = e6_checked(P, gid, nc);
         mbar_arrive_expect_tx(&full[s], bytes);
         tma_load_2d(st, &maps.tcell, 0, int(gc * 128), &full[s]);
@@ -367,7 +396,7 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
   float4 px1 = make_float4(0.f, 0.f, 0.f, 0.f);  // x1 face values of this thread's plane
   auto fetch_x1 = [&](long long g, int nb1) {
     if (L[1].active)
-      px1 = __ldg(reinterpret_cast<const float4*>(P.p.tin + e6_checked(P, g + nb1, P.p.n_cells) * NC + 16 * tid +
+      px1 = __ldg(reinterpret_cast<const float4*>(P.p.tin + e6_checked(P, g + nb1, P.n_units) * NC + 16 * tid +
                                                   4 * L[1].nb_node));
   };
 
@@ -381,7 +410,7 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
   bar_compute();
   if (!s_cont[0]) return;
   int q = 0, k = 0;
-  E6Row R = e6_row(P, s_rows[0]);
+  E6Row R = e6_row<DIM>(P, s_rows[0]);
   fetch_x1(e6_cell(P, R.first, 0), R.nb[1]);
   for (int it = 0;; ++it) {
     const int s = it % E6_STAGES;
@@ -390,9 +419,9 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
     const bool new_row = k + 1 == P.row_len;
 
     // row start: x0 face of the upwind neighbour of the row's first cell (periodic wrap)
-    if (k == 0 && L[0].active) {
+    if (DIM == 6 && k == 0 && L[0].active) {
       const long long g0 = R.first + (L[0].step < 0 ? P.row_len - 1 : 0);
-      const float* src = P.p.tin + e6_checked(P, g0, P.p.n_cells) * NC + 16 * tid + L[0].nb_node;
+      const float* src = P.p.tin + e6_checked(P, g0, P.n_units) * NC + 16 * tid + L[0].nb_node;
 #pragma unroll
       for (int b = 0; b < 4; ++b) carry[b] = __ldg(src + 4 * b);
     }
@@ -422,6 +451,13 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
 #pragma unroll
         for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
       if (L[0].active) {
+        if constexpr (DIM == 4) {
+          // the x0 upwind neighbour is a cell of this unit (a whole periodic
+          // x0-row), staged with it: its face nb_node in this thread's plane
+          const int nodeb = ((((tid >> 4) + L[0].step) & 15) << 8) + ((tid & 15) << 4) + L[0].nb_node;
+#pragma unroll
+          for (int b = 0; b < 4; ++b) carry[b] = st[swz_t(nodeb + 4 * b)];
+        }
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
 #pragma unroll
@@ -436,8 +472,10 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
           acc[3][b] = fmaf(L[0].cl, up, acc[3][b]);
         }
         // the next cell in traversal order needs this cell's face nb_node
+        if constexpr (DIM == 6) {
 #pragma unroll
-        for (int b = 0; b < 4; ++b) carry[b] = L[0].nb_node ? uu[3][b] : uu[0][b];
+          for (int b = 0; b < 4; ++b) carry[b] = L[0].nb_node ? uu[3][b] : uu[0][b];
+        }
       }
       if (L[1].active) {
         const float upv[4] = {px1.x, px1.y, px1.z, px1.w};
@@ -462,7 +500,7 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
     // x1 face of the next cell of this CTA
     if (has_next) {
       if (new_row) {
-        const E6Row Rn = e6_row(P, next_row);
+        const E6Row Rn = e6_row<DIM>(P, next_row);
         fetch_x1(e6_cell(P, Rn.first, 0), Rn.nb[1]);
       } else {
         fetch_x1(e6_cell(P, R.first, k + 1), R.nb[1]);
@@ -526,8 +564,10 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
     bar_compute();
 
     // ---------------- phase 2: directions v1 (a, stride 256) and v2 (b, stride 1024), epilogue
+    // (DIM = 4: the epilogue only; phase 1 left K in the accumulator tile)
     {
       float uu[4][4], acc[4][4];
+      if constexpr (DIM == 6) {
 #pragma unroll
       for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -567,6 +607,7 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
           acc[a][3] = fmaf(L[5].cl, up, acc[a][3]);
         }
       }
+      }  // DIM == 6
       // U at the epilogue nodes (the T tile for the first stage), read before the slot is released
       float4 uv[4];
       if constexpr (MODE != kApply) {
@@ -577,13 +618,16 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[s]);
       // transpose K through this warp's private slice of the accumulator tile
+      if constexpr (DIM == 6) {
 #pragma unroll
-      for (int a = 0; a < 4; ++a)
+        for (int a = 0; a < 4; ++a)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) so[ob2[a & 1] + 256 * a + 1024 * b] = acc[a][b];
+          for (int b = 0; b < 4; ++b) so[ob2[a & 1] + 256 * a + 1024 * b] = acc[a][b];
+      }
       __syncwarp();
 #ifdef HD_CHECK
-      const bool store_ok = gid >= P.p.c_lo && gid < P.p.c_hi;
+      const long long gcell = DIM == 4 ? gid * 16 : gid;
+      const bool store_ok = gcell >= P.p.c_lo && gcell < P.p.c_hi;
       if (!store_ok) atomicExch(P.err, kCheckError);
 #else
       constexpr bool store_ok = true;
@@ -617,7 +661,7 @@ __global__ void __maxnreg__(104) ecl6_kernel(const __grid_constant__ Ecl6Params 
     if (new_row) {
       k = 0;
       ++q;
-      R = e6_row(P, next_row);
+      R = e6_row<DIM>(P, next_row);
     } else {
       ++k;
     }

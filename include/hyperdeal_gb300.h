@@ -133,9 +133,10 @@ int hd_adv_autotune(hd_adv *op, const void *src, void *dst, int reps, int *cells
                     double *ms, void *stream);
 
 /* Kernel selection: AUTO picks the persistent TMA-pipelined kernel where it
- * applies (FP32, degree 3, fully periodic 3x+3v mesh) and the generic
- * shared-memory kernel otherwise; GENERIC forces the latter.  Both compute
- * the same operator.  hd_adv_kernel() returns the kernel that will run. */
+ * applies (FP32, degree 3, fully periodic: 3x+3v meshes, and 2x+2v meshes
+ * with 16 cells along x0 that are not parts) and the generic shared-memory
+ * kernel otherwise; GENERIC forces the latter.  Both compute the same
+ * operator.  hd_adv_kernel() returns the kernel that will run. */
 enum hd_kernel { HD_KERNEL_AUTO = 0, HD_KERNEL_GENERIC = 1, HD_KERNEL_PIPELINED = 2 };
 int hd_adv_set_kernel(hd_adv *op, int variant);
 int hd_adv_kernel(const hd_adv *op);
