@@ -45,6 +45,16 @@ for dx, dv in itertools.product((1, 2, 3), (1, 2, 3)):
                 it.perform_time_step(u, 0.0, 1e-3, op)
                 if op.device_status() != 0:
                     bad.append((dx, dv, k, dtype, arith))
+# the pipelined kernel's 4D units (16 cells along x0), both velocity signs
+for vel in ([0.9, 0.7, 0.5, 0.3], [-0.9, 0.7, -0.5, 0.3]):
+    p = A.AdvectionParameters(2, 2, 3, [16, 2], [2, 3], [0] * 2, [1] * 2, [0] * 2, [1] * 2, vel, dtype="f32")
+    op = A.AdvectionOperation(p)
+    assert op.kernel == "pipelined"
+    u = torch.randn(op.n_dofs, dtype=op.dtype, device="cuda")
+    it = A.LowStorageRungeKuttaIntegrator(op.initialize_dof_vector(), op.initialize_dof_vector(), "rk45")
+    it.perform_time_step(u, 0.0, 1e-3, op)
+    if op.device_status() != 0:
+        bad.append(("pipelined 4D", vel))
 g = Pt.LocalPartGroup(A.AdvectionParameters(3, 3, 3, [2] * 3, [2, 2, 4], [0] * 3, [1] * 3, [0] * 3, [1] * 3,
                                             [1, .8, .6, .4, .3, .2], dtype="f32"), 2)
 sols = g.initialize_dof_vectors()
@@ -76,6 +86,7 @@ def test_no_bounds_violation_in_the_kernel_sweep():
 
 def test_parity_suite_passes_with_the_checked_library():
     r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-x", "-m", "gpu", "tests/test_gpu_parity.py",
-                        "tests/test_gpu_partition.py", "tests/test_gpu_fp32x2.py", "tests/test_gpu_layout.py"],
+                        "tests/test_gpu_partition.py", "tests/test_gpu_fp32x2.py", "tests/test_gpu_layout.py",
+                        "tests/test_gpu_pipelined4d.py"],
                        cwd=ROOT, env=_env(), capture_output=True, text=True, timeout=3600)
     assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
