@@ -28,7 +28,8 @@ EXPORTED_SYMBOLS = (
     "hd_batch_create", "hd_batch_destroy", "hd_batch_n_classes", "hd_batch_class_info", "hd_batch_set_tile",
     "hd_batch_apply", "hd_batch_lsrk_step", "hd_batch_graph_capture", "hd_batch_graph_launch", "hd_batch_autotune",
     "hd_adv_autotune", "hd_vp_lsrk_step_fused", "hd_adv_set_arithmetic", "hd_adv_arithmetic",
-    "hd_batch_class_arithmetic", "hd_vp_set_arithmetic",
+    "hd_batch_class_arithmetic", "hd_vp_set_arithmetic", "hd_vp_set_kernel", "hd_vp_kernel", "hd_vp_device_status",
+    "hd_vp_set_wait_test",
     "hd_part_layout_get", "hd_adv_create_part", "hd_adv_part_layout", "hd_adv_pack_faces", "hd_adv_apply_cells",
     "hd_lsrk_stage", "hd_lsrk_stage_input", "hd_adv_set_wait_test",
 )
@@ -156,6 +157,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.hd_vp_cg_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int), llp, llp, dp, llp]
     L.hd_vp_set_guess.argtypes = [vp, ctypes.c_int]
     L.hd_vp_set_arithmetic.argtypes = [vp, ctypes.c_int]
+    L.hd_vp_set_kernel.argtypes = [vp, ctypes.c_int]
+    L.hd_vp_kernel.argtypes = [vp]
+    L.hd_vp_device_status.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+    L.hd_vp_set_wait_test.argtypes = [vp, ctypes.c_uint, ctypes.c_int]
     L.hd_vp_learn_loss_grad.argtypes = [ctypes.c_longlong, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp,
                                         vp]
     vpp = ctypes.POINTER(vp)

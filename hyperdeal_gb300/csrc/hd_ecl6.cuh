@@ -68,6 +68,9 @@ constexpr unsigned E6_WAIT_LIMIT = 1u << 22;  // try_wait rounds before giving u
 
 enum : int { E6_ERR_TIMEOUT_FULL = 1, E6_ERR_TIMEOUT_EMPTY = 2, E6_ERR_SMEM_ALIGN = 3 };
 
+// tensor maps of a vector of n floats (hd_ecl6.cu); uin may be null (then tin)
+cudaError_t encode_ecl6_maps(const float* tin, const float* uin, long long n, Ecl6Maps* m);
+
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));

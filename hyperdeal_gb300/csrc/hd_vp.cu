@@ -927,6 +927,10 @@ struct hd_vp {
   hd::VpGeom g;
   int dtype;
   int arith;          // HD_ARITH_NATIVE / HD_ARITH_FP32X2 of the FP64 advection
+  int kernel;         // HD_KERNEL_AUTO / HD_KERNEL_GENERIC of the FP32 advection
+  int* d_pipe;        // pipelined advection: device error flag and unit ticket
+  unsigned pipe_wait; // its bounded waits' try_wait rounds (0: the default)
+  int pipe_skip;      // its test hook (hd_vp_set_wait_test; -1: off)
   double* d_wv;       // v-node weights (NCv)
   double* d_partial;  // moment partials (nchunks * nx)
   int nchunks;
@@ -1080,6 +1084,7 @@ void vp_free(hd_vp* v) {
   cudaFree(v->d_dy);
   cudaFree(v->d_judge);
   cudaFree(v->d_binv);
+  cudaFree(v->d_pipe);
   cudaFree(v->d_ls);
   cudaFree(v->d_ls_count);
   cudaFree(v->d_redk);
@@ -1366,13 +1371,21 @@ int solve_poisson(hd_vp* v, cudaStream_t s) {
 }
 
 // the phase-space advection with the current field: apply, or a fused LSRK stage
+// the FP32 advection kernel that runs (HD_KERNEL_PIPELINED where it applies, unless GENERIC is set)
+int vp_kernel(const hd_vp* v) {
+  return v->dtype == HD_F32 && v->kernel != HD_KERNEL_GENERIC && hd::vp_pipe_eligible(v->g) ? HD_KERNEL_PIPELINED
+                                                                                           : HD_KERNEL_GENERIC;
+}
+
 int vp_advect(hd_vp* v, int mode, const void* src, const void* uin, void* dst, void* tout, double fb, double fa,
               cudaStream_t s) {
   cudaError_t e;
   if (v->dtype == HD_F32) {
     hd::VpAdvParams<float> P{(const float*)src, (float*)dst, (const float*)uin, (float*)tout, float(fb), float(fa),
                              (const float*)v->d_xs, (const float*)v->d_es, v->g};
-    e = hd::launch_vp_advection(P, mode, s);
+    e = vp_kernel(v) == HD_KERNEL_PIPELINED
+            ? hd::launch_vp_pipelined(P, mode, s, v->d_pipe, v->pipe_wait, v->pipe_skip)
+            : hd::launch_vp_advection(P, mode, s);
   } else {
     hd::VpAdvParams<double> P{(const double*)src, (double*)dst, (const double*)uin, (double*)tout, fb, fa,
                               (const double*)v->d_xs, (const double*)v->d_es, v->g};
@@ -1413,6 +1426,8 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
   v->desc = d;
   v->dtype = d.dtype;
   v->arith = HD_ARITH_NATIVE;
+  v->kernel = HD_KERNEL_AUTO;
+  v->pipe_skip = -1;
   v->guess = d.guess;
   hd::VpGeom& g = v->g;
   g.dx = d.dim_x;
@@ -1492,7 +1507,7 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
   // the advection kernel keeps two copies of CTA's cells in shared memory: 3x+3v up to degree 3
   if (g.D == 6 && N > 4) { delete v; return vfail(HD_ERR_UNSUPPORTED, "hd_vp_create: 3x+3v only for degree <= 3"); }
   for (int i = 0; i < g.dx; ++i)
-    if (d.cells_v[i] > 64) { delete v; return vfail(HD_ERR_UNSUPPORTED, "hd_vp_create: at most 64 v-cells per direction"); }
+    if (d.cells_v[i] > hd::kVpMaxCellsV) { delete v; return vfail(HD_ERR_UNSUPPORTED, "hd_vp_create: at most 64 v-cells per direction"); }
   // device buffers
   const int NCv = g.NC / g.NCx;
   v->nchunks = int((g.ncv + hd::kMomChunk - 1) / hd::kMomChunk);
@@ -1516,7 +1531,7 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
   alloc((void**)&v->d_phi, sizeof(double) * nx);
   alloc((void**)&v->d_E, sizeof(double) * nx * g.dx);
   alloc(&v->d_es, sizeof(double) * nx * g.dx);
-  alloc(&v->d_xs, sizeof(double) * g.dx * 64 * hd::kMaxN);
+  alloc(&v->d_xs, sizeof(double) * g.dx * hd::kVpMaxCellsV * hd::kMaxN);
   alloc((void**)&v->d_cg, sizeof(double) * (5 * nx + 6 * v->cg_grid));
   v->ell_w = g.gauss ? g.NCx * (1 + 2 * g.dx) : 3 * N * g.dx;
   alloc((void**)&v->d_ell_col, sizeof(int) * size_t(v->ell_w) * nx);
@@ -1529,6 +1544,7 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
   alloc((void**)&v->d_dx, sizeof(double) * nx);
   alloc((void**)&v->d_dy, sizeof(double) * nx);
   alloc((void**)&v->d_judge, sizeof(double) * 2 * 64);
+  alloc((void**)&v->d_pipe, sizeof(int) * 2);
   if (e != cudaSuccess) { vp_free(v); return vcuda(e, "hd_vp_create: cudaMalloc"); }
   {
     double wv[4096];
@@ -1544,15 +1560,21 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
     e = cudaMemcpy(v->d_wv, wv, sizeof(double) * NCv, cudaMemcpyHostToDevice);
     // x-line velocity tables: v-coordinate of node i of v-cell c along v-direction dx + d, over h_{x_d}
     {
-      double xs64[3 * 64 * hd::kMaxN];
-      float xs32[3 * 64 * hd::kMaxN];
-      int k = 0;
+      double xs64[3 * hd::kVpMaxCellsV * hd::kMaxN];
+      float xs32[3 * hd::kVpMaxCellsV * hd::kMaxN];
+      // one block of kVpMaxCellsV v-cells per direction: entry (d * kVpMaxCellsV + c) * N + i
+      const int k = g.dx * hd::kVpMaxCellsV * N;
+      for (int t = 0; t < k; ++t) {
+        xs64[t] = 0.0;
+        xs32[t] = 0.f;
+      }
       for (int d2 = 0; d2 < g.dx; ++d2) {
         const int e2 = g.dx + d2;
         for (int c = 0; c < g.cells[e2]; ++c)
-          for (int i = 0; i < N; ++i, ++k) {
-            xs64[k] = (g.lo[e2] + (c + (g.gauss ? g.gq[i] : g.gl[i])) * g.h[e2]) / g.h[d2];
-            xs32[k] = float(xs64[k]);
+          for (int i = 0; i < N; ++i) {
+            const int t = (d2 * hd::kVpMaxCellsV + c) * N + i;
+            xs64[t] = (g.lo[e2] + (c + (g.gauss ? g.gq[i] : g.gl[i])) * g.h[e2]) / g.h[d2];
+            xs32[t] = float(xs64[t]);
           }
       }
       if (e == cudaSuccess)
@@ -1561,6 +1583,7 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
     }
     if (e == cudaSuccess) e = cudaMemset(v->d_es, 0, sizeof(double) * nx * g.dx);
     if (e == cudaSuccess) e = cudaMemset(v->d_stats, 0, sizeof(hd::VpStats));
+    if (e == cudaSuccess) e = cudaMemset(v->d_pipe, 0, sizeof(int) * 2);
     if (e == cudaSuccess && g.gauss) {
       std::vector<int> col;
       std::vector<double> val;
@@ -1790,6 +1813,35 @@ int hd_vp_set_guess(hd_vp* v, int guess) {
 }
 
 }  // extern "C"
+
+extern "C" int hd_vp_set_kernel(hd_vp* v, int variant) {
+  if (!v) return vfail(HD_ERR_INVALID, "hd_vp_set_kernel: null handle");
+  if (variant != HD_KERNEL_AUTO && variant != HD_KERNEL_GENERIC && variant != HD_KERNEL_PIPELINED)
+    return vfail(HD_ERR_INVALID, "hd_vp_set_kernel: unknown kernel");
+  if (variant == HD_KERNEL_PIPELINED && !(v->dtype == HD_F32 && hd::vp_pipe_eligible(v->g)))
+    return vfail(HD_ERR_UNSUPPORTED, "hd_vp_set_kernel: the pipelined advection needs FP32, 2x+2v, degree 3, "
+                                     "collocation and 16 cells along x0");
+  v->kernel = variant;
+  return HD_OK;
+}
+
+extern "C" int hd_vp_kernel(const hd_vp* v) { return v ? vp_kernel(v) : -1; }
+
+extern "C" int hd_vp_device_status(hd_vp* v, int* status) {
+  if (!v || !status) return vfail(HD_ERR_INVALID, "hd_vp_device_status: null argument");
+  int rc = vcuda(cudaDeviceSynchronize(), "hd_vp_device_status: synchronize");
+  if (!rc) rc = vcuda(cudaMemcpy(status, v->d_pipe, sizeof(int), cudaMemcpyDeviceToHost), "hd_vp_device_status");
+  if (!rc) rc = vcuda(cudaMemset(v->d_pipe, 0, sizeof(int)), "hd_vp_device_status: reset");
+  return rc;
+}
+
+extern "C" int hd_vp_set_wait_test(hd_vp* v, unsigned wait_limit, int skip_issue) {
+  if (!v) return vfail(HD_ERR_INVALID, "hd_vp_set_wait_test: null handle");
+  if (skip_issue != -1 && skip_issue != 0) return vfail(HD_ERR_INVALID, "hd_vp_set_wait_test: skip_issue -1 or 0");
+  v->pipe_wait = wait_limit;
+  v->pipe_skip = skip_issue;
+  return HD_OK;
+}
 
 extern "C" int hd_vp_learn_loss_grad(long long n, int rank, int batch, const float* W1, const float* W2,
                                      const float* X, const float* Y, float* dW1, float* dW2, float* loss,

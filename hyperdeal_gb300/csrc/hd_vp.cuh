@@ -18,6 +18,10 @@
 
 namespace hd {
 
+// v-cells per direction at most (the x-line velocity table holds a block of
+// this many cells per direction)
+constexpr int kVpMaxCellsV = 64;
+
 struct VpGeom {
   int D, dx, N, NCx, NC;
   long long ncx, ncv, n_cells, nx_dofs;
@@ -73,8 +77,10 @@ __device__ inline void vp_line_pass(T* x, const double* A, int N, int nd, int e,
 // advection with the phase-space velocity: dst = A(src).  The velocities
 // enter divided by the cell extent of the line's direction, precomputed in
 // FP64 and rounded to T once (no FP64 arithmetic in the kernel):
-//   x-direction d: xs[(d * cells_v + c) * N + i] = v_d(c, i) / h_{x_d}, the
-//                  v-coordinate of node i of v-cell c,
+//   x-direction d: xs[(d * kVpMaxCellsV + c) * N + i] = v_d(c, i) / h_{x_d}, the
+//                  v-coordinate of node i (quadrature point with Gauss) of
+//                  v-cell c of v-direction d (a block per direction, so that
+//                  v-meshes with different cell counts per direction index alike),
 //   v-direction d: es[(gid_x * NCx + i_x) * dx + d] = d_d phi(x-node) / h_{v_d}.
 //
 // mode kApply: dst = A(src); stage modes (fused LSRK stage, as hd_ecl.cuh):
@@ -96,5 +102,10 @@ struct VpAdvParams {
 cudaError_t launch_vp_advection(const VpAdvParams<float>& P, int mode, cudaStream_t s);
 // x2: FP32x2 arithmetic (hd_df.cuh) for FP64 storage; 1x1v and 2x2v shapes
 cudaError_t launch_vp_advection(const VpAdvParams<double>& P, int mode, cudaStream_t s, bool x2 = false);
+// the TMA-pipelined kernel (hd_vp_pipe.cuh): FP32, 2x+2v, degree 3, collocation,
+// 16 cells along x0; state = {device error flag, unit ticket} (2 device ints)
+bool vp_pipe_eligible(const VpGeom& g);
+cudaError_t launch_vp_pipelined(const VpAdvParams<float>& P, int mode, cudaStream_t s, int* state,
+                                unsigned wait_limit = 0, int skip_issue = -1);
 
 }  // namespace hd

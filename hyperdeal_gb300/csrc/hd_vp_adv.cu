@@ -17,7 +17,9 @@
 #include <cuda_runtime.h>
 
 #include "hd_ecl.cuh"
+#include "hd_ecl6.cuh"
 #include "hd_vp.cuh"
+#include "hd_vp_pipe.cuh"
 
 namespace hd {
 
@@ -60,7 +62,7 @@ __device__ __forceinline__ void vp_block(const VpAdvParams<T>& P, const VpLine<T
     if (d < DX) {
       const int e = DX + d;
       const int ie = (bnode / ipow(N, e)) % N;
-      return __ldg(P.xs + (d * g.cells[e] + cc[e]) * N + ie);
+      return __ldg(P.xs + (d * kVpMaxCellsV + cc[e]) * N + ie);
     }
     return __ldg(P.es + (gx * g.NCx + (bnode % ipow(N, DX))) * DX + (d - DX));
   };
@@ -273,7 +275,7 @@ __device__ __forceinline__ void vp_block_x2(const VpAdvParams<double>& P, const 
       const int e = DX + d;
       int ie = bnode;
       for (int k = 0; k < e; ++k) ie /= N;
-      return __ldg(P.xs + (d * g.cells[e] + cc[e]) * N + ie % N);
+      return __ldg(P.xs + (d * kVpMaxCellsV + cc[e]) * N + ie % N);
     }
     return __ldg(P.es + (gx * g.NCx + (bnode % ipow(N, DX))) * DX + (d - DX));
   };
@@ -572,7 +574,7 @@ __global__ void vp_gauss_kernel(VpAdvParams<T> P) {
           const int e = DX + d;
           int se = 1;
           for (int f = 0; f < e; ++f) se *= N;
-          a = __ldg(P.xs + (d * g.cells[e] + cc[e]) * N + (base / se) % N);
+          a = __ldg(P.xs + (d * kVpMaxCellsV + cc[e]) * N + (base / se) % N);
         } else {
           int sx = 1;
           for (int f = 0; f < DX; ++f) sx *= N;
@@ -662,6 +664,54 @@ static cudaError_t launch_vp_any(const VpAdvParams<T>& P, int mode, cudaStream_t
 
 cudaError_t launch_vp_advection(const VpAdvParams<float>& P, int mode, cudaStream_t s) {
   return launch_vp_any(P, mode, s, false);
+}
+
+bool vp_pipe_eligible(const VpGeom& g) {
+  return !g.gauss && g.D == 4 && g.N == 4 && g.cells[0] == 16 && g.n_cells * 256LL < (1LL << 36);
+}
+
+cudaError_t launch_vp_pipelined(const VpAdvParams<float>& P, int mode, cudaStream_t s, int* state,
+                                unsigned wait_limit, int skip_issue) {
+  if (!vp_pipe_eligible(P.g)) return cudaErrorNotSupported;
+  if (mode < kApply || mode > kStageLast) return cudaErrorInvalidValue;
+  VpPipeParams Q;
+  Q.a = P;
+  for (int i = 0; i < 16; ++i) Q.G[i] = float(P.g.G[i]);
+  Q.winv0 = float(1.0 / P.g.glw[0]);
+  Q.winvk = float(1.0 / P.g.glw[3]);
+  Q.n_units = int(P.g.n_cells / 16);
+  Q.err = state;
+  Q.ticket = state + 1;
+  Q.wait_limit = wait_limit ? wait_limit : E6_WAIT_LIMIT;
+  Q.skip_issue = skip_issue;
+  Ecl6Maps maps;
+  cudaError_t e = encode_ecl6_maps(P.src, P.uin ? P.uin : P.src, P.g.n_cells * 256LL, &maps);
+  if (e != cudaSuccess) return e;
+  static bool attr_done[4] = {false, false, false, false};
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  const int grid = 2 * sms < Q.n_units ? 2 * sms : Q.n_units;
+  auto go = [&](auto kern) -> cudaError_t {
+    if (!attr_done[mode]) {
+      cudaError_t ee = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, E6_SMEM);
+      if (ee != cudaSuccess) return ee;
+      attr_done[mode] = true;
+    }
+    cudaError_t ee = cudaMemsetAsync(Q.ticket, 0, sizeof(int), s);
+    if (ee != cudaSuccess) return ee;
+    kern<<<grid, E6_THREADS, E6_SMEM, s>>>(Q, maps);
+    return cudaGetLastError();
+  };
+  switch (mode) {
+    case kApply: return go(vp_pipe_kernel<kApply>);
+    case kStageFirst: return go(vp_pipe_kernel<kStageFirst>);
+    case kStageMid: return go(vp_pipe_kernel<kStageMid>);
+    default: return go(vp_pipe_kernel<kStageLast>);
+  }
 }
 cudaError_t launch_vp_advection(const VpAdvParams<double>& P, int mode, cudaStream_t s, bool x2) {
   return launch_vp_any(P, mode, s, x2);

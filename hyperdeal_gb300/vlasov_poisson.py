@@ -205,6 +205,27 @@ class VlasovPoissonOperation:
     def set_guess(self, guess: str) -> None:
         check(self._L.hd_vp_set_guess(self._h, _GUESS[guess]))
 
+    def set_kernel(self, kernel: str) -> None:
+        """FP32 advection kernel: 'auto' (the TMA-pipelined kernel where it applies), 'generic' or
+        'pipelined' (hd_vp_set_kernel)."""
+        v = {"auto": _lib.HD_KERNEL_AUTO, "generic": _lib.HD_KERNEL_GENERIC,
+             "pipelined": _lib.HD_KERNEL_PIPELINED}[kernel]
+        check(self._L.hd_vp_set_kernel(self._h, v))
+
+    @property
+    def kernel(self) -> str:
+        return {_lib.HD_KERNEL_GENERIC: "generic", _lib.HD_KERNEL_PIPELINED: "pipelined"}[
+            self._L.hd_vp_kernel(self._h)]
+
+    def device_status(self) -> int:
+        """Status of the pipelined advection since the last call (synchronises, resets it)."""
+        st = ctypes.c_int(0)
+        check(self._L.hd_vp_device_status(self._h, ctypes.byref(st)))
+        return st.value
+
+    def set_wait_test(self, wait_limit: int, skip_issue: int) -> None:
+        check(self._L.hd_vp_set_wait_test(self._h, wait_limit, skip_issue))
+
 
 def learn_loss_grad(W1: torch.Tensor, W2: torch.Tensor, X: torch.Tensor, Y: torch.Tensor):
     """loss = 1/(2B) sum_b ||W2 W1 x_b - y_b||^2 and (dW1, dW2) from the learned guess's own

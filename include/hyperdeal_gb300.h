@@ -462,6 +462,22 @@ int hd_vp_set_guess(hd_vp *vp, int guess);
  * HD_ARITH_NATIVE (default) or HD_ARITH_FP32X2 (dim_x = dim_v <= 2); the
  * moments, the Poisson solve, the field and the stage update stay FP64 */
 int hd_vp_set_arithmetic(hd_vp *vp, int arithmetic);
+/* FP32 advection kernel: AUTO (default) runs the TMA-pipelined kernel where it
+ * applies -- FP32, 2x+2v, degree 3, collocation, 16 cells along x0: one x0-row
+ * of 16 cells per unit, both neighbours' traces staged by TMA, every line's
+ * upwind side from its velocity's sign -- and the generic kernel otherwise;
+ * GENERIC forces the latter (enum hd_kernel; PIPELINED where it does not
+ * apply is HD_ERR_UNSUPPORTED).  hd_vp_kernel returns the kernel that runs. */
+int hd_vp_set_kernel(hd_vp *vp, int variant);
+int hd_vp_kernel(const hd_vp *vp);
+/* device status of the pipelined advection since the last call (0 = none;
+ * 1/2 = a bounded wait timed out and the launch stopped early); synchronises
+ * and resets it */
+int hd_vp_device_status(hd_vp *vp, int *status);
+/* test hook of the pipelined advection's bounded waits (as hd_adv_set_wait_test):
+ * wait_limit try_wait rounds (0: the default); skip_issue 0 = the producer
+ * holding unit 0 issues nothing for it, -1 = off */
+int hd_vp_set_wait_test(hd_vp *vp, unsigned wait_limit, int skip_issue);
 /* loss = 1/(2B) sum_b ||W2 W1 x_b - y_b||^2 and its gradients with the learned
  * guess's own training kernels (device pointers, row-major W1: r x n,
  * W2: n x r, X, Y: B x n) -- exposed to check them against a CPU reference */

@@ -146,6 +146,30 @@ def test_gauss_fused_step_equals_unfused_and_refuses_fp32x2(dtype):
             op.set_arithmetic("fp32x2")
 
 
+@pytest.mark.parametrize("quadrature", QUADS)
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_apply_matches_oracle_unequal_cells(dtype, quadrature):
+    """x- and v-meshes with different cell counts per direction (the x-line velocity table is laid
+    out per direction, so every v-direction's cells are found whatever the other's count)."""
+    cells_x, cells_v = [3, 2], [4, 3]
+    p = V.VlasovPoissonParameters(2, 3, cells_x, cells_v, [0.0] * 2, [4 * math.pi] * 2, [-6.0] * 2, [6.0] * 2,
+                                  dtype=dtype, cg_tol=1e-12, guess="zero", quadrature=quadrature)
+    op = V.VlasovPoissonOperation(p)
+    prob = O.Problem(2, 2, 3, cells_x + cells_v, [0.0, 0.0, -6.0, -6.0], [4 * math.pi] * 2 + [6.0] * 2,
+                     [1.0, 1.0, 6.0, 6.0], collocation=quadrature == "gauss_lobatto")
+    fo = O.interpolate(prob, O.vp_initial_function(2, 2, eps=0.2, perturbed_dims=(0, 1)))
+    fo = fo * (1.0 + 0.05 * np.random.default_rng(5).standard_normal(fo.size))
+    if dtype == "f32":
+        fo = fo.astype(np.float32).astype(np.float64)
+    src = torch.tensor(fo, dtype=torch.float64 if dtype == "f64" else torch.float32, device="cuda")
+    dst = op.initialize_dof_vector()
+    op.apply(dst, src, 0.0)
+    st = O.VPState(prob, 1e-12)
+    ref = np.zeros_like(fo)
+    st.operator(fo, ref, 0.0)
+    assert _rel(dst.cpu().numpy(), ref) <= (1e-9 if dtype == "f64" else 2e-5)
+
+
 def test_apply_rejects_bad_input():
     op, _ = _setup(1, 3, 4, 4)
     a = op.initialize_dof_vector()
