@@ -6,9 +6,10 @@
 // Maxwellian with cos(0.5 x_0), the time-step rule with the transport
 // velocity (1, .., 6, ..), rk45.  Prints "Time" and the diagnostics
 // (field energy per x-direction, mass, L2 norm, kinetic energy, momentum)
-// at every tick.  Gauss-Lobatto collocation.
+// at every tick.  Gauss-Lobatto collocation, or Gauss quadrature with k + 1
+// points (the reference's non-collocation runs, e.g. its VP golden).
 //
-// usage: vlasov_poisson_hyperrectangle dim_x degree cells_x cells_v final_time [f64|f32] [cfl tick]
+// usage: vlasov_poisson_hyperrectangle dim_x degree cells_x cells_v final_time [f64|f32] [cfl tick] [gl|gauss]
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -20,7 +21,7 @@
 using namespace hyperdeal_gb300;
 
 template <typename Number>
-int run(int dim_x, int degree, int cells_x, int cells_v, double final_time, double cfl, double tick) {
+int run(int dim_x, int degree, int cells_x, int cells_v, double final_time, double cfl, double tick, bool gauss) {
   hd_vp_desc desc{};
   desc.dim_x = desc.dim_v = dim_x;
   desc.degree = degree;
@@ -35,6 +36,7 @@ int run(int dim_x, int degree, int cells_x, int cells_v, double final_time, doub
   desc.cg_tol = 1e-12;
   desc.cg_max_iter = 100000;
   desc.guess = HD_VP_GUESS_PREVIOUS;
+  desc.quadrature = gauss ? HD_QUAD_GAUSS : HD_QUAD_GAUSS_LOBATTO;
   VlasovPoissonOperation<Number> op(desc);
   DeviceVector<Number> f = op.create_vector(), Ki = op.create_vector(), Ti = op.create_vector();
   op.interpolate(perturbed_maxwellian(dim_x, 0.01, 0.5, {0}), f);
@@ -62,7 +64,8 @@ int run(int dim_x, int degree, int cells_x, int cells_v, double final_time, doub
 
 int main(int argc, char** argv) {
   if (argc < 6) {
-    std::fprintf(stderr, "usage: %s dim_x degree cells_x cells_v final_time [f64|f32] [cfl tick]\n", argv[0]);
+    std::fprintf(stderr, "usage: %s dim_x degree cells_x cells_v final_time [f64|f32] [cfl tick] [gl|gauss]\n",
+                 argv[0]);
     return 2;
   }
   const int dim_x = std::atoi(argv[1]), degree = std::atoi(argv[2]);
@@ -71,9 +74,10 @@ int main(int argc, char** argv) {
   const std::string dtype = argc > 6 ? argv[6] : "f64";
   const double cfl = argc > 7 ? std::atof(argv[7]) : 0.05;
   const double tick = argc > 8 ? std::atof(argv[8]) : 0.1;
+  const bool gauss = argc > 9 && std::string(argv[9]) == "gauss";
   try {
-    if (dtype == "f32") return run<float>(dim_x, degree, cx, cv, final_time, cfl, tick);
-    return run<double>(dim_x, degree, cx, cv, final_time, cfl, tick);
+    if (dtype == "f32") return run<float>(dim_x, degree, cx, cv, final_time, cfl, tick, gauss);
+    return run<double>(dim_x, degree, cx, cv, final_time, cfl, tick, gauss);
   } catch (const std::exception& e) {
     std::fprintf(stderr, "error: %s\n", e.what());
     return 1;

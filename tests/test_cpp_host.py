@@ -94,6 +94,24 @@ def test_cpp_vp_application_matches_oracle():
             assert abs(x - y) <= 1e-8 * abs(y) + 1e-12
 
 
+@pytest.mark.gpu
+def test_cpp_vp_application_gauss_golden():
+    """The reference's Vlasov-Poisson golden vp_2D_2D_k3.hyperrectangle_01 (Gauss quadrature, 2x2v, k = 3,
+    4 cells per direction, rk45 to t = 0.5) from the C++ host: every row within numdiff's tolerances."""
+    from test_oracle_golden import numdiff_equal
+    case = GOLD["vlasov_poisson"][0]
+    exe = B.build_cpp_app("vlasov_poisson_hyperrectangle")
+    r = subprocess.run([exe, "2", "3", "4", "4", str(case["final_time"]), "f64", str(case["cfl"]), "0.1", "gauss"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    rows = _rows(r.stdout)
+    assert len(rows) == len(case["rows"])
+    for a, g in zip(rows, case["rows"]):
+        assert abs(a[0] - g[0]) <= 1e-3
+        for x, y in zip(a[1:], g[1:]):
+            assert numdiff_equal(x, y), (a[0], x, y)
+
+
 def test_cpp_partitioned_application_builds_and_reports_usage():
     exe = B.build_cpp_app("partitioned_advection")
     r = subprocess.run([exe], capture_output=True, text=True)
