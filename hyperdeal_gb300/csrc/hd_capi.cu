@@ -256,6 +256,12 @@ void fill_params(const hd_adv* op, hd::EclParams<T>* P) {
     }
   }
   if (op->D < hd::kMaxDim) P->cstride[op->D] = st;
+  long long nx = 1;
+  for (int d = 0; d < op->D; ++d) {
+    P->dcell[d] = hd::make_divu64((unsigned long long)op->cells[d]);
+    if (d < op->desc.dim_x) nx *= op->cells[d];
+  }
+  P->dxcells = hd::make_divu64((unsigned long long)nx);
   P->gid0 = op->part.first_cell;
   P->c_lo = 0;
   P->c_hi = op->n_cells;

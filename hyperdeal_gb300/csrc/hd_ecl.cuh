@@ -31,6 +31,40 @@ constexpr int kMaxN = 6;  // nodes per direction (degree <= 5)
 
 __host__ __device__ constexpr int ipow(int b, int e) { return e == 0 ? 1 : b * ipow(b, e - 1); }
 
+// Division of 64-bit unsigned integers by an invariant divisor d >= 1 through
+// a multiply-high (Granlund and Montgomery, "Division by invariant integers
+// using multiplication", PLDI 1994, Figure 4.1 with N = 64):
+//   l = ceil(log2 d), m = floor(2^64 (2^l - d) / d) + 1 (< 2^64),
+//   t = mulhi(m, n), q = (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0),
+// exact for every 0 <= n < 2^64.  The cell coordinates of the generic kernels
+// use it: a 64-bit division by a runtime divisor is a long emulated sequence
+// on the GPU, and every thread decomposes its cell's id once per cell.
+struct DivU64 {
+  unsigned long long d, m;
+  int s1, s2;
+};
+
+inline DivU64 make_divu64(unsigned long long d) {
+  int l = 0;
+  while (l < 64 && (1ULL << l) < d) ++l;
+  const unsigned __int128 num = (((unsigned __int128)1 << l) - d) << 64;
+  DivU64 r;
+  r.d = d;
+  r.m = (unsigned long long)(num / d) + 1;
+  r.s1 = l < 1 ? l : 1;
+  r.s2 = l > 1 ? l - 1 : 0;
+  return r;
+}
+
+__host__ __device__ __forceinline__ unsigned long long divu64(unsigned long long n, const DivU64& v) {
+#ifdef __CUDA_ARCH__
+  const unsigned long long t = __umul64hi(v.m, n);
+#else
+  const unsigned long long t = (unsigned long long)(((unsigned __int128)v.m * n) >> 64);
+#endif
+  return (t + ((n - t) >> v.s1)) >> v.s2;
+}
+
 // analytic function  amp * prod_d trig(omega_d (x_d - speed_d t) + phase_d)
 struct DevFunction {
   int kind;
@@ -64,6 +98,9 @@ struct EclParams {
   int cells[kMaxDim];
   long long cstride[kMaxDim];
   int periodic[kMaxDim];
+  // invariant divisors of the cell-id decomposition: cells[d] and the number of
+  // x-cells cstride[dim_x]
+  DivU64 dcell[kMaxDim], dxcells;
   LineOp<T> op[kMaxDim];
   // FP64 storage only: the same operators as FP32x2 words (hd_df.cuh) for the
   // FP32x2-arithmetic kernels
@@ -110,6 +147,23 @@ __device__ __forceinline__ bool checked(const EclParams<T>& P, const T* base, lo
   (void)idx;
   return true;
 #endif
+}
+
+// coordinates of global cell g: g = gid_x + n_x gid_v, each part lexicographic
+template <int D, typename T>
+__device__ __forceinline__ void cell_coords(const EclParams<T>& P, long long g, int* cc) {
+  const unsigned long long ug = (unsigned long long)g;
+  unsigned long long gv = divu64(ug, P.dxcells);
+  unsigned long long gx = ug - gv * P.dxcells.d;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const bool x = d < P.dim_x;
+    const unsigned long long r = x ? gx : gv;
+    const unsigned long long q = divu64(r, P.dcell[d]);
+    cc[d] = int(r - q * P.dcell[d].d);
+    if (x) gx = q;
+    else gv = q;
+  }
 }
 
 enum EclMode { kApply = 0, kStageFirst = 1, kStageMid = 2, kStageLast = 3 };
@@ -341,15 +395,7 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
 
   // ---- cell coordinates
   int cc[D];
-  {
-    long long g = gg;
-    long long gx = g % (P.cstride[P.dim_x]), gv = g / (P.cstride[P.dim_x]);
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      if (d < P.dim_x) { cc[d] = int(gx % P.cells[d]); gx /= P.cells[d]; }
-      else { cc[d] = int(gv % P.cells[d]); gv /= P.cells[d]; }
-    }
-  }
+  cell_coords<D>(P, gg, cc);
   // position in the layer of the last direction (ghost faces of parts)
   const long long slot = gg - (long long)cc[D - 1] * P.cstride[D - 1];
   constexpr int CST = EclTile<D, N, T>::CST;
@@ -580,15 +626,7 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
   const bool valid = gid < P.c_hi;
   const long long gg = P.gid0 + (valid ? gid : P.c_lo);  // global id
   int cc[D];
-  {
-    long long g = gg;
-    long long gx = g % (P.cstride[P.dim_x]), gv = g / (P.cstride[P.dim_x]);
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      if (d < P.dim_x) { cc[d] = int(gx % P.cells[d]); gx /= P.cells[d]; }
-      else { cc[d] = int(gv % P.cells[d]); gv /= P.cells[d]; }
-    }
-  }
+  cell_coords<D>(P, gg, cc);
   // position in the layer of the last direction (ghost faces of parts)
   const long long slot = gg - (long long)cc[D - 1] * P.cstride[D - 1];
   // the staged input was converted to FP32x2 words in place (ecl_kernel)

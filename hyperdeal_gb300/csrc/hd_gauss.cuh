@@ -93,15 +93,7 @@ __device__ __forceinline__ void gauss_block(const EclParams<T>& P, const GaussEx
   T* so = so_all + lc * NC;
   T* sf = sf_all + lc * NC;
   int cc[D];
-  {
-    long long g = valid ? gid : 0;
-    long long gx = g % (P.cstride[P.dim_x]), gv = g / (P.cstride[P.dim_x]);
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      if (d < P.dim_x) { cc[d] = int(gx % P.cells[d]); gx /= P.cells[d]; }
-      else { cc[d] = int(gv % P.cells[d]); gv /= P.cells[d]; }
-    }
-  }
+  cell_coords<D>(P, valid ? gid : 0, cc);
   // 1. Gauss-point values v, accumulator 0
   for (int i = tl; i < NC; i += TPC) {
     sv[i] = su[i];
