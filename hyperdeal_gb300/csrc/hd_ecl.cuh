@@ -303,20 +303,37 @@ __device__ __forceinline__ const T* trace_src(const EclParams<T>& P, long long n
   return P.ghost;
 }
 
-// exterior value on a boundary (inflow) face: u+ = -u- (+ 2 g(x, t))
+// cell coordinates passed by value (an out-of-line callee gets registers, and
+// the caller's array stays in registers too)
+struct CellCoords {
+  int c[kMaxDim];
+};
+
+// exterior value of an inhomogeneous Dirichlet face, u+ = -u- + 2 g(x, t), out
+// of line: the coordinate arithmetic (FP64) of an inlined copy was hoisted out
+// of the kernels' line loops into every cell and direction, boundary or not
 template <int D, int N, typename T>
-__device__ __forceinline__ T boundary_value(const EclParams<T>& P, const int* cc, int d, int node, T um) {
-  if (!P.bc_inhom) return -um;
+__device__ __noinline__ double dirichlet_inhom_value(const EclParams<T>& P, CellCoords cc, int d, int node, double um) {
   double x[kMaxDim];
   int t = node;
 #pragma unroll
   for (int e = 0; e < D; ++e) {
     const int ie = t % N;
     t /= N;
-    x[e] = (e == d) ? node_coord(P.lo[e], cc[e], P.op[d].step > 0 ? 1.0 : 0.0, P.h[e])
-                    : node_coord(P.lo[e], cc[e], P.gl[ie], P.h[e]);
+    x[e] = (e == d) ? node_coord(P.lo[e], cc.c[e], P.op[d].step > 0 ? 1.0 : 0.0, P.h[e])
+                    : node_coord(P.lo[e], cc.c[e], P.gl[ie], P.h[e]);
   }
-  return T(dirichlet_exterior(double(um), eval_function(P.bc, x, D, P.time)));
+  return dirichlet_exterior(um, eval_function(P.bc, x, D, P.time));
+}
+
+// exterior value on a boundary (inflow) face: u+ = -u- (+ 2 g(x, t))
+template <int D, int N, typename T>
+__device__ __forceinline__ T boundary_value(const EclParams<T>& P, const int* cc, int d, int node, T um) {
+  if (!P.bc_inhom) return -um;
+  CellCoords c;
+#pragma unroll
+  for (int e = 0; e < kMaxDim; ++e) c.c[e] = e < D ? cc[e] : 0;
+  return T(dirichlet_inhom_value<D, N, T>(P, c, d, node, double(um)));
 }
 
 // ---- asynchronous global -> shared copies (cp.async; the copies of a group
@@ -616,6 +633,16 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
 // A cell's threads visit their lines in a rotated order (planes of the first
 // phase lie N*N values apart, a multiple of the bank count), and lines along
 // direction 0 (contiguous, 16-byte aligned for even N) are read as 16-byte words.
+// upwind value of a boundary line of the FP32x2 kernels, out of line (the
+// FP64 conversions and boundary arithmetic stay off the periodic path)
+template <int D, int N>
+__device__ __noinline__ f32x2 x2_boundary_value(const EclParams<double>& P, CellCoords cc, int d, int node,
+                                                const f32x2* sx) {
+  const double um = x2_to_double(sx[node]);
+  const double v = P.bc_inhom ? dirichlet_inhom_value<D, N, double>(P, cc, d, node, um) : -um;
+  return x2_from_double(v);
+}
+
 template <int D, int N, int MODE, bool GH>
 __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long long cell0, int lc, int tl,
                                              const double* su_all, double* so_all, const double* uu_all) {
@@ -716,9 +743,15 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
 #pragma unroll
               for (int q = 0; q < N; ++q) x2_mac(acc[i], Mr[i * N + q], u[q]);
             const int in = L.in_node;
-            const double upv =
-                nb >= 0 ? upd : boundary_value<D, N, double>(P, cc, d, lb + in * st, x2_to_double(sx[lb + in * st]));
-            const f32x2 up = x2_from_double(upv);
+            f32x2 up;
+            if (nb >= 0) {
+              up = x2_from_double(upd);
+            } else {
+              CellCoords c;
+#pragma unroll
+              for (int e = 0; e < kMaxDim; ++e) c.c[e] = e < D ? cc[e] : 0;
+              up = x2_boundary_value<D, N>(P, c, d, lb + in * st, sx);
+            }
             if (in == 0) x2_mac(acc[0], cin, up);
             else x2_mac(acc[N - 1], cin, up);
           }
