@@ -347,6 +347,10 @@ __device__ __forceinline__ void cp_async_small(void* smem, const void* gmem) {
   const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
   asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(BYTES) : "memory");
 }
+// bulk prefetch of [p, p + bytes) into L2 (16-byte aligned, a multiple of 16 bytes)
+__device__ __forceinline__ void prefetch_l2_bulk(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(p), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int PENDING>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory"); }
@@ -617,6 +621,16 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
   }
 }
 
+// upwind value of a boundary line of the FP32x2 kernels, out of line (the
+// FP64 conversions and boundary arithmetic stay off the periodic path)
+template <int D, int N>
+__device__ __noinline__ f32x2 x2_boundary_value(const EclParams<double>& P, CellCoords cc, int d, int node,
+                                                const f32x2* sx) {
+  const double um = x2_to_double(sx[node]);
+  const double v = P.bc_inhom ? dirichlet_inhom_value<D, N, double>(P, cc, d, node, um) : -um;
+  return x2_from_double(v);
+}
+
 // The block in FP32x2 arithmetic on FP64 storage (hd_df.cuh), organised line
 // by line instead of plane by plane: a line's N values and N accumulators are
 // read from shared memory, its N x N double-word multiply-adds and inflow
@@ -633,16 +647,6 @@ __device__ __forceinline__ void ecl_block(const EclParams<T>& P, long long cell0
 // A cell's threads visit their lines in a rotated order (planes of the first
 // phase lie N*N values apart, a multiple of the bank count), and lines along
 // direction 0 (contiguous, 16-byte aligned for even N) are read as 16-byte words.
-// upwind value of a boundary line of the FP32x2 kernels, out of line (the
-// FP64 conversions and boundary arithmetic stay off the periodic path)
-template <int D, int N>
-__device__ __noinline__ f32x2 x2_boundary_value(const EclParams<double>& P, CellCoords cc, int d, int node,
-                                                const f32x2* sx) {
-  const double um = x2_to_double(sx[node]);
-  const double v = P.bc_inhom ? dirichlet_inhom_value<D, N, double>(P, cc, d, node, um) : -um;
-  return x2_from_double(v);
-}
-
 template <int D, int N, int MODE, bool GH>
 __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long long cell0, int lc, int tl,
                                              const double* su_all, double* so_all, const double* uu_all) {
@@ -832,7 +836,17 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
     long long ncell = (P.c_hi - c0) < cpb ? (P.c_hi - c0) : cpb;
     if (!checked<NC, N>(P, P.tin, (c0 + ncell) * NC - 1)) ncell = 0;
     stage_cells<D, N, T>(dst, P.tin + c0 * NC, ncell, tid, nthr);
-    if constexpr (SU) stage_cells<D, N, T>(dstu, P.uin + c0 * NC, ncell, tid, nthr);
+    if constexpr (SU) {
+      stage_cells<D, N, T>(dstu, P.uin + c0 * NC, ncell, tid, nthr);
+    } else if constexpr ((MODE == kStageMid || MODE == kStageLast) && (NC * sizeof(T)) % 16 == 0) {
+      // the block's RK solution, read from global memory by the last phase,
+      // into L2 one block ahead (bulk prefetches of up to 16 KiB)
+      const long long bytes = ncell * NC * (long long)sizeof(T);
+      const long long off = (long long)tid * 16384;
+      if (off < bytes)
+        prefetch_l2_bulk(reinterpret_cast<const char*>(P.uin + c0 * NC) + off,
+                         unsigned(bytes - off < 16384 ? bytes - off : 16384));
+    }
   };
   long long b = blockIdx.x;
   if (b < nblk) stage(s_in0, s_u0, b);
