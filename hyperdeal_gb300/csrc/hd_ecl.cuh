@@ -647,9 +647,14 @@ __device__ __noinline__ f32x2 x2_boundary_value(const EclParams<double>& P, Cell
 // A cell's threads visit their lines in a rotated order (planes of the first
 // phase lie N*N values apart, a multiple of the bank count), and lines along
 // direction 0 (contiguous, 16-byte aligned for even N) are read as 16-byte words.
-template <int D, int N, int MODE, bool GH>
+// CVT: the staged tile still holds the FP64 values; the first direction of
+// the first phase converts each line it reads to FP32x2 in place (a cell's
+// first-phase work items are whole planes of directions 0 and 1, so every
+// value is converted once, by the thread that reads it again for direction 1,
+// before the barrier after which other threads read it)
+template <int D, int N, int MODE, bool GH, bool CVT = false>
 __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long long cell0, int lc, int tl,
-                                             const double* su_all, double* so_all, const double* uu_all) {
+                                             double* su_all, double* so_all, const double* uu_all) {
   using S = EclShape<D, N, double>;
   constexpr int NC = S::NC, TPC = S::TPC;
   constexpr int CST = EclTile<D, N, double>::CST;
@@ -661,7 +666,7 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
   // position in the layer of the last direction (ghost faces of parts)
   const long long slot = gg - (long long)cc[D - 1] * P.cstride[D - 1];
   // the staged input was converted to FP32x2 words in place (ecl_kernel)
-  const f32x2* sx = reinterpret_cast<const f32x2*>(su_all + lc * CST);
+  f32x2* sx = reinterpret_cast<f32x2*>(su_all + lc * CST);
   f32x2* so = reinterpret_cast<f32x2*>(so_all + lc * CST);
   const double* uu = uu_all ? uu_all + lc * CST : nullptr;
   const long long g0 = gid * NC;
@@ -716,7 +721,25 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
           if (nb >= 0 && j + 1 < nl && checked<NC, N>(P, fs, fbase + base + l * lst))
             upn = __ldg(face + base + l * lst);  // next line's trace
           f32x2 u[N], acc[N];
-          if ((N % 2) == 0 && st == 1) {
+          if (CVT && first) {
+            // (direction 0: contiguous lines; 16-byte words for even N)
+            double* const su = su_all + lc * CST;
+            if constexpr ((N % 2) == 0) {
+#pragma unroll
+              for (int q = 0; q < N; q += 2) {
+                const double2 w = *reinterpret_cast<const double2*>(su + lb + q);
+                u[q] = x2_from_double(w.x);
+                u[q + 1] = x2_from_double(w.y);
+                *reinterpret_cast<float4*>(sx + lb + q) = make_float4(u[q].hi, u[q].lo, u[q + 1].hi, u[q + 1].lo);
+              }
+            } else {
+#pragma unroll
+              for (int q = 0; q < N; ++q) {
+                u[q] = x2_from_double(su[lb + q]);
+                sx[lb + q] = u[q];
+              }
+            }
+          } else if ((N % 2) == 0 && st == 1) {
 #pragma unroll
             for (int q = 0; q < N; q += 2) {
               const float4 w = *reinterpret_cast<const float4*>(sx + lb + q);
@@ -862,18 +885,11 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
     cp_async_commit();
     cp_async_wait<1>();  // this thread's copies of block b are complete
     __syncthreads();     // ... and everybody's
-    if constexpr (std::is_same_v<A, f32x2>) {
-      // FP32x2: convert the staged input to double-word FP32 in place, once
-      // per value (the line loops read each value up to D times)
-      const int nv = cpb * EclTile<D, N, T>::CST;
-      for (int i = tid; i < nv; i += nthr) {
-        const double v = cur[i];
-        reinterpret_cast<f32x2*>(cur)[i] = x2_from_double(v);
-      }
-      __syncthreads();
-    }
+    // (FP32x2: the block converts the staged input to double-word FP32 in
+    // place as its first direction reads it, once per value -- the line loops
+    // read each value up to D times)
     if constexpr (std::is_same_v<A, f32x2>)
-      ecl_block_x2<D, N, MODE, GH>(P, P.c_lo + b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+      ecl_block_x2<D, N, MODE, GH, true>(P, P.c_lo + b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
     else
       ecl_block<D, N, T, MODE, GH>(P, P.c_lo + b * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
     __syncthreads();     // cur and s_o are free for the next blocks
