@@ -644,9 +644,10 @@ __device__ __noinline__ f32x2 x2_boundary_value(const EclParams<double>& P, Cell
 // renormalised: they are only ever added to (the TwoSum of x2_mac is exact
 // for any hi, lo), and the few dozen low parts summed per value stay far
 // below hi; the result's conversion adds hi and lo in FP64.
-// A cell's threads visit their lines in a rotated order (planes of the first
-// phase lie N*N values apart, a multiple of the bank count), and lines along
-// direction 0 (contiguous, 16-byte aligned for even N) are read as 16-byte words.
+// In the first phase a cell's threads visit their lines in a rotated order
+// (its planes lie N*N values apart, a multiple of the bank count), and lines
+// along direction 0 (contiguous, 16-byte aligned for even N) are read as
+// 16-byte words.
 // CVT: the staged tile still holds the FP64 values; the first direction of
 // the first phase converts each line it reads to FP32x2 in place (a cell's
 // first-phase work items are whole planes of directions 0 and 1, so every
@@ -681,7 +682,11 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
     const int nitems = dB >= 0 ? ipow(N, D - 2) : ipow(N, D - 1);
     const int ndir = dB >= 0 ? 2 : 1;
     const int nl = dB >= 0 ? N : 1;      // lines per direction in a work item
-    const int rot = nl > 1 ? tl % N : 0;
+    // first line of the thread: rotated in the first phase only (its planes lie
+    // N*N values apart); in the later phases the threads of a warp take the same
+    // line, whose nodes -- and upwind trace values -- are consecutive across
+    // the threads, so that their global loads and stores coalesce
+    const int rot = (ph == 0 && nl > 1) ? tl % N : 0;
     const bool lastph = ph == S::NPH - 1;
     for (int item = tl; item < nitems; item += TPC) {
       const int base = item_base<D, N>(item, dA, dB);
@@ -712,14 +717,22 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
         const double* face = fs + (fo + L.nb_node * st);
         int l = rot;
         const long long fbase = fo + L.nb_node * st;  // index of `face` relative to fs
-        double upn = nb >= 0 && checked<NC, N>(P, fs, fbase + base + l * lst) ? __ldg(face + base + l * lst) : 0.0;
+        // the upwind trace values of all the item's lines, in visiting order,
+        // issued together before the first line
+        double fu[N];
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+          const int lj = (rot + j) % N;
+          fu[j] = j < nl && nb >= 0 && checked<NC, N>(P, fs, fbase + base + lj * lst) ? __ldg(face + base + lj * lst)
+                                                                                        : 0.0;
+        }
 #pragma unroll 1
         for (int j = 0; j < nl; ++j) {
           const int lb = base + l * lst;
-          const double upd = upn;
+          const double upd = fu[0];
+#pragma unroll
+          for (int k = 0; k + 1 < N; ++k) fu[k] = fu[k + 1];
           l = l + 1 < nl ? l + 1 : 0;
-          if (nb >= 0 && j + 1 < nl && checked<NC, N>(P, fs, fbase + base + l * lst))
-            upn = __ldg(face + base + l * lst);  // next line's trace
           f32x2 u[N], acc[N];
           if (CVT && first) {
             // (direction 0: contiguous lines; 16-byte words for even N)
