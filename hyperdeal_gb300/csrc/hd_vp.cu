@@ -1455,6 +1455,8 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
   g.cstride[g.D] = st;
   g.n_cells = st;
   g.nx_dofs = g.ncx * g.NCx;
+  for (int i = 0; i < g.D; ++i) g.dcell[i] = hd::make_divu64((unsigned long long)g.cells[i]);
+  g.dncx = hd::make_divu64((unsigned long long)g.ncx);
   vp_tables(g.N, g.gl, g.glw, g.Dm);
   const int N = g.N;
   for (int i = 0; i < N; ++i)

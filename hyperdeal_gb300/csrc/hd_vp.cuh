@@ -26,6 +26,7 @@ struct VpGeom {
   int D, dx, N, NCx, NC;
   long long ncx, ncv, n_cells, nx_dofs;
   int cells[kMaxDim];
+  DivU64 dcell[kMaxDim], dncx;  // invariant divisors of cells[d] and ncx
   long long cstride[kMaxDim + 1];
   double lo[kMaxDim], h[kMaxDim];
   double gl[kMaxN], glw[kMaxN];
@@ -50,6 +51,26 @@ struct VpGeom {
   double Ap[kMaxN * kMaxN], Am[kMaxN * kMaxN];
   double cp[kMaxN], cm[kMaxN];
 };
+
+// coordinates of cell gid (gid = gid_x + ncx gid_v, each part lexicographic);
+// returns gid_x
+template <int D>
+__device__ __forceinline__ long long vp_cell_coords(const VpGeom& g, long long gid, int* cc) {
+  const unsigned long long ug = (unsigned long long)gid;
+  unsigned long long b = divu64(ug, g.dncx);
+  const unsigned long long gx = ug - b * g.dncx.d;
+  unsigned long long a = gx;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const bool x = d < D / 2;
+    const unsigned long long r = x ? a : b;
+    const unsigned long long q = divu64(r, g.dcell[d]);
+    cc[d] = int(r - q * g.dcell[d].d);
+    if (x) a = q;
+    else b = q;
+  }
+  return (long long)gx;
+}
 
 // x <- A applied along direction e of an nd-dimensional tensor x with N^nd
 // entries (A row-major N x N, A[i*N + j]), in place; the block's threads

@@ -42,12 +42,9 @@ __device__ __forceinline__ void vp_block(const VpAdvParams<T>& P, const VpLine<T
   long long gx = 0;
   {
     const long long gg = valid ? gid : 0;
-    gx = gg % g.ncx;
-    long long a = gx, b = gg / g.ncx;
+    gx = vp_cell_coords<D>(g, gg, cc);
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-      if (d < DX) { cc[d] = int(a % g.cells[d]); a /= g.cells[d]; }
-      else { cc[d] = int(b % g.cells[d]); b /= g.cells[d]; }
       const long long cs = g.cstride[d];
       nbL[d] = cc[d] > 0 ? gg - cs : gg + (long long)(g.cells[d] - 1) * cs;
       nbR[d] = cc[d] + 1 < g.cells[d] ? gg + cs : gg - (long long)(g.cells[d] - 1) * cs;
@@ -256,12 +253,9 @@ __device__ __forceinline__ void vp_block_x2(const VpAdvParams<double>& P, const 
   long long gx = 0;
   {
     const long long gg = valid ? gid : 0;
-    gx = gg % g.ncx;
-    long long a = gx, b = gg / g.ncx;
+    gx = vp_cell_coords<D>(g, gg, cc);
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-      if (d < DX) { cc[d] = int(a % g.cells[d]); a /= g.cells[d]; }
-      else { cc[d] = int(b % g.cells[d]); b /= g.cells[d]; }
       const long long cs = g.cstride[d];
       nbL[d] = cc[d] > 0 ? gg - cs : gg + (long long)(g.cells[d] - 1) * cs;
       nbR[d] = cc[d] + 1 < g.cells[d] ? gg + cs : gg - (long long)(g.cells[d] - 1) * cs;
