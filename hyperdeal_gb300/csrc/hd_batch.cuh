@@ -79,7 +79,16 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
     const long long c0 = lb * cpb;
     const long long ncell = (P.n_cells - c0) < cpb ? (P.n_cells - c0) : cpb;
     stage_cells<D, N, T>(dst, P.tin + c0 * NC, ncell, tid, nthr);
-    if constexpr (SU) stage_cells<D, N, T>(dstu, P.uin + c0 * NC, ncell, tid, nthr);
+    if constexpr (SU) {
+      stage_cells<D, N, T>(dstu, P.uin + c0 * NC, ncell, tid, nthr);
+    } else if constexpr ((MODE == kStageMid || MODE == kStageLast) && (NC * sizeof(T)) % 16 == 0) {
+      // the block's RK solution into L2 one block ahead (as in ecl_kernel)
+      const long long bytes = ncell * NC * (long long)sizeof(T);
+      const long long off = (long long)tid * 16384;
+      if (off < bytes)
+        prefetch_l2_bulk(reinterpret_cast<const char*>(P.uin + c0 * NC) + off,
+                         unsigned(bytes - off < 16384 ? bytes - off : 16384));
+    }
   };
   long long b = blockIdx.x;
   int inst = 0;
@@ -104,14 +113,10 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
     cp_async_wait<1>();
     __syncthreads();
     if constexpr (std::is_same_v<A, f32x2>) {
-      // FP32x2: the staged input converted to double-word FP32 in place (as in ecl_kernel)
-      const int nv = cpb * EclTile<D, N, T>::CST;
-      for (int i = tid; i < nv; i += nthr) {
-        const double v = cur[i];
-        reinterpret_cast<f32x2*>(cur)[i] = x2_from_double(v);
-      }
-      __syncthreads();
-      ecl_block_x2<D, N, MODE, false>(params[inst], (b - s_prefix[inst]) * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
+      // FP32x2: the block converts the staged input to double-word FP32 in
+      // place as its first direction reads it (as in ecl_kernel)
+      ecl_block_x2<D, N, MODE, false, true>(params[inst], (b - s_prefix[inst]) * cpb, lc, tl, cur, s_o,
+                                            SU ? curu : nullptr);
     } else {
       ecl_block<D, N, T, MODE, false>(params[inst], (b - s_prefix[inst]) * cpb, lc, tl, cur, s_o, SU ? curu : nullptr);
     }
