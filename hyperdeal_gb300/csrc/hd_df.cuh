@@ -58,6 +58,16 @@ __device__ __forceinline__ void x2_mac(f32x2& acc, const f32x2& c, const f32x2& 
   acc.lo = __fadd_rn(acc.lo, __fadd_rn(e, pl));
 }
 
+// c * u as the first term of a sum: x2_mac on a zero accumulator without
+// the TwoSum with zero (the same value; a zero product may keep its sign)
+__device__ __forceinline__ f32x2 x2_mul(const f32x2& c, const f32x2& u) {
+  const float ph = __fmul_rn(c.hi, u.hi);
+  float pl = __fmaf_rn(c.hi, u.hi, -ph);
+  pl = __fmaf_rn(c.hi, u.lo, pl);
+  pl = __fmaf_rn(c.lo, u.hi, pl);
+  return f32x2{ph, pl};
+}
+
 // hi + lo with |lo| <= ulp(hi) / 2 (TwoSum: valid whatever the magnitudes)
 __device__ __forceinline__ f32x2 x2_norm(const f32x2& a) {
   f32x2 r;

@@ -779,9 +779,13 @@ __device__ __forceinline__ void ecl_block_x2(const EclParams<double>& P, long lo
           }
           if (act) {
 #pragma unroll
-            for (int i = 0; i < N; ++i)
+            for (int i = 0; i < N; ++i) {
+              // (the first direction's accumulators start from its first product)
+              if (first) acc[i] = x2_mul(Mr[i * N], u[0]);
+              else x2_mac(acc[i], Mr[i * N], u[0]);
 #pragma unroll
-              for (int q = 0; q < N; ++q) x2_mac(acc[i], Mr[i * N + q], u[q]);
+              for (int q = 1; q < N; ++q) x2_mac(acc[i], Mr[i * N + q], u[q]);
+            }
             const int in = L.in_node;
             f32x2 up;
             if (nb >= 0) {

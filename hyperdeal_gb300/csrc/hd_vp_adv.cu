@@ -333,17 +333,14 @@ __device__ __forceinline__ void vp_block_x2(const VpAdvParams<double>& P, const 
           if (s2.hi != 0.f) {
 #pragma unroll
             for (int i = 0; i < N; ++i) {
-              f32x2 t{0.f, 0.f};
+              f32x2 t = x2_mul(Lk.G[i * N], u[0]);
 #pragma unroll
-              for (int q = 0; q < N; ++q) x2_mac(t, Lk.G[i * N + q], u[q]);
+              for (int q = 1; q < N; ++q) x2_mac(t, Lk.G[i * N + q], u[q]);
               x2_mac(acc[i], s2, x2_norm(t));
             }
             // upwind face: (s / w_k)(u+ - u-) at the inflow node
-            f32x2 c0{0.f, 0.f}, ck{0.f, 0.f};
-            x2_mac(c0, s2, Lk.winv0);
-            x2_mac(ck, s2, Lk.winvk);
-            c0 = x2_norm(c0);
-            ck = x2_norm(ck);
+            const f32x2 c0 = x2_norm(x2_mul(s2, Lk.winv0));
+            const f32x2 ck = x2_norm(x2_mul(s2, Lk.winvk));
             const f32x2 nck{-ck.hi, -ck.lo};
             const f32x2 upx = x2_from_double(up);
             if (pos) {
