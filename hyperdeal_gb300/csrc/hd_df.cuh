@@ -17,8 +17,9 @@
 //     the low parts summed in FP32 -- the "double-word times double-word" and
 //     "double-word plus double-word" building blocks of Joldes, Muller and
 //     Popescu, "Tight and rigorous error bounds for basic building blocks of
-//     double-word arithmetic", ACM TOMS 44 (2017), with the renormalisation
-//     deferred to the end of a line;
+//     double-word arithmetic", ACM TOMS 44 (2017); a sum is renormalised
+//     only where it becomes a factor of another product (accumulators that
+//     are only added to stay unnormalised);
 //   * FP32x2 -> storage: hi and lo become doubles by integer operations and
 //     one FP64 add rounds their sum.
 // The relative error of a contraction is a few units of 2^-48 of the sum of
