@@ -590,7 +590,7 @@ __global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
   }
   double bb = -1.0;  // ||rhs||^2 once summed
   if (ls && lsk > 0) {
-    // the judge: the guess starts CG only if its residual is below ||rhs|| (that of 0)
+    // the selection: the guess starts CG only if its residual is below ||rhs|| (that of 0)
     const double2 jb = grid_sum2(grid, lbb, lr0, A.red, slot, sh);
     bb = jb.x;
     const bool keep = jb.y < jb.x;
@@ -740,7 +740,7 @@ __global__ void residual_partials(long long n, int W, const int* __restrict__ co
   }
 }
 
-// the judge: the candidate with the smaller initial residual starts CG
+// the selection: the candidate with the smaller initial residual starts CG
 // (u1 is copied over u0 when it wins, and counted)
 __global__ void choose_guess(long long n, int nblocks, const double* __restrict__ partial, double* __restrict__ u0,
                              const double* __restrict__ u1, VpStats* stats) {
@@ -954,7 +954,7 @@ struct hd_vp {
   double* d_dy;       // phi - phi_prev
   bool have_prev;
   long long observed;  // pairs given to the learned model
-  double* d_judge;    // residual partials of the judge
+  double* d_pick;     // residual partials of the guess selection
   int cg_grid;
   int guess;
   hd::VpModel* model;  // learned initial guess, Adam-trained (HD_VP_FIT_ADAM)
@@ -1082,7 +1082,7 @@ void vp_free(hd_vp* v) {
   cudaFree(v->d_phi_prev);
   cudaFree(v->d_dx);
   cudaFree(v->d_dy);
-  cudaFree(v->d_judge);
+  cudaFree(v->d_pick);
   cudaFree(v->d_binv);
   cudaFree(v->d_pipe);
   cudaFree(v->d_ls);
@@ -1322,7 +1322,7 @@ int solve_poisson(hd_vp* v, cudaStream_t s) {
     if (rc) return rc;
   }
   if (v->guess == HD_VP_GUESS_LEARNED && v->d_ls) {
-    // least-squares fit: one launch predicts, judges, solves and adds the pair
+    // least-squares fit: one launch predicts, selects, solves and adds the pair
     v->ls_head = (v->ls_head + 1) % v->ls_kkeep;
     if (v->ls_nraw < v->ls_kkeep) ++v->ls_nraw;
     return launch_poisson(v, 3, s);
@@ -1331,7 +1331,7 @@ int solve_poisson(hd_vp* v, cudaStream_t s) {
   if (!learned) return launch_poisson(v, 3, s);
   // learned: the solution map is linear, so the model is trained on and
   // applied to differences to the previous solve: guess = phi_prev +
-  // model(rho - rho_prev), judged against phi_prev by the initial residual
+  // model(rho - rho_prev), weighed against phi_prev by the initial residual
   // (without a previous solve both differences are taken from zero)
   int rc = launch_poisson(v, 1, s);
   if (rc) return rc;
@@ -1349,10 +1349,10 @@ int solve_poisson(hd_vp* v, cudaStream_t s) {
     rc = vcuda(hd::vp_model_predict(v->model, v->d_dx, v->d_guess, s), "learned guess");
     if (rc) return rc;
     hd::add_kernel<<<nb, 256, 0, s>>>(nx, v->d_phi_prev, v->d_guess);
-    constexpr int kJudgeBlocks = 64;
-    hd::residual_partials<<<kJudgeBlocks, 256, 0, s>>>(nx, v->ell_w, v->d_ell_col, v->d_ell_val, v->d_rhs, v->d_phi,
-                                                       v->d_guess, v->d_judge);
-    hd::choose_guess<<<1, 1024, 0, s>>>(nx, kJudgeBlocks, v->d_judge, v->d_phi, v->d_guess, v->d_stats);
+    constexpr int kPickBlocks = 64;
+    hd::residual_partials<<<kPickBlocks, 256, 0, s>>>(nx, v->ell_w, v->d_ell_col, v->d_ell_val, v->d_rhs, v->d_phi,
+                                                       v->d_guess, v->d_pick);
+    hd::choose_guess<<<1, 1024, 0, s>>>(nx, kPickBlocks, v->d_pick, v->d_phi, v->d_guess, v->d_stats);
   }
   rc = vcuda(cudaGetLastError(), "learned guess");
   if (rc) return rc;
@@ -1545,7 +1545,7 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
   alloc((void**)&v->d_phi_prev, sizeof(double) * nx);
   alloc((void**)&v->d_dx, sizeof(double) * nx);
   alloc((void**)&v->d_dy, sizeof(double) * nx);
-  alloc((void**)&v->d_judge, sizeof(double) * 2 * 64);
+  alloc((void**)&v->d_pick, sizeof(double) * 2 * 64);
   alloc((void**)&v->d_pipe, sizeof(int) * 2);
   if (e != cudaSuccess) { vp_free(v); return vcuda(e, "hd_vp_create: cudaMalloc"); }
   {

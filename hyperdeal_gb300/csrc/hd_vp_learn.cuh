@@ -5,7 +5,7 @@
 // is trained online with Adam on the (x, y) pairs that the solver itself
 // produces (a ring of the last H pairs); the caller passes density and
 // potential differences between consecutive solves.  Training and inference
-// run in this project's own kernels (hd_vp_learn.cu).  The caller judges the
+// run in this project's own kernels (hd_vp_learn.cu).  The caller weighs the
 // resulting guess against the previous potential by the initial CG residual;
 // the better one starts CG, which still converges to the same tolerance.
 #pragma once

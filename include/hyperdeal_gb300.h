@@ -389,7 +389,7 @@ enum hd_vp_guess {
  *   basis is rebuilt from the last learn_history pairs (0: 3/8 of the rank,
  *   less than the rank).
  * ADAM: FP32 weights trained by Adam on normalised differences between
- *   consecutive solves, guess = phi_prev + W2 W1 (rho - rho_prev), judged
+ *   consecutive solves, guess = phi_prev + W2 W1 (rho - rho_prev), weighed
  *   against phi_prev (learn_rank 0: 32, learn_history 0: 64 pairs); its
  *   loss and gradients are exposed by hd_vp_learn_loss_grad. */
 enum hd_vp_learn_fit { HD_VP_FIT_LEAST_SQUARES = 0, HD_VP_FIT_ADAM = 1 };

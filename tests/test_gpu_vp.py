@@ -239,7 +239,7 @@ def _run_steps(op, f, n_steps, dt):
 @pytest.mark.parametrize("rhs_relative", [False, True])
 def test_learned_guess_same_solution(rhs_relative, learn_fit):
     """The learned guess only changes where CG starts: the fields after a number of
-    steps agree with the previous-potential run to the CG tolerance, the judge
+    steps agree with the previous-potential run to the CG tolerance, the selection
     picks the learned guess at least once, and the first solves fall back (the
     least-squares fit starts from 0 before its first pair, the Adam-trained
     network from the previous potential before its second)."""
