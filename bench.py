@@ -210,12 +210,15 @@ def run_vp(args):
     f0 = V.perturbed_maxwellian(VP_DIM_X, eps=0.01, k=0.5, perturbed_dims=(0, 1))
 
     def make(guess, dtype, tol, rhs_rel, precond=args.vp_precond):
-        # "learned": the least-squares fitted network; "learned_adam": the Adam-trained one
+        # "learned": the least-squares fitted network; "learned_adam": the Adam-trained one;
+        # "direct": no CG, the SIPG matrix's pseudo-inverse applied (hd_vp_solver)
         p = V.VlasovPoissonParameters(VP_DIM_X, DEGREE, [VP_CELLS_X] * 2, [VP_CELLS_V] * 2, [0.0] * 2,
                                       [two_pi] * 2, [-6.0] * 2, [6.0] * 2, dtype=dtype, cg_tol=tol,
-                                      guess="learned" if guess.startswith("learned") else guess,
+                                      guess="learned" if guess.startswith("learned") else
+                                      "zero" if guess == "direct" else guess,
                                       cg_rhs_relative=rhs_rel, cg_precond=precond,
-                                      learn_fit="adam" if guess == "learned_adam" else "least_squares")
+                                      learn_fit="adam" if guess == "learned_adam" else "least_squares",
+                                      poisson_solver="direct" if guess == "direct" else "cg")
         return V.VlasovPoissonOperation(p)
 
     stream = torch.cuda.current_stream()
@@ -225,7 +228,7 @@ def run_vp(args):
     selected = [r.strip() for r in args.vp_runs.split(",")]
     for dtype in ("f64", "f64x", "f32"):  # f64x: FP64 storage, FP32x2 advection contractions
         for guess in ("previous", "zero", "learned", "learned_adam", "previous_noprecond", "zero_noprecond",
-                      "learned_noprecond"):
+                      "learned_noprecond", "direct"):
             if "%s/%s" % (dtype, guess) not in selected:
                 continue
             pre = "none" if guess.endswith("_noprecond") else args.vp_precond
@@ -629,8 +632,9 @@ def main():
     ap.add_argument("--vp-runs", default="f64/previous,f64/zero,f64/learned,f64/learned_adam,f64/previous_noprecond,"
                                          "f64/zero_noprecond,f64/learned_noprecond,f64x/previous,f64x/zero,"
                                          "f64x/learned,f32/previous,f32/zero,f32/learned,f32/previous_noprecond,"
-                                         "f32/zero_noprecond,f32/learned_noprecond",
-                    help="dtype/guess combinations timed (vp2x2v; _noprecond: CG without the preconditioner)")
+                                         "f32/zero_noprecond,f32/learned_noprecond,f64/direct,f64x/direct,f32/direct",
+                    help="dtype/guess combinations timed (vp2x2v; _noprecond: CG without the preconditioner; "
+                         "direct: the pseudo-inverse instead of CG)")
     ap.add_argument("--vp-precond", default="block_jacobi", choices=["block_jacobi", "none"],
                     help="preconditioner of the Poisson CG (vp2x2v)")
     args = ap.parse_args()

@@ -38,6 +38,7 @@ HD_ARITH_NATIVE, HD_ARITH_FP32X2 = 0, 1
 HD_VP_GUESS_ZERO, HD_VP_GUESS_PREVIOUS, HD_VP_GUESS_LEARNED = 0, 1, 2
 HD_CELLS_ALL, HD_CELLS_INTERIOR, HD_CELLS_BOUNDARY = 0, 1, 2
 HD_VP_PRECOND_NONE, HD_VP_PRECOND_BLOCK_JACOBI = 0, 1
+HD_VP_SOLVER_CG, HD_VP_SOLVER_DIRECT = 0, 1
 HD_VP_FIT_LEAST_SQUARES, HD_VP_FIT_ADAM = 0, 1
 
 
@@ -72,7 +73,7 @@ class hd_vp_desc(ctypes.Structure):
                 ("cg_tol", ctypes.c_double), ("cg_max_iter", ctypes.c_int), ("guess", ctypes.c_int),
                 ("learn_rank", ctypes.c_int), ("learn_history", ctypes.c_int), ("cg_rhs_relative", ctypes.c_int),
                 ("learn_every", ctypes.c_int), ("cg_precond", ctypes.c_int), ("learn_fit", ctypes.c_int),
-                ("quadrature", ctypes.c_int)]
+                ("quadrature", ctypes.c_int), ("poisson_solver", ctypes.c_int)]
 
 
 class hd_part_layout(ctypes.Structure):

@@ -291,7 +291,7 @@ struct PoissonArgs {
   const double* val;
   const double* partial;  // moment partials (nchunks x nx)
   int nchunks;
-  int phases;             // bit 0: rho and rhs from the partials; bit 1: CG and the field
+  int phases;             // bit 0: rho and rhs from the partials; bit 1: CG and the field; bit 2: the field only
   double* rho;
   double* rhs;
   double* x;              // potential: initial guess in, solution out
@@ -495,6 +495,46 @@ __device__ __forceinline__ double block_jacobi_row(const VpGeom& g, const double
   return z;
 }
 
+// the field E = grad(phi) at the x-nodes (derivative_container.h:158-251),
+// and E / h_v in the storage precision, for this thread's rows
+__device__ void poisson_field(const PoissonArgs& A, long long t0, long long stride) {
+  const VpGeom& g = A.g;
+  const long long n = g.nx_dofs;
+  const int N = g.N;
+  for (long long i = t0; i < n; i += stride) {
+    const long long gx = i / g.NCx;
+    const int ix = int(i - gx * g.NCx);
+    int s = 1;
+    for (int d = 0; d < g.dx; ++d) {
+      const int idd = (ix / s) % N;
+      const int base = ix - idd * s;
+      double a = 0.0;
+      if (g.gauss) {
+        // at Gauss point ix: the derivative along d, the values (S) along the others
+        for (int j = 0; j < g.NCx; ++j) {
+          double w = 1.0;
+          int qa = ix, jb = j;
+          for (int e2 = 0; e2 < g.dx; ++e2) {
+            const int q = qa % N, jj = jb % N;
+            w *= e2 == d ? g.GS[q * N + jj] : g.S[q * N + jj];
+            qa /= N;
+            jb /= N;
+          }
+          a = fma(w, A.x[gx * g.NCx + j], a);
+        }
+      } else {
+        for (int j = 0; j < N; ++j) a += g.Dm[idd * N + j] * A.x[gx * g.NCx + base + j * s];
+      }
+      const double e = a / g.h[d];
+      A.E[i * g.dx + d] = e;
+      const double es = e / g.h[g.dx + d];
+      if (A.es_f32) static_cast<float*>(A.es)[i * g.dx + d] = float(es);
+      else static_cast<double*>(A.es)[i * g.dx + d] = es;
+      s *= N;
+    }
+  }
+}
+
 // One cooperative launch per solve (or two around the learned guess):
 // rho and the right-hand side (application.h:531-568: rho~ = rho - mean,
 // rhs = -M rho~, rhs -= mean), conjugate gradients on the SIPG system, and
@@ -541,6 +581,16 @@ __global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
     }
     const double mean2 = grid_sum2(grid, l2, 0.0, A.red, slot, sh).x / double(n);
     for (long long i = t0; i < n; i += stride) A.rhs[i] -= mean2;
+  }
+  if (A.phases & 4) {
+    // direct solve: x was written by the dense product (an earlier launch)
+    poisson_field(A, t0, stride);
+    if (t0 == 0) {
+      A.stats->last_iters = 0;
+      A.stats->solves += 1;
+      A.stats->last_res = 0.0;
+    }
+    return;
   }
   if (!(A.phases & 2)) return;
   // least-squares learned guess: x = Z (Q^T rhs), or 0 before the first pair
@@ -680,45 +730,79 @@ __global__ void __launch_bounds__(kCgThreads) poisson_kernel(PoissonArgs A) {
     if (t0 == 0) *A.lsCount = lsk;
   }
   grid.sync();  // x complete before the field reads it
-  const int N = g.N;
-  for (long long i = t0; i < n; i += stride) {
-    const long long gx = i / g.NCx;
-    const int ix = int(i - gx * g.NCx);
-    int s = 1;
-    for (int d = 0; d < g.dx; ++d) {
-      const int idd = (ix / s) % N;
-      const int base = ix - idd * s;
-      double a = 0.0;
-      if (g.gauss) {
-        // at Gauss point ix: the derivative along d, the values (S) along the others
-        for (int j = 0; j < g.NCx; ++j) {
-          double w = 1.0;
-          int qa = ix, jb = j;
-          for (int e2 = 0; e2 < g.dx; ++e2) {
-            const int q = qa % N, jj = jb % N;
-            w *= e2 == d ? g.GS[q * N + jj] : g.S[q * N + jj];
-            qa /= N;
-            jb /= N;
-          }
-          a = fma(w, A.x[gx * g.NCx + j], a);
-        }
-      } else {
-        for (int j = 0; j < N; ++j) a += g.Dm[idd * N + j] * A.x[gx * g.NCx + base + j * s];
-      }
-      const double e = a / g.h[d];
-      A.E[i * g.dx + d] = e;
-      const double es = e / g.h[g.dx + d];
-      if (A.es_f32) static_cast<float*>(A.es)[i * g.dx + d] = float(es);
-      else static_cast<double*>(A.es)[i * g.dx + d] = es;
-      s *= N;
-    }
-  }
+  poisson_field(A, t0, stride);
   if (t0 == 0) {
     A.stats->last_iters = it;
     A.stats->total_iters += it;
     A.stats->solves += 1;
     A.stats->last_res = r0 > 0.0 ? rnorm / r0 : 0.0;
   }
+}
+
+// ---------------------------------------------------------------- direct solve
+// The x-space SIPG matrix A (fixed for the whole run) is singular only in the
+// constants; the right-hand sides are mean-free, and on them the inverse of
+// A + beta 1 1^T acts as the pseudo-inverse.  It is formed once, densely, by
+// Gauss-Jordan elimination in place without pivoting (the matrix is symmetric
+// positive definite): step k scales the pivot row by 1/a_kk and subtracts
+// a_ik times it from every other row, keeping -a_ik/a_kk in column k.
+
+// M = beta everywhere, then += A from the ELL form (each thread its own row)
+__global__ void dense_from_ell(long long n, int W, const int* __restrict__ col, const double* __restrict__ val,
+                               double* __restrict__ M) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int k = 0; k < W; ++k) {
+    const double v = val[(size_t)k * n + i];
+    if (v != 0.0) M[i * n + col[(size_t)k * n + i]] += v;
+  }
+}
+
+__global__ void fill_kernel(long long n, double v, double* __restrict__ x) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) x[i] = v;
+}
+
+// step k, part 1: the pivot row divided by the pivot (its diagonal entry
+// 1/a_kk) and the pivot column, before the step overwrites them
+__global__ void gj_pivot(long long n, int k, const double* __restrict__ M, double* __restrict__ rowk,
+                         double* __restrict__ colk) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double piv = M[(long long)k * n + k];
+  rowk[i] = i == k ? 1.0 / piv : M[(long long)k * n + i] / piv;
+  colk[i] = M[i * n + k];
+}
+
+// step k, part 2: every entry (row blockIdx.y)
+__global__ void gj_update(long long n, int k, double* __restrict__ M, const double* __restrict__ rowk,
+                          const double* __restrict__ colk) {
+  const long long i = blockIdx.y;
+  const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  double* const e = M + i * n + j;
+  if (i == k) *e = rowk[j];
+  else if (j == k) *e = -colk[i] * rowk[k];
+  else *e = fma(-colk[i], rowk[j], *e);
+}
+
+// x = M b: one warp per row, the lanes over the columns, a fixed-order reduction
+__global__ void dense_gemv(long long n, const double* __restrict__ M, const double* __restrict__ b,
+                           double* __restrict__ x) {
+  const long long row = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;  // (whole warps)
+  const double* r = M + row * n;
+  double s0 = 0.0, s1 = 0.0;
+  long long j = lane;
+  for (; j + 32 < n; j += 64) {
+    s0 = fma(__ldg(r + j), __ldg(b + j), s0);
+    s1 = fma(__ldg(r + j + 32), __ldg(b + j + 32), s1);
+  }
+  if (j < n) s0 = fma(__ldg(r + j), __ldg(b + j), s0);
+  double s = s0 + s1;
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) x[row] = s;
 }
 
 // per-block partial sums of ||rhs - A u||^2 for two candidate vectors u0, u1
@@ -942,6 +1026,7 @@ struct hd_vp {
   void* d_es;         // E / h_v in the storage precision
   double* d_cg;       // r, p, A z, A p, z (5 * nx) + reductions (2 halves * 3 values * cg_grid)
   double* d_binv;     // cell-block Jacobi preconditioner: ncx blocks of NCx x NCx (null: none)
+  double* d_ainv;     // direct solve: the pseudo-inverse of the SIPG matrix, nx x nx (null: CG)
   int ell_w;          // SIPG matrix in ELL form (ell_w entries per row, [k][row])
   int* d_ell_col;
   double* d_ell_val;
@@ -1084,6 +1169,7 @@ void vp_free(hd_vp* v) {
   cudaFree(v->d_dy);
   cudaFree(v->d_pick);
   cudaFree(v->d_binv);
+  cudaFree(v->d_ainv);
   cudaFree(v->d_pipe);
   cudaFree(v->d_ls);
   cudaFree(v->d_ls_count);
@@ -1234,6 +1320,47 @@ int build_block_jacobi(hd_vp* v) {
   return vcuda(e, "hd_vp_create: preconditioner");
 }
 
+// Direct solve: A + beta 1 1^T (beta = the mean diagonal entry over nx, so
+// that the constants get an eigenvalue of the size of A's diagonal) formed
+// densely on the device and inverted in place by Gauss-Jordan elimination
+// (2 nx launches, once per operator).
+constexpr long long kDirectMaxDofs = 8192;
+int build_direct(hd_vp* v) {
+  const long long nx = v->g.nx_dofs;
+  if (nx > kDirectMaxDofs) return vfail(HD_ERR_UNSUPPORTED, "hd_vp_create: direct Poisson solve up to 8192 x-DoFs");
+  const int W = v->ell_w;
+  std::vector<int> col(size_t(W) * nx);
+  std::vector<double> val(size_t(W) * nx);
+  cudaError_t e = cudaMemcpy(col.data(), v->d_ell_col, sizeof(int) * col.size(), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(val.data(), v->d_ell_val, sizeof(double) * val.size(), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return vcuda(e, "hd_vp_create: matrix read-back");
+  double tr = 0.0;
+  for (long long i = 0; i < nx; ++i)
+    for (int k = 0; k < W; ++k)
+      if (col[size_t(k) * nx + i] == i) tr += val[size_t(k) * nx + i];
+  if (!(tr > 0.0)) return vfail(HD_ERR_INVALID, "hd_vp_create: Poisson matrix without a positive diagonal");
+  const double beta = tr / double(nx) / double(nx);
+  double* buf = nullptr;
+  e = cudaMalloc(&v->d_ainv, sizeof(double) * size_t(nx) * nx);
+  if (e == cudaSuccess) e = cudaMalloc(&buf, sizeof(double) * 2 * nx);
+  if (e != cudaSuccess) {
+    cudaFree(buf);
+    return vcuda(e, "hd_vp_create: direct solve storage");
+  }
+  const long long nn = nx * nx;
+  hd::fill_kernel<<<unsigned((nn + 255) / 256), 256>>>(nn, beta, v->d_ainv);
+  hd::dense_from_ell<<<unsigned((nx + 255) / 256), 256>>>(nx, W, v->d_ell_col, v->d_ell_val, v->d_ainv);
+  const dim3 ug(unsigned((nx + 255) / 256), unsigned(nx));
+  for (int k = 0; k < nx; ++k) {
+    hd::gj_pivot<<<unsigned((nx + 255) / 256), 256>>>(nx, k, v->d_ainv, buf, buf + nx);
+    hd::gj_update<<<ug, 256>>>(nx, k, v->d_ainv, buf, buf + nx);
+  }
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  cudaFree(buf);
+  return vcuda(e, "hd_vp_create: direct solve (Gauss-Jordan)");
+}
+
 hd::PoissonArgs poisson_args(hd_vp* v, int phases) {
   hd::PoissonArgs A;
   const long long nx = v->g.nx_dofs;
@@ -1317,6 +1444,15 @@ int launch_poisson(hd_vp* v, int phases, cudaStream_t s) {
 // initial guess and the field; asynchronous (statistics stay on the device)
 int solve_poisson(hd_vp* v, cudaStream_t s) {
   const long long nx = v->g.nx_dofs;
+  if (v->d_ainv) {
+    // direct: rho and rhs, phi = A^+ rhs, the field
+    int rc = launch_poisson(v, 1, s);
+    if (rc) return rc;
+    hd::dense_gemv<<<unsigned((nx * 32 + 255) / 256), 256, 0, s>>>(nx, v->d_ainv, v->d_rhs, v->d_phi);
+    rc = vcuda(cudaGetLastError(), "direct Poisson solve");
+    if (rc) return rc;
+    return launch_poisson(v, 4, s);
+  }
   if (v->guess == HD_VP_GUESS_ZERO) {
     int rc = vcuda(cudaMemsetAsync(v->d_phi, 0, sizeof(double) * nx, s), "zero guess");
     if (rc) return rc;
@@ -1413,6 +1549,8 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
     return vfail(HD_ERR_INVALID, "hd_vp_create: unknown preconditioner");
   if (d.learn_fit != HD_VP_FIT_LEAST_SQUARES && d.learn_fit != HD_VP_FIT_ADAM)
     return vfail(HD_ERR_INVALID, "hd_vp_create: unknown learned-guess fit");
+  if (d.poisson_solver != HD_VP_SOLVER_CG && d.poisson_solver != HD_VP_SOLVER_DIRECT)
+    return vfail(HD_ERR_INVALID, "hd_vp_create: unknown Poisson solver");
   if (d.learn_fit == HD_VP_FIT_LEAST_SQUARES &&
       (d.learn_rank < 0 || d.learn_rank > hd::kLsMax || d.learn_history < 0 ||
        (d.learn_rank > 0 && d.learn_history >= d.learn_rank)))
@@ -1601,7 +1739,10 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
     if (e == cudaSuccess) e = cudaMemset(v->d_E, 0, sizeof(double) * nx * g.dx);
     if (e != cudaSuccess) { vp_free(v); return vcuda(e, "hd_vp_create: init"); }
   }
-  if (d.cg_precond == HD_VP_PRECOND_BLOCK_JACOBI) {
+  if (d.poisson_solver == HD_VP_SOLVER_DIRECT) {
+    const int rc = build_direct(v);
+    if (rc) { vp_free(v); return rc; }
+  } else if (d.cg_precond == HD_VP_PRECOND_BLOCK_JACOBI) {
     const int rc = build_block_jacobi(v);
     if (rc) { vp_free(v); return rc; }
   }

@@ -58,6 +58,9 @@ class VlasovPoissonParameters:
     cg_precond: str = "block_jacobi"  # "none" or "block_jacobi" (x-cell diagonal blocks of the SIPG matrix)
     learn_fit: str = "least_squares"  # or "adam" (hd_vp_learn_fit)
     quadrature: str = "gauss_lobatto"  # or "gauss" (n_points = degree + 1, the reference's non-collocation runs)
+    # "cg", or "direct": the SIPG matrix's pseudo-inverse kept in HBM, one matrix-vector product per solve
+    # (x-spaces up to 8192 DoFs; guess and preconditioner unused)
+    poisson_solver: str = "cg"
 
     def c(self) -> _lib.hd_vp_desc:
         d = _lib.hd_vp_desc()
@@ -80,6 +83,7 @@ class VlasovPoissonParameters:
             self.cg_precond]
         d.learn_fit = {"least_squares": _lib.HD_VP_FIT_LEAST_SQUARES, "adam": _lib.HD_VP_FIT_ADAM}[self.learn_fit]
         d.quadrature = {"gauss_lobatto": _lib.HD_QUAD_GAUSS_LOBATTO, "gauss": _lib.HD_QUAD_GAUSS}[self.quadrature]
+        d.poisson_solver = {"cg": _lib.HD_VP_SOLVER_CG, "direct": _lib.HD_VP_SOLVER_DIRECT}[self.poisson_solver]
         return d
 
 

@@ -401,6 +401,16 @@ enum hd_vp_learn_fit { HD_VP_FIT_LEAST_SQUARES = 0, HD_VP_FIT_ADAM = 1 };
  * error that FP32 round-off in the density carries into the right-hand side. */
 enum hd_vp_precond { HD_VP_PRECOND_NONE = 0, HD_VP_PRECOND_BLOCK_JACOBI = 1 };
 
+/* Solver of the x-space Poisson problem.  CG (the reference's solver, with
+ * the initial guess and preconditioner above) or, for x-spaces of up to 8192
+ * DoFs, DIRECT: the fixed SIPG matrix's pseudo-inverse (on the mean-free
+ * right-hand sides the problem has) is computed once at creation, on the
+ * device by Gauss-Jordan elimination of A + beta 1 1^T, and kept in HBM
+ * (8 n^2 bytes: 134 MB for 16^2 x-cells of degree 3); every solve is then one
+ * dense matrix-vector product.  The guess and preconditioner fields are
+ * ignored, and the CG statistics count solves with zero iterations. */
+enum hd_vp_solver { HD_VP_SOLVER_CG = 0, HD_VP_SOLVER_DIRECT = 1 };
+
 typedef struct hd_vp_desc {
   int dim_x, dim_v, degree, dtype;
   int cells_x[3], cells_v[3];
@@ -426,6 +436,7 @@ typedef struct hd_vp_desc {
                            integral at the Gauss points as the reference's
                            non-collocation runs; up to 3x+3v degree 3 in
                            FP64; FP32x2 arithmetic refused)                  */
+  int poisson_solver;   /* enum hd_vp_solver (0: CG)                          */
 } hd_vp_desc;
 
 typedef struct hd_vp hd_vp;

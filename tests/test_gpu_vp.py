@@ -23,14 +23,14 @@ if torch.cuda.is_available():
 
 
 def _setup(dim_x, degree, cx, cv, dtype="f64", guess="previous", cg_tol=1e-12, rhs_relative=False,
-           cg_precond="block_jacobi", learn_fit="least_squares", quadrature="gauss_lobatto"):
+           cg_precond="block_jacobi", learn_fit="least_squares", quadrature="gauss_lobatto", poisson_solver="cg"):
     D = 2 * dim_x
     lo = [0.0] * dim_x + [-6.0] * dim_x
     hi = [4 * math.pi] * dim_x + [6.0] * dim_x
     params = V.VlasovPoissonParameters(dim_x, degree, [cx] * dim_x, [cv] * dim_x, lo[:dim_x], hi[:dim_x],
                                        lo[dim_x:], hi[dim_x:], dtype=dtype, cg_tol=cg_tol, guess=guess,
                                        cg_rhs_relative=rhs_relative, cg_precond=cg_precond, learn_fit=learn_fit,
-                                       quadrature=quadrature)
+                                       quadrature=quadrature, poisson_solver=poisson_solver)
     prob = O.Problem(dim_x, dim_x, degree, [cx] * dim_x + [cv] * dim_x, lo, hi, [1.0] * dim_x + [6.0] * dim_x,
                      collocation=quadrature == "gauss_lobatto")
     assert len(lo) == D
@@ -431,3 +431,49 @@ def test_block_jacobi_preconditioner_same_potential_fewer_iterations(dim_x, degr
         assert out["block_jacobi"][1] <= out["none"][1], out
     else:
         assert out["block_jacobi"][1] < out["none"][1], out
+
+
+@pytest.mark.parametrize("dim_x,degree,cx,cv,quadrature", [(1, 3, 8, 8, "gauss_lobatto"), (2, 3, 4, 4, "gauss_lobatto"),
+                                                           (2, 2, 3, 5, "gauss_lobatto"), (2, 3, 4, 4, "gauss"),
+                                                           (3, 2, 2, 2, "gauss_lobatto")])
+def test_direct_poisson_solve_matches_cg(dim_x, degree, cx, cv, quadrature):
+    """The direct solve (the SIPG matrix's pseudo-inverse, formed once by Gauss-Jordan elimination on the
+    device) solves the oracle's system to round-off, gives the CG potential (CG to 1e-13) and field, the
+    potential mean-free, with zero CG iterations counted per solve."""
+    out = {}
+    for solver in ("cg", "direct"):
+        op, prob = _setup(dim_x, degree, cx, cv, guess="zero", cg_tol=1e-13, rhs_relative=True,
+                          quadrature=quadrature, poisson_solver=solver)
+        f = op.initialize_dof_vector()
+        op.interpolate(V.perturbed_maxwellian(dim_x, eps=0.05, perturbed_dims=tuple(range(dim_x))), f)
+        noise = np.random.default_rng(8).standard_normal(f.numel()) * 1e-3
+        f += torch.tensor(noise, dtype=f.dtype, device="cuda")
+        op.solve_field(f)
+        rho, phi, E = (t.cpu().numpy() for t in op.fields())
+        rhs = O.poisson_rhs(prob, rho)
+        assert np.linalg.norm(O.poisson_apply(prob, phi) - rhs) <= 1e-11 * np.linalg.norm(rhs)
+        st = op.cg_stats()
+        out[solver] = (phi - phi.mean(), E, st)
+    assert _rel(out["direct"][0], out["cg"][0]) <= 1e-10
+    assert _rel(out["direct"][1], out["cg"][1]) <= 1e-10
+    assert out["direct"][2]["solves"] == 1 and out["direct"][2]["last_iterations"] == 0
+    assert out["cg"][2]["last_iterations"] > 0
+
+
+def test_direct_poisson_solve_steps_and_limits():
+    """Fused rk45 steps with the direct solve give the CG run's solution and field energy (CG to 1e-13,
+    FP64 and FP32 storage); x-spaces above 8192 DoFs are refused."""
+    for dtype, tol in (("f64", 1e-12), ("f32", 2e-6)):
+        res = {}
+        for solver in ("cg", "direct"):
+            op, _ = _setup(2, 3, 4, 4, dtype=dtype, guess="zero", cg_tol=1e-13, rhs_relative=True,
+                           poisson_solver=solver)
+            f = op.initialize_dof_vector()
+            op.interpolate(V.perturbed_maxwellian(2, eps=0.05, perturbed_dims=(0, 1)), f)
+            hx, hv = 4 * math.pi / 4, 12.0 / 4
+            _run_steps(op, f, 3, 0.05 * min(hx, hv / 6.0) / 3 ** 1.5)
+            res[solver] = (f.double().cpu().numpy(), op.diagnostics(f))
+        assert _rel(res["direct"][0], res["cg"][0]) <= tol
+        assert _rel(res["direct"][1][:2], res["cg"][1][:2]) <= tol
+    with pytest.raises(V.HdError):
+        _setup(3, 3, 6, 2, poisson_solver="direct")  # 6^3 x-cells of 64 DoFs: 13,824 x-DoFs
