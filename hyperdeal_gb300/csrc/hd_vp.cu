@@ -793,14 +793,19 @@ __global__ void dense_gemv(long long n, const double* __restrict__ M, const doub
   const int lane = threadIdx.x & 31;
   if (row >= n) return;  // (whole warps)
   const double* r = M + row * n;
-  double s0 = 0.0, s1 = 0.0;
+  // eight independent partial sums: eight 256-byte row loads of the warp in flight
+  double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   long long j = lane;
-  for (; j + 32 < n; j += 64) {
-    s0 = fma(__ldg(r + j), __ldg(b + j), s0);
-    s1 = fma(__ldg(r + j + 32), __ldg(b + j + 32), s1);
+  for (; j + 7 * 32 < n; j += 8 * 32) {
+    double m[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) m[u] = __ldcs(r + j + 32 * u);  // streamed: read once per solve
+#pragma unroll
+    for (int u = 0; u < 8; ++u) acc[u] = fma(m[u], __ldg(b + j + 32 * u), acc[u]);
   }
-  if (j < n) s0 = fma(__ldg(r + j), __ldg(b + j), s0);
-  double s = s0 + s1;
+  double tail = 0.0;
+  for (; j < n; j += 32) tail = fma(__ldcs(r + j), __ldg(b + j), tail);
+  double s = (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]))) + tail;
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) x[row] = s;
 }

@@ -253,7 +253,7 @@ def learn_loss_grad(W1: torch.Tensor, W2: torch.Tensor, X: torch.Tensor, Y: torc
 def run_hyperrectangle(dim_x: int = 2, degree: int = 3, cells_x: int = 4, cells_v: int = 4, dtype: str = "f64",
                        final_time: float = 0.5, time_step: float = 0.1, cfl: float = 0.05, tick: float = 0.1,
                        rk: str = "rk45", cg_tol: float = 1e-12, guess: str = "previous",
-                       quadrature: str = "gauss_lobatto"):
+                       quadrature: str = "gauss_lobatto", poisson_solver: str = "cg"):
     """The reference's Vlasov-Poisson application on its hyperrectangle case: x in [0, 4 pi]^dim_x,
     v in [-6, 6]^dim_x, periodic, the time-step rule with transport velocity (1, .., 6, ..)
     (examples/vlasov_poisson/cases/hyperrectangle.h, application.h:345-602).  Returns the
@@ -261,7 +261,8 @@ def run_hyperrectangle(dim_x: int = 2, degree: int = 3, cells_x: int = 4, cells_
     and the operator."""
     params = VlasovPoissonParameters(dim_x, degree, [cells_x] * dim_x, [cells_v] * dim_x, [0.0] * dim_x,
                                      [4 * math.pi] * dim_x, [-6.0] * dim_x, [6.0] * dim_x, dtype=dtype,
-                                     cg_tol=cg_tol, guess=guess, quadrature=quadrature)
+                                     cg_tol=cg_tol, guess=guess, quadrature=quadrature,
+                                     poisson_solver=poisson_solver)
     op = VlasovPoissonOperation(params)
     sol = op.initialize_dof_vector()
     op.interpolate(perturbed_maxwellian(dim_x), sol)

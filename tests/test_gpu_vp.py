@@ -101,18 +101,19 @@ def test_apply_matches_oracle(dim_x, degree, cx, cv, dtype, quadrature):
     assert _rel(dst2.cpu().numpy(), dst.cpu().numpy()) <= (1e-10 if dtype == "f64" else 1e-5)
 
 
-def test_gauss_golden_vp_2D_2D_k3_hyperrectangle_01():
+@pytest.mark.parametrize("poisson_solver", ["cg", "direct"])
+def test_gauss_golden_vp_2D_2D_k3_hyperrectangle_01(poisson_solver):
     """The reference's Vlasov-Poisson golden examples/vlasov_poisson/tests/vp_2D_2D_k3.hyperrectangle_01
     (2x2v, k = 3, 4 cells per direction, Gauss quadrature with k + 1 points, rk45 to t = 0.5) replayed
     on the GPU through the C ABI: every diagnostics row within numdiff's tolerances, mass, L2 norm
     and kinetic energy to 1e-12, the field energy to 1e-7 (the reference solves Poisson with
-    multigrid to a 1e-4 reduction)."""
+    multigrid to a 1e-4 reduction) -- with CG and with the direct solve."""
     from test_oracle_golden import GOLD, numdiff_equal
     case = GOLD["vlasov_poisson"][0]
     assert case["name"] == "vp_2D_2D_k3.hyperrectangle_01" and not case["collocation"]
     rows, op = V.run_hyperrectangle(case["dim_x"], case["degree"], case["cells_x"], case["cells_v"],
                                     final_time=case["final_time"], time_step=case["time_step"], cfl=case["cfl"],
-                                    quadrature="gauss")
+                                    quadrature="gauss", poisson_solver=poisson_solver)
     ref = case["rows"]
     assert len(rows) == len(ref)
     dx = case["dim_x"]
