@@ -29,7 +29,8 @@ namespace hd {
 
 namespace {
 
-constexpr int kMomChunk = 16;   // v-cells summed by one block of the moment kernel
+constexpr int kMomChunk = 16;   // v-cells whose values a thread of the moment kernel loads together
+constexpr int kMomBlockChunks = 4;  // chunks summed by one block (64 v-cells)
 constexpr int kCgThreads = 64;  // small blocks: the x-space system is small, spread it over many SMs
 constexpr int kLsMax = 16;      // basis columns of the least-squares learned guess (upper bound)
 constexpr int kLsRed = kLsMax + 1;
@@ -43,59 +44,71 @@ struct VpStats {
 };
 
 // ---------------------------------------------------------------- moments
-// partial[chunk][gx*NCx + ix] = sum over the chunk's v-cells and the v-nodes of f * JxW_v
-// (the chunk's kMomChunk values of a node are loaded independently before they are summed)
+// sum of f over the kMomChunk v-cells gv0.. at one node of x-cell gxc (the
+// values are loaded independently before they are summed)
+template <typename T>
+__device__ __forceinline__ double moment_chunk_sum(const VpGeom& g, const T* __restrict__ f, long long gxc,
+                                                   long long gv0, int node) {
+  T vals[kMomChunk];
+#pragma unroll
+  for (int k = 0; k < kMomChunk; ++k) {
+    const long long gv = gv0 + k;
+    const long long gvc = gv < g.ncv ? gv : g.ncv - 1;  // valid address even if loaded unconditionally
+    vals[k] = gv < g.ncv ? __ldg(f + (gxc + g.ncx * gvc) * g.NC + node) : T(0);
+  }
+  if constexpr (sizeof(T) == 4) {
+    // FP32 storage: compensated pairwise sum on the FP32 pipe (the FP64 pipe
+    // is the scarce resource here): every pairwise add is Knuth's TwoSum,
+    // whose rounding error is kept in a second float and summed alongside,
+    // so the chunk sum hi + lo carries about twice FP32's precision before
+    // it is widened to FP64 (Ogita, Rump, Oishi, SIAM J. Sci. Comput. 2005)
+    float hi[kMomChunk], lo[kMomChunk];
+#pragma unroll
+    for (int k = 0; k < kMomChunk; ++k) {
+      hi[k] = vals[k];
+      lo[k] = 0.f;
+    }
+#pragma unroll
+    for (int w = kMomChunk / 2; w > 0; w /= 2)
+#pragma unroll
+      for (int k = 0; k < w; ++k) {
+        float sum, err;
+        two_sum(hi[k], hi[k + w], sum, err);
+        hi[k] = sum;
+        lo[k] = __fadd_rn(__fadd_rn(lo[k], lo[k + w]), err);
+      }
+    return x2_to_double(f32x2{hi[0], lo[0]});
+  } else {
+    // FP64 storage: summed pairwise in FP64
+    T h[kMomChunk];
+#pragma unroll
+    for (int k = 0; k < kMomChunk; ++k) h[k] = vals[k];
+#pragma unroll
+    for (int w = kMomChunk / 2; w > 0; w /= 2)
+#pragma unroll
+      for (int k = 0; k < w; ++k) h[k] += h[k + w];
+    return double(h[0]);
+  }
+}
+
+// partial[block][gx*NCx + ix] = sum over the block's kMomBlockChunks chunks of
+// v-cells and the v-nodes of f * JxW_v (the chunk sums of a node added in
+// FP64, in order)
 template <typename T>
 __global__ void moment_partials(VpGeom g, const T* __restrict__ f, const double* __restrict__ wv,
                                 double* __restrict__ partial) {
   extern __shared__ double sh[];
   const long long gxc = blockIdx.x;  // x-cell
   const int chunk = blockIdx.y;
-  const long long gv0 = (long long)chunk * kMomChunk;
   const int NCv = g.NC / g.NCx;
   for (int node = threadIdx.x; node < g.NC; node += blockDim.x) {
-    T vals[kMomChunk];
-#pragma unroll
-    for (int k = 0; k < kMomChunk; ++k) {
-      const long long gv = gv0 + k;
-      const long long gvc = gv < g.ncv ? gv : g.ncv - 1;  // valid address even if loaded unconditionally
-      vals[k] = gv < g.ncv ? __ldg(f + (gxc + g.ncx * gvc) * g.NC + node) : T(0);
+    double node_sum = 0.0;
+    for (int cb = 0; cb < kMomBlockChunks; ++cb) {
+      const long long gv0 = ((long long)chunk * kMomBlockChunks + cb) * kMomChunk;
+      if (gv0 >= g.ncv) break;
+      node_sum += moment_chunk_sum(g, f, gxc, gv0, node);
     }
-    double chunk_sum;
-    if constexpr (sizeof(T) == 4) {
-      // FP32 storage: compensated pairwise sum on the FP32 pipe (the FP64 pipe
-      // is the scarce resource here): every pairwise add is Knuth's TwoSum,
-      // whose rounding error is kept in a second float and summed alongside,
-      // so the chunk sum hi + lo carries about twice FP32's precision before
-      // it is widened to FP64 (Ogita, Rump, Oishi, SIAM J. Sci. Comput. 2005)
-      float hi[kMomChunk], lo[kMomChunk];
-#pragma unroll
-      for (int k = 0; k < kMomChunk; ++k) {
-        hi[k] = vals[k];
-        lo[k] = 0.f;
-      }
-#pragma unroll
-      for (int w = kMomChunk / 2; w > 0; w /= 2)
-#pragma unroll
-        for (int k = 0; k < w; ++k) {
-          float sum, err;
-          two_sum(hi[k], hi[k + w], sum, err);
-          hi[k] = sum;
-          lo[k] = __fadd_rn(__fadd_rn(lo[k], lo[k + w]), err);
-        }
-      chunk_sum = x2_to_double(f32x2{hi[0], lo[0]});
-    } else {
-      // FP64 storage: summed pairwise in FP64
-      T h[kMomChunk];
-#pragma unroll
-      for (int k = 0; k < kMomChunk; ++k) h[k] = vals[k];
-#pragma unroll
-      for (int w = kMomChunk / 2; w > 0; w /= 2)
-#pragma unroll
-        for (int k = 0; k < w; ++k) h[k] += h[k + w];
-      chunk_sum = double(h[0]);
-    }
-    sh[node] = chunk_sum * wv[node / g.NCx];
+    sh[node] = node_sum * wv[node / g.NCx];
   }
   __syncthreads();
   for (int ix = threadIdx.x; ix < g.NCx; ix += blockDim.x) {
@@ -1655,7 +1668,7 @@ int hd_vp_create(const hd_vp_desc* desc, hd_vp** out) {
     if (d.cells_v[i] > hd::kVpMaxCellsV) { delete v; return vfail(HD_ERR_UNSUPPORTED, "hd_vp_create: at most 64 v-cells per direction"); }
   // device buffers
   const int NCv = g.NC / g.NCx;
-  v->nchunks = int((g.ncv + hd::kMomChunk - 1) / hd::kMomChunk);
+  v->nchunks = int((g.ncv + hd::kMomChunk * hd::kMomBlockChunks - 1) / (hd::kMomChunk * hd::kMomBlockChunks));
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
