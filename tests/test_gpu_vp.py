@@ -462,13 +462,15 @@ def test_direct_poisson_solve_matches_cg(dim_x, degree, cx, cv, quadrature):
 
 
 def test_direct_poisson_solve_steps_and_limits():
-    """Fused rk45 steps with the direct solve give the CG run's solution and field energy (CG to 1e-13,
-    FP64 and FP32 storage); x-spaces above 8192 DoFs are refused."""
-    for dtype, tol in (("f64", 1e-12), ("f32", 2e-6)):
+    """Fused rk45 steps with the direct solve give the CG run's solution and field energy (CG to 1e-13;
+    FP64 storage with native and FP32x2 advection, FP32 storage); x-spaces above 8192 DoFs are refused."""
+    for dtype, tol in (("f64", 1e-12), ("f64x", 1e-12), ("f32", 2e-6)):
         res = {}
         for solver in ("cg", "direct"):
-            op, _ = _setup(2, 3, 4, 4, dtype=dtype, guess="zero", cg_tol=1e-13, rhs_relative=True,
+            op, _ = _setup(2, 3, 4, 4, dtype=dtype[:3], guess="zero", cg_tol=1e-13, rhs_relative=True,
                            poisson_solver=solver)
+            if dtype == "f64x":
+                op.set_arithmetic("fp32x2")
             f = op.initialize_dof_vector()
             op.interpolate(V.perturbed_maxwellian(2, eps=0.05, perturbed_dims=(0, 1)), f)
             hx, hv = 4 * math.pi / 4, 12.0 / 4
