@@ -497,6 +497,26 @@ def run_adv2d(args):
     ms_graph = e0.elapsed_time(e1) / nsteps
     _, err_graph = A.VectorTools.norm_and_error(op, exact, ug, nsteps * dt)
     n = op.n_dofs
+    cpu = None
+    if not args.no_cpu:
+        # the oracle (CPU restatement, FP64) on the same problem and steps, all host threads
+        import numpy as np
+
+        from oracle import oracle as O
+        O.build()
+        threads = os.cpu_count()
+        prob = O.Problem(1, 1, DEGREE, [32, 32], [0.0, 0.0], [1.0, 1.0], vel, n_threads=threads)
+        fo = O.make_func(2, 1.0, omega=[2 * math.pi] * 2, speed=[0.0, 0.0])
+        uo = O.interpolate(prob, fo)
+        Ko, To = np.zeros_like(uo), np.zeros_like(uo)
+        c0 = time.perf_counter()
+        for s_ in range(nsteps):
+            O.lsrk_step(prob, "rk45", uo, s_ * dt, dt, Ko, To)
+        cpu_s = (time.perf_counter() - c0) / nsteps
+        diff = float(np.abs(uo - ug.cpu().numpy()).max() / np.abs(uo).max())
+        cpu = {"value": round(n * N_STAGES / cpu_s / 1e9, 4), "unit": "GDoF/s", "cores": threads, "kind": "port",
+               "ms_per_step": round(cpu_s * 1e3, 4), "max_rel_diff_gpu_vs_oracle": diff,
+               "sample": "the same 100 rk45 steps by the oracle (CPU restatement, FP64, OpenMP)"}
     out = {"metric": "advection GDoF/s (2D k=3, 32 x 32, FP64) over 100 rk45 steps", "value":
            round(n * N_STAGES / (ms_graph / 1e3) / 1e9, 3), "unit": "GDoF/s", "n_gpus": 1, "steps": nsteps,
            "warmup": args.warmup, "ms_per_step": round(ms_graph, 5), "higher_is_better": True, "scaling": "weak",
@@ -507,7 +527,7 @@ def run_adv2d(args):
            "graph_replay": {"ms_per_step": round(ms_graph, 5), "error_vs_exact": err_graph},
            "per_step_launches": {"ms_per_step": round(ms_plain, 5), "error_vs_exact": err_plain,
                                  "gdof_per_s": round(n * N_STAGES / (ms_plain / 1e3) / 1e9, 3)},
-           "gpu_launches": N_STAGES * nsteps + 1}
+           "cpu_baseline": cpu, "gpu_launches": N_STAGES * nsteps + 1}
     print(json.dumps(out))
     return 0
 
