@@ -853,19 +853,28 @@ struct EclStaging {
 // GH: the launch may read a ghost region (P.ghost != nullptr; parts of a
 // partitioned mesh only) -- the kernels without it keep the plain neighbour
 // addressing of an unpartitioned vector
+// 6D FP32x2: one staging buffer (the next block's input prefetched into L2
+// instead of staged) and three CTAs per SM at 85 registers
+template <int D, int N, typename T, typename A>
+struct EclX2Single {
+  static constexpr bool value = std::is_same_v<A, f32x2> && D == 6;
+};
+
 template <int D, int N, typename T, int MODE, typename A = T, bool GH = false>
 __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
-                                  std::is_same_v<A, f32x2> ? 2 : EclShape<D, N, T>::MINB)
+                                  std::is_same_v<A, f32x2> ? (EclX2Single<D, N, T, A>::value ? 3 : 2)
+                                                           : EclShape<D, N, T>::MINB)
     ecl_kernel(const __grid_constant__ EclParams<T> P) {
   using S = EclShape<D, N, T>;
   constexpr int NC = S::NC, TPC = S::TPC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int cpb = P.cpb;
   constexpr bool SU = EclStaging<D, N, T, MODE, A>::STAGE_U;
+  constexpr bool SINGLE = EclX2Single<D, N, T, A>::value;
   const long long bufe = ecl_buffer_elems<D, N, T>(cpb);
   T* const s_in0 = reinterpret_cast<T*>(smem_raw);
   T* const s_in1 = s_in0 + bufe;
-  T* const s_o = s_in0 + 2 * bufe;
+  T* const s_o = s_in0 + (SINGLE ? 1 : 2) * bufe;
   T* const s_u0 = s_in0 + 3 * bufe;  // (stage modes with STAGE_U only)
   T* const s_u1 = s_in0 + 4 * bufe;
   const int tid = threadIdx.x, nthr = blockDim.x;
@@ -888,6 +897,28 @@ __global__ void __launch_bounds__(EclShape<D, N, T>::THREADS,
                          unsigned(bytes - off < 16384 ? bytes - off : 16384));
     }
   };
+  if constexpr (SINGLE) {
+    for (long long b = blockIdx.x; b < nblk; b += gridDim.x) {
+      stage(s_in0, nullptr, b);
+      cp_async_commit();
+      // the next block's input into L2 meanwhile (bulk prefetches of up to 16 KiB)
+      const long long nb = b + gridDim.x;
+      if (nb < nblk) {
+        const long long c0 = P.c_lo + nb * cpb;
+        const long long ncell = (P.c_hi - c0) < cpb ? (P.c_hi - c0) : cpb;
+        const long long bytes = ncell * NC * (long long)sizeof(T);
+        const long long off = (long long)tid * 16384;
+        if (off < bytes)
+          prefetch_l2_bulk(reinterpret_cast<const char*>(P.tin + c0 * NC) + off,
+                           unsigned(bytes - off < 16384 ? bytes - off : 16384));
+      }
+      cp_async_wait<0>();
+      __syncthreads();
+      ecl_block_x2<D, N, MODE, GH, true>(P, P.c_lo + b * cpb, lc, tl, s_in0, s_o, nullptr);
+      __syncthreads();  // the buffer and s_o are free for the next block
+    }
+    return;
+  }
   long long b = blockIdx.x;
   if (b < nblk) stage(s_in0, s_u0, b);
   cp_async_commit();
@@ -988,7 +1019,8 @@ cudaError_t launch_ecl(const EclParams<T>& P0, int mode, cudaStream_t stream) {
     EclParams<T> P = P0;
     if (P.cpb < 1 || P.cpb > S::CPB) P.cpb = ecl_default_cpb<D, N, T>();
     if (mode < kApply || mode > kStageLast) return cudaErrorInvalidValue;
-    const int nbuf = mode == kStageMid ? EclStaging<D, N, T, kStageMid, A>::NBUF
+    const int nbuf = EclX2Single<D, N, T, A>::value ? 2
+                     : mode == kStageMid ? EclStaging<D, N, T, kStageMid, A>::NBUF
                      : mode == kStageLast ? EclStaging<D, N, T, kStageLast, A>::NBUF : 3;
     // the staged tiles of the largest shape may not fit five times: shrink the tile
     while (P.cpb > 1 && size_t(nbuf * ecl_buffer_elems<D, N, T>(P.cpb)) * sizeof(T) > 220 * 1024) --P.cpb;
